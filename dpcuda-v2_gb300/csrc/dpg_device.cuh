@@ -1,0 +1,220 @@
+// dpg_device.cuh -- device-resident system layout shared by the kernels.
+//
+// One system lives in HBM as:
+//   params  (DevParams)  written by the host when the box / neighbour setup changes
+//   view    (DevView)    pointers to the CURRENT buffers; the cell reorder writes the
+//                        gathered data into the alternate buffers and swaps the
+//                        pointers here on the device, so no host round trip (and no
+//                        CUDA-graph re-capture) is needed when particles are re-sorted
+//   state   (DevState)   scalars owned by the device: displacement maxima, rebuild
+//                        decision, FIRE state, reduction results, stop flags
+// Particle data are SoA over particles with x,y interleaved as double2 so each
+// particle's position / velocity / force is one coalesced 16-byte access.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace dpg {
+
+constexpr int kTPB = 256;      // threads per block for per-particle kernels
+constexpr int kScanTPB = 1024; // single-block cell-count scan
+
+enum StopBits : int {
+    kDone = 1,       // loop finished (converged, stopped or out of steps)
+    kOverflow = 2,   // neighbour count exceeded capacity: halt until the host grows it
+    kError = 4,
+};
+
+struct DevParams {
+    int n;
+    int method;   // DPG_NEIGH_*
+    int ncd;      // cells per dimension
+    int ncells;
+    int cap;      // neighbour capacity per particle
+    int precision;
+    double box[2];
+    double e_c, n_c;
+    double cutoff2;     // neighbour cutoff squared
+    double cell_size;
+    double nthr2, cthr2;  // rebuild thresholds (squared)
+    double inv_area;
+};
+
+struct DevView {
+    double2 *pos, *vel, *frc;
+    double *rad, *mass;
+    int *sidx;  // static index of the particle in each slot
+    double2 *pos_t, *vel_t, *frc_t;
+    double *rad_t, *mass_t;
+    int *sidx_t;
+    double2 *m1, *m2, *m1_t, *m2_t;  // Adam moments and their swap twins
+    int *nbr;                        // neighbour list, column-major [cap][n]
+};
+
+struct DevState {
+    double max_nd2, max_cd2;  // max squared displacement since the last list / cell build
+    int rebuild;              // 0 none, 1 neighbour list, 2 cell list + neighbour list
+    int max_count;
+    int flags;                // StopBits
+    int fire_uphill;          // apply the FIRE "uphill" branch at the next move
+    long long n_rebuilds, n_cell_rebuilds;
+    // results of the last reductions
+    double pe, ke, power, fmax2, fsum_x, fsum_y;
+    double stress[4];
+    double contacts;
+    // FIRE (include/integrator/fire.h:15-35)
+    double f_alpha, f_alpha0, f_dt, f_dtmax, f_dtmin;
+    long long f_ngood, f_nbad;
+    int f_stopped;
+    int f_converged;
+    // minimizeFire loop (src/routines/minimization.cu:75-112)
+    double last_avg_pe, pe_target, pe_diff_target, fmax_target, dof;
+    long long iter, max_steps, result_step;
+    long long nve_steps_done;
+    // loop guard: the WHILE body ends with k_loop_guard, which stops the loop
+    // when a flag is raised or after guard_limit iterations, whatever else happens
+    long long guard, guard_limit;
+    // conditional-node handles of the running graph (0 outside a graph)
+    unsigned long long h_loop, h_rb;
+    unsigned int ticket;  // last-block-done counter
+    unsigned int pad;
+};
+
+struct DevScratch {
+    double2 *pos_n, *pos_c;  // positions at the last neighbour / cell build
+    double *pe;
+    int *count;              // neighbour counts
+    int *cell_raw;           // cell of each particle before the sort
+    int *cell_of;            // cell of each particle in sorted order
+    int *cell_cnt, *cell_cur, *cell_start, *perm;
+    double *partials;        // per-block reduction partials
+    int max_blocks;
+    // snapshot (setLastState)
+    double2 *s_pos, *s_vel, *s_frc;
+    double *s_rad, *s_mass;
+    int *s_sidx;
+    double s_box[2];
+};
+
+struct DevSys {
+    DevParams p;
+    DevView v;
+    DevState s;
+    DevScratch w;
+};
+
+// ---- shared arithmetic (reference order, see oracle/dpg_oracle.c) ----------
+
+// minimum image: include/particles/base/kernels.cuh:65-72
+__device__ __forceinline__ double pbc_dist(double a, double b, double L) {
+    double d = a - b;
+    return d - L * round(d / L);
+}
+
+// include/particles/base/kernels.cuh:53-55
+__device__ __forceinline__ int pmod(int a, int b) { return (a % b + b) % b; }
+
+// getPBCCellIndex: include/particles/base/kernels.cuh:285-301
+__device__ __forceinline__ int cell_coord(double p, double cs, int ncd) {
+    long long idx = __double2ll_rd(p / cs);
+    long long m = idx % ncd;
+    return (int)(idx >= 0 ? m : (m + ncd) % ncd);
+}
+
+// ---- block reductions with a deterministic order ---------------------------
+
+template <int K>
+__device__ __forceinline__ void warp_sum(double (&v)[K]) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+        for (int k = 0; k < K; k++) v[k] += __shfl_down_sync(0xffffffffu, v[k], off);
+}
+
+template <int K>
+__device__ __forceinline__ void warp_max(double (&v)[K]) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+        for (int k = 0; k < K; k++) v[k] = fmax(v[k], __shfl_down_sync(0xffffffffu, v[k], off));
+}
+
+// Reduce K values over the block (ops[k]: 0 = sum, 1 = max).  Thread 0 gets the result.
+template <int K>
+__device__ __forceinline__ void block_reduce(double (&v)[K], const int (&ops)[K], double *sm) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    double s[K], m[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) { s[k] = v[k]; m[k] = v[k]; }
+    warp_sum(s);
+    warp_max(m);
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < K; k++) sm[wid * K + k] = ops[k] ? m[k] : s[k];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            double a = sm[k];
+            for (int w = 1; w < nw; w++) a = ops[k] ? fmax(a, sm[w * K + k]) : a + sm[w * K + k];
+            v[k] = a;
+        }
+    }
+    __syncthreads();
+}
+
+// Grid-wide reduction by "last block done": every block publishes its partials,
+// the last block to arrive reduces them in a fixed order.  Returns true on
+// thread 0 of the last block, with the totals in v.  All threads of every
+// block must call it.
+template <int K>
+__device__ bool grid_reduce(double (&v)[K], const int (&ops)[K], DevSys *ds) {
+    __shared__ double sm[32 * K];
+    __shared__ int am_last;
+    block_reduce<K>(v, ops, sm);
+    const int G = gridDim.x;
+    double *part = ds->w.partials;
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < K; k++) part[k * G + blockIdx.x] = v[k];
+        __threadfence();
+        unsigned t = atomicAdd(&ds->s.ticket, 1u);
+        am_last = (t == (unsigned)G - 1);
+    }
+    __syncthreads();
+    if (!am_last) return false;
+    __threadfence();
+    double a[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) a[k] = ops[k] ? -INFINITY : 0.0;
+    for (int b = threadIdx.x; b < G; b += blockDim.x)
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            double x = __ldcg(&part[k * G + b]);
+            a[k] = ops[k] ? fmax(a[k], x) : a[k] + x;
+        }
+    block_reduce<K>(a, ops, sm);
+    if (threadIdx.x == 0) {
+        ds->s.ticket = 0;
+#pragma unroll
+        for (int k = 0; k < K; k++) v[k] = a[k];
+        return true;
+    }
+    return false;
+}
+
+// Same arrival protocol with no data: true on thread 0 of the last block.
+__device__ __forceinline__ bool grid_last_block(DevSys *ds) {
+    __shared__ int am_last;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        unsigned t = atomicAdd(&ds->s.ticket, 1u);
+        am_last = (t == gridDim.x - 1);
+        if (am_last) ds->s.ticket = 0;
+    }
+    __syncthreads();
+    return am_last && threadIdx.x == 0;
+}
+
+}  // namespace dpg

@@ -1,0 +1,130 @@
+"""Loads ``_build/libdpg.so`` and declares the C ABI signatures (include/dpg.h)."""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+from . import build as _build
+
+D = C.c_double
+I32 = C.c_int
+I64 = C.c_int64
+VP = C.c_void_p
+DP = C.POINTER(C.c_double)
+IP = C.POINTER(C.c_int)
+I32P = C.POINTER(C.c_int32)
+I64P = C.POINTER(C.c_int64)
+
+DPG_OK = 0
+STATUS_NAMES = {1: "DPG_ERR_ARG", 2: "DPG_ERR_CUDA", 3: "DPG_ERR_OVERFLOW",
+                4: "DPG_ERR_NOT_CONVERGED", 5: "DPG_ERR_STATE", 6: "DPG_ERR_TIMEOUT"}
+
+
+class DpgError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{STATUS_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Params(C.Structure):
+    _fields_ = [("n_particles", I64), ("box_x", D), ("box_y", D), ("e_c", D), ("n_c", D),
+                ("precision", I32), ("reserved", I32)]
+
+
+class NeighborConfig(C.Structure):
+    _fields_ = [("method", I32), ("cutoff_multiplier", D), ("displacement_multiplier", D),
+                ("particles_per_cell", D), ("cell_displacement_multiplier", D)]
+
+
+class NeighborInfo(C.Structure):
+    _fields_ = [("method", I32), ("capacity", I32), ("n_cells_dim", I32), ("reserved", I32),
+                ("cutoff", D), ("neighbor_threshold_sq", D), ("cell_size", D),
+                ("cell_threshold_sq", D), ("n_rebuilds", I64), ("n_cell_rebuilds", I64)]
+
+
+class FireParams(C.Structure):
+    _fields_ = [("alpha_init", D), ("dt", D), ("avg_pe_target", D), ("avg_pe_diff_target", D),
+                ("max_steps", I64), ("fmax_target", D)]
+
+
+class FireResult(C.Structure):
+    _fields_ = [("steps", I64), ("stopped", I32), ("converged", I32), ("avg_pe", D),
+                ("max_force", D), ("alpha", D), ("dt", D)]
+
+
+# name -> argtypes (all return int status unless listed in _RESTYPES)
+SIGNATURES = {
+    "dpg_create": [C.POINTER(Params), VP, C.POINTER(VP)],
+    "dpg_destroy": [VP],
+    "dpg_last_error": [],
+    "dpg_version": [],
+    "dpg_set_state": [VP, DP, DP, DP, DP, DP, DP, I32],
+    "dpg_get_state": [VP, DP, DP, DP, DP, DP, DP, DP, I32],
+    "dpg_set_forces": [VP, DP, DP, I32],
+    "dpg_set_box": [VP, D, D],
+    "dpg_get_box": [VP, DP, DP],
+    "dpg_synchronize": [VP],
+    "dpg_setup_neighbors": [VP, C.POINTER(NeighborConfig), C.POINTER(NeighborInfo)],
+    "dpg_build_neighbors": [VP],
+    "dpg_check_neighbors": [VP, IP],
+    "dpg_neighbor_info_get": [VP, C.POINTER(NeighborInfo)],
+    "dpg_get_neighbors": [VP, I32P, I32P, IP],
+    "dpg_get_cells": [VP, I64P, I64P, I64P],
+    "dpg_zero_forces": [VP],
+    "dpg_compute_forces": [VP],
+    "dpg_kick": [VP, D],
+    "dpg_drift": [VP, D],
+    "dpg_nve_steps": [VP, D, I64],
+    "dpg_power_fire": [VP, DP],
+    "dpg_mix": [VP, D],
+    "dpg_zero_velocities": [VP],
+    "dpg_fire_init": [VP, D, D],
+    "dpg_fire_step": [VP, IP],
+    "dpg_fire_get": [VP, DP, DP, I64P, I64P, IP],
+    "dpg_fire_minimize": [VP, C.POINTER(FireParams), C.POINTER(FireResult)],
+    "dpg_adam_init": [VP],
+    "dpg_adam_step": [VP, I64, D, D, D, D],
+    "dpg_adam_minimize": [VP, D, D, D, D, D, D, I64, I64P],
+    "dpg_reduce_energies": [VP, DP, DP],
+    "dpg_force_stats": [VP, DP, DP],
+    "dpg_pressure": [VP, DP, DP],
+    "dpg_contact_count": [VP, DP],
+    "dpg_packing_fraction": [VP, DP],
+    "dpg_scale_box": [VP, D],
+    "dpg_scale_to_packing_fraction": [VP, D],
+    "dpg_save_state": [VP],
+    "dpg_restore_state": [VP],
+    "dpg_profile_loop": [VP, I32, I32, D, DP, I64P],
+}
+_RESTYPES = {"dpg_last_error": C.c_char_p}
+
+_lib: C.CDLL | None = None
+
+
+def library_path() -> Path:
+    return _build.LIB
+
+
+def load_library(build_if_missing: bool = True) -> C.CDLL:
+    """Load libdpg.so (building it first when the sources are newer)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if build_if_missing:
+        _build.build()
+    path = library_path()
+    if not path.exists():
+        raise FileNotFoundError(f"{path} not built; run __graft_entry__.build()")
+    lib = C.CDLL(str(path))
+    for name, args in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = _RESTYPES.get(name, C.c_int)
+    _lib = lib
+    return lib
+
+
+def check(code: int):
+    if code != DPG_OK:
+        lib = load_library()
+        raise DpgError(code, (lib.dpg_last_error() or b"").decode())

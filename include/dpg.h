@@ -1,0 +1,229 @@
+/*
+ * dpg.h -- C ABI of the GB300-native (sm_103a) granular contact library.
+ *
+ * Drop-in boundary for the hot path of mmccraw98/dpCUDA-v2: the cell-list and
+ * Verlet neighbour build, harmonic disk contacts, and the NVE, FIRE and Adam
+ * updates, plus the stress / box-scaling / last-state pieces the jamming
+ * drivers use.  Each entry point names the reference interface it replaces
+ * (file:line in the reference tree).  Plain C types only: pointers, sizes,
+ * doubles, status codes.
+ *
+ * Conventions
+ *  - Every function returns an int status (DPG_OK = 0).  dpg_last_error()
+ *    gives a message for the calling thread's last failure.
+ *  - A handle owns its device memory and a CUDA stream; there is no global
+ *    state, so several handles may coexist.  A handle is not thread-safe.
+ *  - Arrays crossing the boundary are in STATIC order (the order the
+ *    particles were given at setup), like the reference's state files
+ *    (src/io/state_log.cu:30-32).  Internally particles are kept cell-sorted.
+ *  - `where` arguments say whether a pointer is host (DPG_HOST) or device
+ *    (DPG_DEVICE) memory.
+ *  - Arithmetic of the plain form is IEEE FP64 without FMA contraction, in the
+ *    reference's operation order: per-particle results are bit-identical to
+ *    the reference kernels given identical inputs and neighbour lists.
+ */
+#ifndef DPG_H
+#define DPG_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes --------------------------------------------------- */
+#define DPG_OK 0
+#define DPG_ERR_ARG 1          /* bad argument */
+#define DPG_ERR_CUDA 2         /* CUDA runtime error */
+#define DPG_ERR_OVERFLOW 3     /* neighbour capacity exceeded and could not grow */
+#define DPG_ERR_NOT_CONVERGED 4
+#define DPG_ERR_STATE 5        /* call out of order (e.g. forces before neighbours) */
+#define DPG_ERR_TIMEOUT 6      /* a bounded device wait ran out */
+
+#define DPG_HOST 0
+#define DPG_DEVICE 1
+
+/* neighbour methods (src/particles/base/particle.cu:237-265) */
+#define DPG_NEIGH_CELL 0
+#define DPG_NEIGH_VERLET 1
+#define DPG_NEIGH_ALL 2
+
+/* precision forms */
+#define DPG_FP64 0  /* plain all-FP64 drop-in */
+#define DPG_MIXED 1 /* FP64 cell origin + FP32 offsets, FP32 pair maths, FP64 accumulation */
+
+typedef struct dpg_system *dpg_handle;
+
+/* Particle parameters: Particle::setEnergyScale / setExponent
+ * (src/particles/base/particle.cu:729-825) and the box. */
+typedef struct {
+    int64_t n_particles;
+    double box_x, box_y;
+    double e_c; /* contact energy scale */
+    double n_c; /* contact exponent (2 = harmonic) */
+    int precision; /* DPG_FP64 or DPG_MIXED */
+    int reserved;
+} dpg_params;
+
+/* Neighbour configuration: Particle::setupNeighbors config keys
+ * (src/particles/base/particle.cu:71-100, include/particles/standard_configs.h:135-141). */
+typedef struct {
+    int method;                 /* DPG_NEIGH_* (requested; fallbacks as in the reference) */
+    double cutoff_multiplier;   /* r_c = multiplier * max diameter */
+    double displacement_multiplier;
+    double particles_per_cell;
+    double cell_displacement_multiplier;
+} dpg_neighbor_config;
+
+/* What setup chose (Particle members neighbor_cutoff, n_cells_dim, ...). */
+typedef struct {
+    int method;
+    int capacity;  /* max_neighbors_allocated */
+    int n_cells_dim;
+    int reserved;
+    double cutoff;
+    double neighbor_threshold_sq;
+    double cell_size;
+    double cell_threshold_sq;
+    int64_t n_rebuilds;
+    int64_t n_cell_rebuilds;
+} dpg_neighbor_info;
+
+/* FIRE parameters: Fire (include/integrator/fire.h:15-35) + minimizeFire
+ * (src/routines/minimization.cu:75-112).  fmax_target > 0 adds a
+ * max_i |F_i| <= fmax_target stop (not in the reference). */
+typedef struct {
+    double alpha_init;
+    double dt;
+    double avg_pe_target;
+    double avg_pe_diff_target;
+    int64_t max_steps;
+    double fmax_target;
+} dpg_fire_params;
+
+typedef struct {
+    int64_t steps;   /* loop index at exit, as minimizeFire's `step` */
+    int stopped;     /* Fire::stopped */
+    int converged;   /* left through a stop criterion (not max_steps) */
+    double avg_pe;   /* PE / N at exit */
+    double max_force;
+    double alpha, dt;
+} dpg_fire_result;
+
+/* ---- lifetime ------------------------------------------------------- */
+/* Disk::initializeFromConfig / Particle::setNumParticles + setBoxSize
+ * (src/particles/disk/disk.cu:98-170).  stream may be NULL (own stream). */
+int dpg_create(const dpg_params *p, void *cuda_stream, dpg_handle *out);
+int dpg_destroy(dpg_handle h);
+const char *dpg_last_error(void);
+int dpg_version(void);
+
+/* ---- state ---------------------------------------------------------- */
+/* Particle::setData on positions, velocities, radii, masses (static order).
+ * Any pointer may be NULL to leave that array unchanged. */
+int dpg_set_state(dpg_handle h, const double *x, const double *y, const double *vx,
+                  const double *vy, const double *radii, const double *masses, int where);
+/* Particle::getArrayData (src/particles/base/particle.cu:480-692), un-permuted
+ * to static order like the reference IO.  NULL pointers are skipped. */
+int dpg_get_state(dpg_handle h, double *x, double *y, double *vx, double *vy, double *fx,
+                  double *fy, double *pe, int where);
+int dpg_set_forces(dpg_handle h, const double *fx, const double *fy, int where);
+/* Particle::setBoxSize / getBoxSize (src/particles/base/particle.cu:694-709) */
+int dpg_set_box(dpg_handle h, double box_x, double box_y);
+int dpg_get_box(dpg_handle h, double *box_x, double *box_y);
+int dpg_synchronize(dpg_handle h);
+
+/* ---- neighbours ----------------------------------------------------- */
+/* Particle::setupNeighbors (src/particles/base/particle.cu:71-100): method
+ * fallbacks, cell size, initial lists, then calculateForces (+= semantics). */
+int dpg_setup_neighbors(dpg_handle h, const dpg_neighbor_config *cfg, dpg_neighbor_info *info);
+/* Particle::updateNeighborList (src/particles/base/particle.cu:1167-1169) */
+int dpg_build_neighbors(dpg_handle h);
+/* Particle::checkForNeighborUpdate (src/particles/base/particle.cu:1137-1161);
+ * *rebuilt = 0 none, 1 neighbour list, 2 cell list + neighbour list. */
+int dpg_check_neighbors(dpg_handle h, int *rebuilt);
+int dpg_neighbor_info_get(dpg_handle h, dpg_neighbor_info *info);
+/* Neighbour list in STATIC indices, row-major [n * cap] padded with -1, and
+ * counts[n]; cap in/out: capacity of `list` rows in, used capacity out. */
+int dpg_get_neighbors(dpg_handle h, int32_t *list, int32_t *counts, int *cap);
+/* Cell list in the reference's representation: cell_index[n] of the particle
+ * in each sorted slot, cell_start[n_cells + 1] with -1 for empty cells, and
+ * static_index[n] of each slot (src/particles/base/kernels.cu:309-438). */
+int dpg_get_cells(dpg_handle h, int64_t *cell_index, int64_t *cell_start, int64_t *static_index);
+
+/* ---- forces and integration ----------------------------------------- */
+/* kernelZeroForceAndPotentialEnergy (src/particles/base/kernels.cu:150-161) */
+int dpg_zero_forces(dpg_handle h);
+/* Disk::calculateForces -> kernelCalcDiskForces, accumulates into F and PE
+ * (src/particles/disk/disk.cu:218-221, src/particles/disk/kernels.cu:11-57) */
+int dpg_compute_forces(dpg_handle h);
+/* Particle::updateVelocities (src/particles/base/particle.cu:1090-1092) */
+int dpg_kick(dpg_handle h, double dt);
+/* Particle::updatePositions (src/particles/base/particle.cu:1086-1088) */
+int dpg_drift(dpg_handle h, double dt);
+/* n_steps of NVE::step (src/integrator/nve.cu:15-25), device-resident loop */
+int dpg_nve_steps(dpg_handle h, double dt, int64_t n_steps);
+
+/* ---- FIRE / Adam ------------------------------------------------------ */
+/* Particle::getPowerFire (src/particles/base/particle.cu:993-1009) */
+int dpg_power_fire(dpg_handle h, double *power);
+/* Particle::mixVelocitiesAndForces (src/particles/base/particle.cu:895-897) */
+int dpg_mix(dpg_handle h, double alpha);
+/* Particle::setVelocitiesToZero (src/particles/base/particle.cu:871-873) */
+int dpg_zero_velocities(dpg_handle h);
+/* Fire::Fire (src/integrator/fire.cu:3-7) */
+int dpg_fire_init(dpg_handle h, double alpha_init, double dt);
+/* Fire::step (src/integrator/fire.cu:13-46); *stopped = Fire::stopped */
+int dpg_fire_step(dpg_handle h, int *stopped);
+int dpg_fire_get(dpg_handle h, double *alpha, double *dt, int64_t *n_good, int64_t *n_bad,
+                 int *stopped);
+/* minimizeFire (src/routines/minimization.cu:75-112), device-resident loop */
+int dpg_fire_minimize(dpg_handle h, const dpg_fire_params *p, dpg_fire_result *r);
+/* Particle::initAdamVariables (src/particles/base/particle.cu:319-322) */
+int dpg_adam_init(dpg_handle h);
+/* Particle::updatePositionsAdam (src/particles/base/particle.cu:329-333) */
+int dpg_adam_step(dpg_handle h, int64_t step, double alpha, double beta1, double beta2,
+                  double epsilon);
+/* minimizeAdam (src/routines/minimization.cu:3-33); *steps as its `step` */
+int dpg_adam_minimize(dpg_handle h, double alpha, double beta1, double beta2, double epsilon,
+                      double avg_pe_target, double avg_pe_diff_target, int64_t max_steps,
+                      int64_t *steps);
+
+/* ---- observables ---------------------------------------------------- */
+/* totalPotentialEnergy / totalKineticEnergy (src/particles/base/particle.cu:1074-1080) */
+int dpg_reduce_energies(dpg_handle h, double *pe, double *ke);
+/* max_i |F_i| and |sum_i F_i| (getForceBalance, src/particles/base/particle.cu:231-235) */
+int dpg_force_stats(dpg_handle h, double *max_force, double *force_balance);
+/* calculateStressTensor + getStressTensor + getPressure
+ * (src/particles/disk/disk.cu:281-285, src/particles/base/particle.cu:1371-1384) */
+int dpg_pressure(dpg_handle h, double *pressure, double stress[4]);
+/* countContacts + getContactCount (src/particles/disk/disk.cu:250-255) */
+int dpg_contact_count(dpg_handle h, double *contacts);
+/* getPackingFraction (src/particles/base/particle.cu:1011-1015) */
+int dpg_packing_fraction(dpg_handle h, double *phi);
+
+/* ---- box scaling and snapshots ---------------------------------------- */
+/* Particle::scaleBox (src/particles/base/particle.cu:1057-1064) */
+int dpg_scale_box(dpg_handle h, double factor);
+/* Particle::scaleToPackingFractionFull (src/particles/base/particle.cu:1047-1055) */
+int dpg_scale_to_packing_fraction(dpg_handle h, double phi);
+/* setLastState / revertToLastState as device-side snapshots
+ * (src/particles/base/particle.cu:956-991) */
+int dpg_save_state(dpg_handle h);
+int dpg_restore_state(dpg_handle h);
+
+/* ---- measurement ------------------------------------------------------ */
+/* Runs `iters` iterations of a device loop (kind 0 = FIRE from the current
+ * state, as dpg_fire_minimize's body; kind 1 = NVE with step dt) as plain
+ * stream launches with a CUDA-event pair around each phase, and returns the
+ * mean device time per iteration of each phase in avg_us[3] (0 = move /
+ * first half, 1 = neighbour check + rebuild kernels, 2 = forces + kick) and
+ * counts[3] = {iterations, neighbour-list builds, cell-list builds}.  No
+ * reference counterpart: this is the measurement hook bench.py uses for the
+ * per-kernel roofline. */
+int dpg_profile_loop(dpg_handle h, int kind, int iters, double dt, double *avg_us, int64_t *counts);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,369 @@
+"""ctypes front end for the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+Loads ``oracle/_build/liboracle.so`` (the C restatement, prefix ``orc_``) and,
+where it was built, ``oracle/_ref/libdpref.so`` (the reference's own kernel
+sources compiled on the host, prefix ``ref_``).  Both expose the same C API, so
+``DiskOracle(kind="oracle")`` and ``DiskOracle(kind="reference")`` are
+interchangeable.  Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU
+baseline leg use this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ORACLE_SO = HERE / "_build" / "liboracle.so"
+REF_SO = HERE / "_ref" / "libdpref.so"
+
+NEIGH_CELL, NEIGH_VERLET, NEIGH_ALL = 0, 1, 2
+
+_libs: dict[str, C.CDLL] = {}
+
+D = C.c_double
+I64 = C.c_int64
+P = C.c_void_p
+DP = C.POINTER(C.c_double)
+LP = C.POINTER(C.c_int64)
+
+
+def build_oracle() -> Path:
+    subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+    return ORACLE_SO
+
+
+def build_reference() -> Path | None:
+    subprocess.run(["bash", str(HERE / "ref" / "build_ref.sh")], check=True,
+                   stdout=subprocess.DEVNULL)
+    return REF_SO if REF_SO.exists() else None
+
+
+def reference_available() -> bool:
+    return REF_SO.exists()
+
+
+_SIGS = {
+    "create": (P, [I64, D, D, D, D]),
+    "destroy": (None, [P]),
+    "set_arrays": (None, [P, DP, DP, DP, DP, DP, DP]),
+    "get_arrays": (None, [P, DP, DP, DP, DP, DP, DP, DP, DP, DP]),
+    "get_current": (None, [P, DP, DP, DP, DP, DP, DP, DP, LP]),
+    "get_box": (None, [P, DP, DP]),
+    "setup_neighbors": (C.c_int, [P, C.c_int, D, D, D, D]),
+    "update_neighbor_list": (None, [P]),
+    "check_for_neighbor_update": (C.c_int, [P]),
+    "neighbor_info": (None, [P, C.POINTER(C.c_int), DP, DP, LP, DP, DP, LP]),
+    "get_neighbors": (None, [P, LP, LP]),
+    "get_cells": (None, [P, LP, LP]),
+    "num_rebuilds": (I64, [P, LP]),
+    "zero_force_and_pe": (None, [P]),
+    "calculate_forces": (None, [P]),
+    "update_velocities": (None, [P, D]),
+    "update_positions": (None, [P, D]),
+    "mix_velocities_and_forces": (None, [P, D]),
+    "set_velocities_zero": (None, [P]),
+    "power_fire": (D, [P]),
+    "total_pe": (D, [P]),
+    "total_ke": (D, [P]),
+    "max_force": (D, [P]),
+    "nve_steps": (None, [P, D, I64]),
+    "fire_init": (None, [P, D, D]),
+    "fire_step": (C.c_int, [P]),
+    "fire_state": (None, [P, DP, DP, LP, LP, C.POINTER(C.c_int)]),
+    "minimize_fire": (I64, [P, D, D, D, D, I64, D, C.POINTER(C.c_int)]),
+    "init_adam": (None, [P]),
+    "adam_step": (None, [P, I64, D, D, D, D]),
+    "minimize_adam": (I64, [P, D, D, D, D, D, D, I64]),
+    "stress_tensor": (None, [P, DP]),
+    "pressure": (D, [P]),
+    "contact_count": (D, [P]),
+    "particle_area": (D, [P]),
+    "packing_fraction": (D, [P]),
+    "scale_to_packing_fraction": (None, [P, D]),
+    "scale_box": (None, [P, D]),
+    "set_last_state": (None, [P]),
+    "revert_to_last_state": (None, [P]),
+    "fill_uniform": (None, [DP, I64, D, D, I64, I64]),
+}
+
+
+def _load(kind: str) -> tuple[C.CDLL, str]:
+    if kind == "oracle":
+        path, prefix = ORACLE_SO, "orc_"
+        if not path.exists():
+            build_oracle()
+    elif kind == "reference":
+        path, prefix = REF_SO, "ref_"
+        if not path.exists():
+            raise FileNotFoundError("oracle/_ref/libdpref.so not built (needs the reference tree)")
+    else:
+        raise ValueError(kind)
+    if kind not in _libs:
+        lib = C.CDLL(str(path))
+        for name, (res, args) in _SIGS.items():
+            fn = getattr(lib, prefix + name, None)
+            if fn is None:
+                continue
+            fn.restype = res
+            fn.argtypes = args
+        if kind == "oracle":
+            lib.orc_fill_normal.restype = None
+            lib.orc_fill_normal.argtypes = [DP, I64, D, D, I64, I64]
+            lib.orc_erfcinv.restype = D
+            lib.orc_erfcinv.argtypes = [D]
+            lib.orc_set_threads.argtypes = [C.c_int]
+            lib.orc_set_forces.argtypes = [P, DP, DP]
+            lib.orc_force_balance.restype = D
+            lib.orc_force_balance.argtypes = [P]
+        _libs[kind] = lib
+    return _libs[kind], prefix
+
+
+def _dp(a):
+    return None if a is None else a.ctypes.data_as(DP)
+
+
+def _lp(a):
+    return None if a is None else a.ctypes.data_as(LP)
+
+
+class DiskOracle:
+    """One disk system held by the oracle or by the reference-kernel harness."""
+
+    def __init__(self, n, box, e_c=1.0, n_c=2.0, kind="oracle"):
+        self.lib, self.pre = _load(kind)
+        self.kind = kind
+        self.n = int(n)
+        bx, by = (box, box) if np.isscalar(box) else box
+        self.h = self._f("create")(self.n, float(bx), float(by), float(e_c), float(n_c))
+
+    def _f(self, name):
+        return getattr(self.lib, self.pre + name)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._f("destroy")(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- state -----------------------------------------------------------
+    def set_arrays(self, x=None, y=None, vx=None, vy=None, r=None, m=None):
+        arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+                for a in (x, y, vx, vy, r, m)]
+        self._f("set_arrays")(self.h, *[_dp(a) for a in arrs])
+
+    def get_arrays(self):
+        out = {k: np.zeros(self.n) for k in ("x", "y", "vx", "vy", "fx", "fy", "pe", "r", "m")}
+        self._f("get_arrays")(self.h, *[_dp(out[k]) for k in
+                                        ("x", "y", "vx", "vy", "fx", "fy", "pe", "r", "m")])
+        return out
+
+    def get_current(self):
+        out = {k: np.zeros(self.n) for k in ("x", "y", "vx", "vy", "fx", "fy", "pe")}
+        sidx = np.zeros(self.n, dtype=np.int64)
+        self._f("get_current")(self.h, *[_dp(out[k]) for k in
+                                         ("x", "y", "vx", "vy", "fx", "fy", "pe")], _lp(sidx))
+        out["static_index"] = sidx
+        return out
+
+    def box(self):
+        bx, by = D(), D()
+        self._f("get_box")(self.h, C.byref(bx), C.byref(by))
+        return bx.value, by.value
+
+    # -- neighbours ------------------------------------------------------
+    def setup_neighbors(self, method=NEIGH_CELL, cutoff_mult=1.5, disp_mult=0.2,
+                        particles_per_cell=8.0, cell_disp_mult=0.5):
+        return self._f("setup_neighbors")(self.h, int(method), float(cutoff_mult),
+                                          float(disp_mult), float(particles_per_cell),
+                                          float(cell_disp_mult))
+
+    def update_neighbor_list(self):
+        self._f("update_neighbor_list")(self.h)
+
+    def check_for_neighbor_update(self):
+        return self._f("check_for_neighbor_update")(self.h)
+
+    def neighbor_info(self):
+        m = C.c_int()
+        cutoff, thr2, cs, cthr2 = D(), D(), D(), D()
+        ncd, cap = I64(), I64()
+        self._f("neighbor_info")(self.h, C.byref(m), C.byref(cutoff), C.byref(thr2),
+                                 C.byref(ncd), C.byref(cs), C.byref(cthr2), C.byref(cap))
+        return dict(method=m.value, cutoff=cutoff.value, thr2=thr2.value, n_cells_dim=ncd.value,
+                    cell_size=cs.value, cell_thr2=cthr2.value, cap=cap.value)
+
+    def neighbors(self):
+        """(list[n, cap] int64 in current order, -1 padded; counts[n])"""
+        cap = self.neighbor_info()["cap"]
+        lst = np.zeros(self.n * cap, dtype=np.int64)
+        cnt = np.zeros(self.n, dtype=np.int64)
+        self._f("get_neighbors")(self.h, _lp(lst), _lp(cnt))
+        return lst.reshape(self.n, cap), cnt
+
+    def static_neighbor_sets(self):
+        """neighbour sets keyed by static (input) index"""
+        lst, cnt = self.neighbors()
+        sidx = self.get_current()["static_index"]
+        sets = [None] * self.n
+        for i in range(self.n):
+            sets[sidx[i]] = frozenset(int(sidx[j]) for j in lst[i, :cnt[i]] if j >= 0)
+        return sets
+
+    def cells(self):
+        info = self.neighbor_info()
+        ci = np.zeros(self.n, dtype=np.int64)
+        ncells = max(info["n_cells_dim"], 0) ** 2
+        cs = np.zeros(ncells + 1, dtype=np.int64)
+        self._f("get_cells")(self.h, _lp(ci), _lp(cs))
+        return ci, cs
+
+    def num_rebuilds(self):
+        nc = I64()
+        n = self._f("num_rebuilds")(self.h, C.byref(nc))
+        return n, nc.value
+
+    # -- dynamics ----------------------------------------------------------
+    def zero_force_and_pe(self):
+        self._f("zero_force_and_pe")(self.h)
+
+    def calculate_forces(self):
+        self._f("calculate_forces")(self.h)
+
+    def update_velocities(self, dt):
+        self._f("update_velocities")(self.h, float(dt))
+
+    def update_positions(self, dt):
+        self._f("update_positions")(self.h, float(dt))
+
+    def mix_velocities_and_forces(self, alpha):
+        self._f("mix_velocities_and_forces")(self.h, float(alpha))
+
+    def set_velocities_zero(self):
+        self._f("set_velocities_zero")(self.h)
+
+    def power_fire(self):
+        return self._f("power_fire")(self.h)
+
+    def total_pe(self):
+        return self._f("total_pe")(self.h)
+
+    def total_ke(self):
+        return self._f("total_ke")(self.h)
+
+    def max_force(self):
+        return self._f("max_force")(self.h)
+
+    def nve_steps(self, dt, n):
+        self._f("nve_steps")(self.h, float(dt), int(n))
+
+    def fire_init(self, alpha_init=0.1, dt=1e-2):
+        self._f("fire_init")(self.h, float(alpha_init), float(dt))
+
+    def fire_step(self):
+        return self._f("fire_step")(self.h)
+
+    def fire_state(self):
+        a, dt = D(), D()
+        ng, nb = I64(), I64()
+        st = C.c_int()
+        self._f("fire_state")(self.h, C.byref(a), C.byref(dt), C.byref(ng), C.byref(nb), C.byref(st))
+        return dict(alpha=a.value, dt=dt.value, n_good=ng.value, n_bad=nb.value, stopped=st.value)
+
+    def minimize_fire(self, alpha_init=0.1, dt=1e-2, pe_target=1e-16, pe_diff_target=1e-16,
+                      num_steps=100000, fmax_target=0.0):
+        st = C.c_int()
+        steps = self._f("minimize_fire")(self.h, float(alpha_init), float(dt), float(pe_target),
+                                         float(pe_diff_target), int(num_steps),
+                                         float(fmax_target), C.byref(st))
+        return steps, st.value
+
+    def init_adam(self):
+        self._f("init_adam")(self.h)
+
+    def adam_step(self, step, alpha=1e-4, beta1=0.9, beta2=0.999, eps=1e-8):
+        self._f("adam_step")(self.h, int(step), float(alpha), float(beta1), float(beta2), float(eps))
+
+    def minimize_adam(self, alpha=1e-4, beta1=0.9, beta2=0.999, eps=1e-8, pe_target=1e-16,
+                      pe_diff_target=1e-16, num_steps=100000):
+        return self._f("minimize_adam")(self.h, float(alpha), float(beta1), float(beta2),
+                                        float(eps), float(pe_target), float(pe_diff_target),
+                                        int(num_steps))
+
+    def stress_tensor(self):
+        out = np.zeros(4)
+        self._f("stress_tensor")(self.h, _dp(out))
+        return out
+
+    def pressure(self):
+        return self._f("pressure")(self.h)
+
+    def contact_count(self):
+        return self._f("contact_count")(self.h)
+
+    def packing_fraction(self):
+        return self._f("packing_fraction")(self.h)
+
+    def particle_area(self):
+        return self._f("particle_area")(self.h)
+
+    def scale_to_packing_fraction(self, phi):
+        self._f("scale_to_packing_fraction")(self.h, float(phi))
+
+    def scale_box(self, f):
+        self._f("scale_box")(self.h, float(f))
+
+    def set_last_state(self):
+        self._f("set_last_state")(self.h)
+
+    def revert_to_last_state(self):
+        self._f("revert_to_last_state")(self.h)
+
+
+def fill_uniform(n, lo, hi, seed_offset, seed, kind="oracle"):
+    lib, pre = _load(kind)
+    out = np.zeros(int(n))
+    getattr(lib, pre + "fill_uniform")(_dp(out), int(n), float(lo), float(hi), int(seed_offset),
+                                       int(seed))
+    return out
+
+
+def fill_normal(n, mean, std, seed_offset, seed):
+    lib, _ = _load("oracle")
+    out = np.zeros(int(n))
+    lib.orc_fill_normal(_dp(out), int(n), float(mean), float(std), int(seed_offset), int(seed))
+    return out
+
+
+def set_threads(n: int):
+    lib, _ = _load("oracle")
+    lib.orc_set_threads(int(n))
+
+
+def disk_packing(n, phi, seed, size_ratio=1.4, count_ratio=0.5, kind="oracle"):
+    """Reference-style bidisperse initial state (Disk::initializeFromConfig,
+    src/particles/disk/disk.cu:98-141): first floor(n*count_ratio) particles
+    large (diameter size_ratio), rest diameter 1; square box at packing
+    fraction phi; positions from the reference's uniform generator."""
+    n = int(n)
+    n_large = int(n * count_ratio)
+    r = np.full(n, 0.5)
+    r[:n_large] = size_ratio / 2.0
+    area = float(np.sum(r * r)) * np.pi  # sequential order matters little; see oracle
+    a = 0.0
+    for v in r:
+        a += v * v
+    area = a * 3.141592653589793238462643383279502884197
+    L = (area / phi) ** 0.5
+    x = fill_uniform(n, 0.0, L, 0, seed, kind)
+    y = fill_uniform(n, 0.0, L, n, seed, kind)
+    return dict(x=x, y=y, r=r, m=np.ones(n), box=L)

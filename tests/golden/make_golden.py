@@ -1,0 +1,152 @@
+"""Generates the golden fixtures in tests/golden/ from the REFERENCE's own kernel
+sources (mmccraw98/dpCUDA-v2 src/particles/{base,disk}/kernels.cu compiled on
+the host by oracle/ref/build_ref.sh and driven by oracle/ref/ref_driver.cpp).
+
+Run here, where the reference tree exists:
+    python tests/golden/make_golden.py
+The fixtures are committed; the GPU tests and the CPU oracle tests read them
+without needing the reference tree.
+
+Inputs come from the reference's own seeded generator (include/functors.h
+RandomUniform, exact) for positions; velocities come from the oracle's
+restatement of the GPU normal sampler (stored as given inputs).
+"""
+from __future__ import annotations
+
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent.parent
+sys.path.insert(0, str(ROOT))
+
+from oracle.oracle import (DiskOracle, build_reference, disk_packing, fill_normal,  # noqa: E402
+                           fill_uniform)
+
+CUT_MULT = 1.7 / 1.4  # r_c = d_max + skin 0.3 with d_max = 1.4
+
+
+def padded_static_neighbors(o: DiskOracle) -> np.ndarray:
+    sets = o.static_neighbor_sets()
+    width = max(1, max(len(s) for s in sets))
+    out = np.full((o.n, width), -1, dtype=np.int32)
+    for i, s in enumerate(sets):
+        row = sorted(s)
+        out[i, :len(row)] = row
+    return out
+
+
+def snapshot(o: DiskOracle, prefix: str, d: dict):
+    a = o.get_arrays()
+    for k in ("x", "y", "vx", "vy", "fx", "fy", "pe"):
+        d[f"{prefix}_{k}"] = a[k]
+
+
+def system(n, phi, seed, method=0, vel_T=None):
+    st = disk_packing(n, phi, seed, kind="reference")
+    o = DiskOracle(n, st["box"], kind="reference")
+    vx = vy = None
+    if vel_T is not None:
+        vx = fill_normal(n, 0.0, np.sqrt(vel_T), 1, seed)
+        vy = fill_normal(n, 0.0, np.sqrt(vel_T), 1 + n, seed)
+        vx -= vx.mean()
+        vy -= vy.mean()
+    o.set_arrays(x=st["x"], y=st["y"], vx=vx, vy=vy, r=st["r"], m=st["m"])
+    info = o.setup_neighbors(method, CUT_MULT, 0.2, 8.0, 0.5)
+    return o, st, vx, vy, info
+
+
+def make_small():
+    d = {}
+    o, st, vx, vy, meth = system(64, 0.80, 7, vel_T=1e-3)
+    d.update(x0=st["x"], y0=st["y"], r=st["r"], m=st["m"], box=st["box"], vx0=vx, vy0=vy,
+             method=meth)
+    snapshot(o, "setup", d)
+    d["setup_neighbors"] = padded_static_neighbors(o)
+    o.nve_steps(1e-2, 200)
+    snapshot(o, "nve200", d)
+    d["nve200_total_pe"] = o.total_pe()
+    d["nve200_total_ke"] = o.total_ke()
+    o.fire_init(0.1, 1e-2)
+    for _ in range(100):
+        o.fire_step()
+    snapshot(o, "fire100", d)
+    fs = o.fire_state()
+    d["fire100_state"] = np.array([fs["alpha"], fs["dt"], fs["n_good"], fs["n_bad"], fs["stopped"]])
+    np.savez_compressed(HERE / "disk_n64_verlet.npz", **d)
+
+
+def make_cfg1():
+    d = {}
+    n, phi, seed = 1024, 0.80, 1
+    o, st, vx, vy, meth = system(n, phi, seed, vel_T=1e-4)
+    d.update(x0=st["x"], y0=st["y"], r=st["r"], m=st["m"], box=st["box"], vx0=vx, vy0=vy,
+             method=meth)
+    info = o.neighbor_info()
+    d["n_cells_dim"] = info["n_cells_dim"]
+    d["cap"] = info["cap"]
+    ci, cs = o.cells()
+    d["setup_cell_index"] = ci
+    d["setup_cell_start"] = cs
+    d["setup_static_index"] = o.get_current()["static_index"]
+    snapshot(o, "setup", d)
+    d["setup_neighbors"] = padded_static_neighbors(o)
+    d["setup_stress"] = o.stress_tensor()
+    d["setup_contacts"] = o.contact_count()
+    o.nve_steps(1e-2, 500)
+    snapshot(o, "nve500", d)
+    d["nve500_rebuilds"] = np.array(o.num_rebuilds())
+    d["nve500_total_pe"] = o.total_pe()
+    d["nve500_total_ke"] = o.total_ke()
+    o.fire_init(0.1, 1e-2)
+    for _ in range(300):
+        o.fire_step()
+    snapshot(o, "fire300", d)
+    fs = o.fire_state()
+    d["fire300_state"] = np.array([fs["alpha"], fs["dt"], fs["n_good"], fs["n_bad"], fs["stopped"]])
+    o.init_adam()
+    for k in range(40):
+        o.zero_force_and_pe()
+        o.check_for_neighbor_update()
+        o.calculate_forces()
+        o.adam_step(k, 1e-3, 0.9, 0.999, 1e-8)
+    snapshot(o, "adam40", d)
+    np.savez_compressed(HERE / "disk_n1024_cell.npz", **d)
+
+
+def make_fire_min():
+    """FIRE minimisation to the reference's own stop criteria (PE change)."""
+    d = {}
+    n, phi, seed = 2048, 0.86, 3
+    o, st, _, _, meth = system(n, phi, seed)
+    d.update(x0=st["x"], y0=st["y"], r=st["r"], m=st["m"], box=st["box"], method=meth)
+    steps, stopped = o.minimize_fire(0.1, 1e-2, 1e-16, 1e-16, 100000, 0.0)
+    d["steps"] = steps
+    d["stopped"] = stopped
+    d["avg_pe"] = o.total_pe() / n
+    d["max_force"] = o.max_force()
+    a = o.get_arrays()
+    d["x"], d["y"] = a["x"], a["y"]
+    d["pressure"] = o.pressure()
+    d["contacts"] = o.contact_count()
+    np.savez_compressed(HERE / "disk_n2048_fire_min.npz", **d)
+
+
+def make_rng():
+    d = {}
+    for seed in (1, 7, 12345):
+        d[f"uniform_seed{seed}"] = fill_uniform(1000, 0.0, 38.5, 0, seed, kind="reference")
+        d[f"uniform_seed{seed}_off"] = fill_uniform(1000, -0.5, 0.5, 3000, seed, kind="reference")
+    np.savez_compressed(HERE / "rng_uniform.npz", **d)
+
+
+if __name__ == "__main__":
+    if build_reference() is None:
+        sys.exit("reference tree not available; cannot regenerate fixtures")
+    make_rng()
+    make_small()
+    make_cfg1()
+    make_fire_min()
+    print("fixtures written to", HERE)

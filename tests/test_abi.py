@@ -1,0 +1,51 @@
+"""CPU: the C-ABI library builds for sm_103a, loads, and exports every entry
+point that include/*.h declares (no compute calls: there is no GPU here)."""
+import ctypes
+import re
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def declared_symbols():
+    names = set()
+    for h in (ROOT / "include").glob("*.h"):
+        text = h.read_text()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        names.update(re.findall(r"\b(dpg_\w+)\s*\(", text))
+    return sorted(names)
+
+
+def test_header_declares_entry_points():
+    names = declared_symbols()
+    assert "dpg_create" in names and "dpg_fire_minimize" in names
+    assert len(names) >= 30
+
+
+def test_library_exports_every_declared_symbol():
+    from dpcuda_gb300 import build
+    lib_path = build.build()
+    lib = ctypes.CDLL(str(lib_path))
+    missing = [n for n in declared_symbols() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_python_binding_covers_the_abi():
+    from dpcuda_gb300.lib import SIGNATURES
+    missing = [n for n in declared_symbols() if n not in SIGNATURES]
+    assert not missing, missing
+
+
+def test_error_path_without_gpu_is_loud():
+    """Creating a system must fail with a CUDA error, never fall back to CPU."""
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present")
+    except ImportError:
+        pass
+    from dpcuda_gb300 import Disk, DpgError
+    with pytest.raises(DpgError):
+        Disk(16, 10.0)

@@ -1,0 +1,297 @@
+"""GPU parity: the sm_103a FP64 disk path (through the C ABI) against the golden
+fixtures made by the reference's own kernels and against the CPU oracle.
+
+Per-particle FP64 arithmetic is compiled without FMA contraction and follows
+the reference's operation order, so forces, neighbour sets, cell lists and
+whole NVE / FIRE / Adam trajectories must be BIT-IDENTICAL to the reference.
+Only totals from grid reductions (summation order differs) carry a tolerance:
+1e-12 relative.
+"""
+import os
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+G = Path(__file__).resolve().parent / "golden"
+CUT_MULT = 1.7 / 1.4
+KEYS = ("x", "y", "vx", "vy", "fx", "fy", "pe")
+RTOL_SUM = 1e-12
+
+
+@pytest.fixture(scope="module")
+def dpg():
+    import dpcuda_gb300
+    dpcuda_gb300.load_library()
+    return dpcuda_gb300
+
+
+def load(name):
+    return dict(np.load(G / name))
+
+
+def make(dpg, d, method="cell"):
+    n = len(d["r"])
+    s = dpg.Disk(n, float(d["box"]))
+    s.setState(d["x0"], d["y0"], d.get("vx0"), d.get("vy0"), d["r"], d["m"])
+    info = s.setupNeighbors(method, CUT_MULT, 0.2, 8.0, 0.5)
+    assert info["method"] == int(d["method"])
+    return s
+
+
+def assert_state(s, d, prefix):
+    a = s.getState()
+    for k in KEYS:
+        np.testing.assert_array_equal(a[k], d[f"{prefix}_{k}"], err_msg=f"{prefix}_{k}")
+
+
+def golden_sets(arr):
+    return [frozenset(int(j) for j in row if j >= 0) for row in arr]
+
+
+def oracle_for(d):
+    from oracle.oracle import DiskOracle
+    n = len(d["r"])
+    o = DiskOracle(n, float(d["box"]))
+    o.set_arrays(x=d["x0"], y=d["y0"], vx=d.get("vx0"), vy=d.get("vy0"), r=d["r"], m=d["m"])
+    o.setup_neighbors(0, CUT_MULT, 0.2, 8.0, 0.5)
+    return o
+
+
+# ---------------------------------------------------------------------------
+def test_setup_forces_neighbors_cells_bitexact(dpg):
+    d = load("disk_n1024_cell.npz")
+    s = make(dpg, d)
+    info = s.neighborInfo()
+    assert info["n_cells_dim"] == int(d["n_cells_dim"]) and info["capacity"] == int(d["cap"])
+    assert_state(s, d, "setup")
+    assert s.getNeighborSets() == golden_sets(d["setup_neighbors"])
+    ci, cs, si = s.getCells()
+    np.testing.assert_array_equal(ci, d["setup_cell_index"])
+    np.testing.assert_array_equal(cs, d["setup_cell_start"])
+    np.testing.assert_array_equal(si, d["setup_static_index"])
+    np.testing.assert_allclose(s.getStressTensor(), d["setup_stress"], rtol=RTOL_SUM, atol=1e-18)
+    assert s.getContactCount() == float(d["setup_contacts"])
+
+
+def test_nve_trajectory_bitexact(dpg):
+    d = load("disk_n1024_cell.npz")
+    s = make(dpg, d)
+    s.nveSteps(1e-2, 500)
+    assert_state(s, d, "nve500")
+    info = s.neighborInfo()
+    assert (info["n_rebuilds"], info["n_cell_rebuilds"]) == tuple(int(v) for v in d["nve500_rebuilds"])
+    np.testing.assert_allclose(s.totalPotentialEnergy(), float(d["nve500_total_pe"]), rtol=RTOL_SUM)
+    np.testing.assert_allclose(s.totalKineticEnergy(), float(d["nve500_total_ke"]), rtol=RTOL_SUM)
+
+
+def test_single_ops_match_fused_nve(dpg):
+    """The drop-in per-method calls give the same trajectory as the fused loop."""
+    d = load("disk_n1024_cell.npz")
+    s = make(dpg, d)
+    for _ in range(120):  # NVE::step spelled out (src/integrator/nve.cu:15-25)
+        s.updateVelocities(0.5e-2)
+        s.updatePositions(1e-2)
+        s.checkForNeighborUpdate()
+        s.zeroForceAndPotentialEnergy()
+        s.calculateForces()
+        s.updateVelocities(0.5e-2)
+    f = make(dpg, d)
+    f.nveSteps(1e-2, 120)
+    a, b = s.getState(), f.getState()
+    for k in KEYS:
+        np.testing.assert_array_equal(a[k], b[k])
+
+
+def test_fire_steps_bitexact(dpg):
+    d = load("disk_n1024_cell.npz")
+    s = make(dpg, d)
+    s.nveSteps(1e-2, 500)
+    fire = dpg.Fire(s, 0.1, 1e-2)
+    for _ in range(300):
+        fire.step()
+    assert_state(s, d, "fire300")
+    st = fire.state()
+    np.testing.assert_array_equal([st["alpha"], st["dt"], st["n_good"], st["n_bad"], st["stopped"]],
+                                  d["fire300_state"])
+
+
+def test_adam_bitexact(dpg):
+    d = load("disk_n1024_cell.npz")
+    s = make(dpg, d)
+    s.nveSteps(1e-2, 500)
+    fire = dpg.Fire(s, 0.1, 1e-2)
+    for _ in range(300):
+        fire.step()
+    s.initAdamVariables()
+    adam = dpg.Adam(s, 1e-3, 0.9, 0.999, 1e-8)
+    for k in range(40):
+        adam.minimize(k)
+    assert_state(s, d, "adam40")
+
+
+def test_small_system_verlet_fallback_bitexact(dpg):
+    d = load("disk_n64_verlet.npz")
+    s = make(dpg, d)
+    assert_state(s, d, "setup")
+    assert s.getNeighborSets() == golden_sets(d["setup_neighbors"])
+    s.nveSteps(1e-2, 200)
+    assert_state(s, d, "nve200")
+    fire = dpg.Fire(s, 0.1, 1e-2)
+    for _ in range(100):
+        fire.step()
+    assert_state(s, d, "fire100")
+
+
+def test_fire_minimize_matches_reference(dpg):
+    """minimizeFire to the reference's own criteria (PE stationary): same
+    minimum.  The device loop's PE reductions round differently from the
+    reference's sequential sums, so the exit step may differ slightly."""
+    d = load("disk_n2048_fire_min.npz")
+    s = make(dpg, d)
+    r = dpg.minimizeFire(s, 0.1, 1e-2, 1e-16, 1e-16, 100000)
+    assert r["stopped"] == int(d["stopped"])
+    assert abs(r["steps"] - int(d["steps"])) <= max(50, int(d["steps"]) // 100)
+    np.testing.assert_allclose(r["avg_pe"], float(d["avg_pe"]), rtol=1e-10)
+    a = s.getState()
+    np.testing.assert_allclose(a["x"], d["x"], rtol=0, atol=1e-8)
+    np.testing.assert_allclose(s.getPressure(), float(d["pressure"]), rtol=1e-10)
+
+
+def test_fire_minimize_first_steps_bitexact_with_oracle(dpg):
+    """Before any PE-ratio test can fire, the device loop and the oracle take
+    identical steps (checked after max_steps iterations)."""
+    d = load("disk_n2048_fire_min.npz")
+    s = make(dpg, d)
+    o = oracle_for(d)
+    r = dpg.minimizeFire(s, 0.1, 1e-2, 1e-16, 1e-16, 700)
+    steps, _ = o.minimize_fire(0.1, 1e-2, 1e-16, 1e-16, 700, 0.0)
+    assert r["steps"] == steps == 700
+    a, b = s.getState(), o.get_arrays()
+    for k in ("x", "y", "fx", "fy", "pe"):
+        np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+
+
+def test_fire_to_residual_force(dpg):
+    """FIRE run past PE stagnation to max|F| <= 1e-13 (the added stop)."""
+    from oracle.oracle import disk_packing
+    st = disk_packing(1024, 0.86, 11)
+    s = dpg.Disk(1024, st["box"])
+    s.setState(st["x"], st["y"], None, None, st["r"], st["m"])
+    s.setupNeighbors("cell", CUT_MULT, 0.2, 8.0, 0.5)
+    r = dpg.minimizeFire(s, 0.1, 1e-2, 0.0, 0.0, 200000, fmax_target=1e-13)
+    assert r["converged"] == 1 and r["stopped"] == 0
+    assert r["max_force"] <= 1e-13
+    mx, bal = s.forceStats()
+    assert mx <= 1e-13 and bal < 1e-12
+
+
+def test_loop_modes_agree(dpg, monkeypatch):
+    """Conditional-graph, chunked-graph and plain-stream loops: same result."""
+    d = load("disk_n1024_cell.npz")
+    out = {}
+    for mode in ("cond", "graph", "stream"):
+        monkeypatch.setenv("DPG_LOOP_MODE", mode)
+        s = make(dpg, d)
+        s.nveSteps(1e-2, 77)
+        r = dpg.minimizeFire(s, 0.1, 1e-2, 1e-16, 1e-16, 333)
+        out[mode] = (s.getState(), r["steps"])
+    for mode in ("graph", "stream"):
+        assert out[mode][1] == out["cond"][1]
+        for k in KEYS:
+            np.testing.assert_array_equal(out[mode][0][k], out["cond"][0][k])
+
+
+def test_scale_save_revert_match_oracle(dpg):
+    d = load("disk_n1024_cell.npz")
+    s = make(dpg, d)
+    o = oracle_for(d)
+    s.setLastState()
+    o.set_last_state()
+    s.scaleToPackingFractionFull(0.9)
+    o.scale_to_packing_fraction(0.9)
+    assert tuple(s.getBoxSize()) == o.box()
+    dpg.minimizeFire(s, 0.1, 1e-2, 1e-16, 1e-16, 200)
+    o.minimize_fire(0.1, 1e-2, 1e-16, 1e-16, 200, 0.0)
+    a, b = s.getState(), o.get_arrays()
+    for k in ("x", "y", "fx", "fy"):
+        np.testing.assert_array_equal(a[k], b[k])
+    s.revertToLastState()
+    o.revert_to_last_state()
+    s.scaleBox(0.98)
+    o.scale_box(0.98)
+    dpg.minimizeFire(s, 0.1, 1e-2, 1e-16, 1e-16, 200)
+    o.minimize_fire(0.1, 1e-2, 1e-16, 1e-16, 200, 0.0)
+    a, b = s.getState(), o.get_arrays()
+    for k in ("x", "y", "fx", "fy"):
+        np.testing.assert_array_equal(a[k], b[k])
+    assert tuple(s.getBoxSize()) == o.box()
+
+
+def test_capacity_growth_mid_loop(dpg):
+    """Compression raises neighbour counts past the capacity during a device
+    loop: the loop halts, the host grows the list (power of two) and resumes;
+    the trajectory equals the oracle's (which resizes the same way)."""
+    from oracle.oracle import disk_packing
+    st = disk_packing(512, 0.5, 5)
+    s = dpg.Disk(512, st["box"])
+    s.setState(st["x"], st["y"], None, None, st["r"], st["m"])
+    s.setupNeighbors("verlet", 1.5, 0.2, 8.0, 0.5)
+    from oracle.oracle import DiskOracle
+    o = DiskOracle(512, st["box"])
+    o.set_arrays(x=st["x"], y=st["y"], r=st["r"], m=st["m"])
+    o.setup_neighbors(1, 1.5, 0.2, 8.0, 0.5)
+    cap0 = s.neighborInfo()["capacity"]
+    for phi in (0.7, 0.85, 0.95):
+        s.scaleToPackingFractionFull(phi)
+        o.scale_to_packing_fraction(phi)
+        dpg.minimizeFire(s, 0.1, 1e-2, 1e-16, 1e-16, 150)
+        o.minimize_fire(0.1, 1e-2, 1e-16, 1e-16, 150, 0.0)
+    assert s.neighborInfo()["capacity"] > cap0
+    assert s.neighborInfo()["capacity"] == o.neighbor_info()["cap"]
+    a, b = s.getState(), o.get_arrays()
+    for k in ("x", "y", "fx", "fy"):
+        np.testing.assert_array_equal(a[k], b[k])
+
+
+def test_large_n_properties(dpg):
+    """N = 2^20 (the large-N configuration): Newton's third law, neighbour
+    symmetry, and forces of sampled particles against a direct sum."""
+    from oracle.oracle import fill_uniform
+    n = 1 << 20
+    rng = np.random.default_rng(5)
+    r = rng.uniform(0.4, 0.6, n)
+    area = float(np.sum(r * r)) * np.pi
+    L = (area / 0.84) ** 0.5
+    x = fill_uniform(n, 0.0, L, 0, 1)
+    y = fill_uniform(n, 0.0, L, n, 1)
+    s = dpg.Disk(n, L)
+    s.setState(x, y, None, None, r, np.ones(n))
+    info = s.setupNeighbors("cell", 1.5 / 1.2, 0.2, 8.0, 0.5)
+    assert info["method"] == 0
+    a = s.getState()
+    assert abs(a["fx"].sum()) < 1e-9 * n and abs(a["fy"].sum()) < 1e-9 * n
+    lst, cnt = s.getNeighbors()
+    idx = rng.choice(n, 64, replace=False)
+    rc = info["cutoff"]
+    for i in idx:
+        dx = x - x[i]
+        dx -= L * np.round(dx / L)
+        dy = y - y[i]
+        dy -= L * np.round(dy / L)
+        d2 = dx * dx + dy * dy
+        want = set(np.nonzero(d2 < rc * rc)[0].tolist()) - {int(i)}
+        assert set(lst[i, :cnt[i]].tolist()) == want
+        for j in want:  # symmetric list
+            assert i in set(lst[j, :cnt[j]].tolist())
+        rs = r + r[i]
+        m = (d2 < rs * rs) & (np.arange(n) != i)
+        dd = np.sqrt(d2[m])
+        fm = (1.0 - dd / rs[m]) / (rs[m] * dd)
+        fx = np.sum(fm * (-dx[m]))
+        np.testing.assert_allclose(a["fx"][i], fx, rtol=1e-9, atol=1e-13)
+    s.nveSteps(1e-2, 50)
+    b = s.getState()
+    assert np.all(np.isfinite(b["x"]))
