@@ -367,3 +367,206 @@ def disk_packing(n, phi, seed, size_ratio=1.4, count_ratio=0.5, kind="oracle"):
     x = fill_uniform(n, 0.0, L, 0, seed, kind)
     y = fill_uniform(n, 0.0, L, n, seed, kind)
     return dict(x=x, y=y, r=r, m=np.ones(n), box=L)
+
+
+# ---------------------------------------------------------------------------
+# rigid bumpy bodies
+# ---------------------------------------------------------------------------
+_BSIGS = {
+    "create": (P, [I64, I64, D, D, D, D, D, D, C.c_int]),
+    "destroy": (None, [P]),
+    "set_bodies": (C.c_int, [P, DP, DP, DP, DP, DP, DP, DP, LP]),
+    "init_vertices": (None, [P]),
+    "set_vertices": (None, [P, DP, DP]),
+    "set_mass": (None, [P, D]),
+    "setup_neighbors": (C.c_int, [P, C.c_int, D, D, D, D]),
+    "check_for_neighbor_update": (C.c_int, [P]),
+    "zero": (None, [P]),
+    "calculate_forces": (None, [P]),
+    "update_velocities": (None, [P, D]),
+    "update_positions": (None, [P, D]),
+    "mix": (None, [P, D]),
+    "set_velocities_zero": (None, [P]),
+    "power_fire": (D, [P]),
+    "total_pe": (D, [P]),
+    "total_ke": (D, [P]),
+    "nve_steps": (None, [P, D, I64]),
+    "fire_init": (None, [P, D, D]),
+    "fire_step": (C.c_int, [P]),
+    "get_bodies": (None, [P] + [DP] * 11),
+    "get_vertices": (None, [P, DP, DP]),
+    "get_vertex_neighbors": (I64, [P, LP, LP]),
+    "neighbor_info": (None, [P, C.POINTER(C.c_int), DP, DP, DP, LP, LP, LP, LP]),
+}
+_blibs: dict[str, C.CDLL] = {}
+
+
+def _bload(kind):
+    lib, _ = _load(kind)
+    prefix = "orcb_" if kind == "oracle" else "refb_"
+    if kind not in _blibs:
+        for name, (res, args) in _BSIGS.items():
+            fn = getattr(lib, prefix + name)
+            fn.restype = res
+            fn.argtypes = args
+        if kind == "oracle":
+            lib.orcb_minimize_fire.restype = I64
+            lib.orcb_minimize_fire.argtypes = [P, D, D, D, D, I64, D, D, C.POINTER(C.c_int)]
+            lib.orcb_vertex_radius.restype = D
+            lib.orcb_vertex_radius.argtypes = [D, I64, D]
+        _blibs[kind] = lib
+    return lib, prefix
+
+
+def bumpy_vertex_radius(min_diameter, n_vertices_small, seg):
+    lib, _ = _bload("oracle")
+    return lib.orcb_vertex_radius(float(min_diameter), int(n_vertices_small), float(seg))
+
+
+class BumpyOracle:
+    """Rigid bumpy bodies held by the oracle or by the reference-kernel harness."""
+
+    BODY_KEYS = ("x", "y", "th", "vx", "vy", "w", "fx", "fy", "tq", "pe", "I")
+
+    def __init__(self, n_bodies, n_vertices, box, e_c, n_c, vertex_radius, seg, rotation=True,
+                 kind="oracle"):
+        self.lib, self.pre = _bload(kind)
+        self.nb, self.nv = int(n_bodies), int(n_vertices)
+        bx, by = (box, box) if np.isscalar(box) else box
+        self.h = self._f("create")(self.nb, self.nv, float(bx), float(by), float(e_c), float(n_c),
+                                   float(vertex_radius), float(seg), int(bool(rotation)))
+
+    def _f(self, name):
+        return getattr(self.lib, self.pre + name)
+
+    def __del__(self):
+        try:
+            if self.h:
+                self._f("destroy")(self.h)
+        except Exception:
+            pass
+
+    def set_bodies(self, x, y, th, r, nvb, vx=None, vy=None, w=None):
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) if a is not None else None
+                for a in (x, y, th, vx, vy, w, r)]
+        nv = np.ascontiguousarray(nvb, dtype=np.int64)
+        rc = self._f("set_bodies")(self.h, *[_dp(a) for a in arrs], _lp(nv))
+        if rc != 0:
+            raise ValueError("vertex counts do not sum to n_vertices")
+
+    def init_vertices(self):
+        self._f("init_vertices")(self.h)
+
+    def set_vertices(self, px, py):
+        self._f("set_vertices")(self.h, _dp(np.ascontiguousarray(px, dtype=np.float64)),
+                                _dp(np.ascontiguousarray(py, dtype=np.float64)))
+
+    def set_mass(self, m):
+        self._f("set_mass")(self.h, float(m))
+
+    def setup_neighbors(self, method=NEIGH_CELL, cutoff_mult=1.5, disp_mult=0.2, ppc=8.0, cdm=0.5):
+        return self._f("setup_neighbors")(self.h, int(method), float(cutoff_mult), float(disp_mult),
+                                          float(ppc), float(cdm))
+
+    def check_for_neighbor_update(self):
+        return self._f("check_for_neighbor_update")(self.h)
+
+    def zero(self):
+        self._f("zero")(self.h)
+
+    def calculate_forces(self):
+        self._f("calculate_forces")(self.h)
+
+    def update_velocities(self, dt):
+        self._f("update_velocities")(self.h, float(dt))
+
+    def update_positions(self, dt):
+        self._f("update_positions")(self.h, float(dt))
+
+    def mix(self, alpha):
+        self._f("mix")(self.h, float(alpha))
+
+    def set_velocities_zero(self):
+        self._f("set_velocities_zero")(self.h)
+
+    def power_fire(self):
+        return self._f("power_fire")(self.h)
+
+    def total_pe(self):
+        return self._f("total_pe")(self.h)
+
+    def total_ke(self):
+        return self._f("total_ke")(self.h)
+
+    def nve_steps(self, dt, n):
+        self._f("nve_steps")(self.h, float(dt), int(n))
+
+    def fire_init(self, alpha=0.1, dt=1e-2):
+        self._f("fire_init")(self.h, float(alpha), float(dt))
+
+    def fire_step(self):
+        return self._f("fire_step")(self.h)
+
+    def minimize_fire(self, alpha=0.1, dt=1e-2, pe_target=1e-16, pe_diff_target=1e-16,
+                      num_steps=100000, fmax=0.0, tmax=0.0):
+        st = C.c_int()
+        n = self.lib.orcb_minimize_fire(self.h, float(alpha), float(dt), float(pe_target),
+                                        float(pe_diff_target), int(num_steps), float(fmax),
+                                        float(tmax), C.byref(st))
+        return n, st.value
+
+    def bodies(self):
+        out = {k: np.zeros(self.nb) for k in self.BODY_KEYS}
+        self._f("get_bodies")(self.h, *[_dp(out[k]) for k in self.BODY_KEYS])
+        return out
+
+    def vertices(self):
+        px, py = np.zeros(self.nv), np.zeros(self.nv)
+        self._f("get_vertices")(self.h, _dp(px), _dp(py))
+        return px, py
+
+    def vertex_neighbor_sets(self):
+        cap = self._f("get_vertex_neighbors")(self.h, None, None)
+        lst = np.zeros(self.nv * cap, dtype=np.int64)
+        cnt = np.zeros(self.nv, dtype=np.int64)
+        self._f("get_vertex_neighbors")(self.h, _lp(lst), _lp(cnt))
+        lst = lst.reshape(self.nv, cap)
+        return [frozenset(int(u) for u in lst[v, :cnt[v]]) for v in range(self.nv)]
+
+    def neighbor_info(self):
+        m = C.c_int()
+        c, vc, t = D(), D(), D()
+        cap, vcap, nr, ncr = I64(), I64(), I64(), I64()
+        self._f("neighbor_info")(self.h, C.byref(m), C.byref(c), C.byref(vc), C.byref(t),
+                                 C.byref(cap), C.byref(vcap), C.byref(nr), C.byref(ncr))
+        return dict(method=m.value, cutoff=c.value, vertex_cutoff=vc.value, thr2=t.value,
+                    cap=cap.value, vertex_cap=vcap.value, n_rebuilds=nr.value,
+                    n_cell_rebuilds=ncr.value)
+
+
+def bumpy_packing(n_bodies, phi, seed, n_small=20, seg=0.9, size_ratio=1.4, count_ratio=0.5,
+                  kind="oracle"):
+    """Reference-style rigid bumpy initial state (RigidBumpy::initializeFromConfig,
+    src/particles/rigid_bumpy/rigid_bumpy.cu:138-230): bidisperse radii, vertex
+    counts n_small / floor(n_small * d_max / d_min), vertex radius from the
+    segment rule, box at packing fraction phi of the disk area, positions and
+    angles from the reference's uniform generator (angles share the positions'
+    x stream, as the reference's offsets do), vertex energy scale
+    e_c * (2 r_v / d_min)^2."""
+    n = int(n_bodies)
+    n_large = int(n * count_ratio)
+    r = np.full(n, 0.5)
+    r[:n_large] = size_ratio / 2.0
+    a = 0.0
+    for v in r:
+        a += v * v
+    L = (a * 3.141592653589793238462643383279502884197 / phi) ** 0.5
+    x = fill_uniform(n, 0.0, L, 0, seed, kind)
+    y = fill_uniform(n, 0.0, L, n, seed, kind)
+    th = fill_uniform(n, 0.0, 2 * np.pi, 0, seed, kind)
+    d_min, d_max = 1.0, size_ratio
+    n_lg = int(n_small * d_max / d_min)
+    nvb = np.where(r == d_max / 2.0, n_lg, n_small).astype(np.int64)
+    rv = bumpy_vertex_radius(d_min, n_small, seg)
+    e_c = 1.0 * (2.0 * rv / d_min) ** 2
+    return dict(x=x, y=y, th=th, r=r, nvb=nvb, nv=int(nvb.sum()), box=L, rv=rv, e_c=e_c, seg=seg)
