@@ -12,6 +12,7 @@
 #include "dpg_device.cuh"
 
 namespace dpg {
+namespace {  // kernels have internal linkage: each translation unit owns its copy
 
 __device__ __forceinline__ bool halted(const DevSys *ds) { return ds->s.flags != 0; }
 
@@ -810,4 +811,5 @@ __global__ void k_snapshot(DevSys *ds, int dir) {
     }
 }
 
+}  // namespace
 }  // namespace dpg

@@ -22,6 +22,7 @@
 
 #include "../../include/dpg.h"
 #include "disk_kernels.cuh"
+#include "host_common.h"
 
 using namespace dpg;
 
@@ -30,13 +31,14 @@ using namespace dpg;
 // ---------------------------------------------------------------------------
 static thread_local char g_err[512] = "";
 
-static int set_err(int code, const char *fmt, ...) {
+int dpg::set_error(int code, const char *fmt, ...) {
     va_list ap;
     va_start(ap, fmt);
     vsnprintf(g_err, sizeof(g_err), fmt, ap);
     va_end(ap);
     return code;
 }
+#define set_err dpg::set_error
 
 #define CK(x)                                                                        \
     do {                                                                             \

@@ -24,6 +24,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", str(REP
 # so its arithmetic is the reference's, operation for operation.
 UNITS = [
     ("disk_system.cu", ["--fmad=false"]),
+    ("bumpy_system.cu", ["--fmad=false"]),
 ]
 
 

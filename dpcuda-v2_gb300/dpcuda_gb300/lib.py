@@ -52,6 +52,12 @@ class FireResult(C.Structure):
                 ("max_force", D), ("alpha", D), ("dt", D)]
 
 
+class BumpyParams(C.Structure):
+    _fields_ = [("n_bodies", I64), ("n_vertices", I64), ("box_x", D), ("box_y", D), ("e_c", D),
+                ("n_c", D), ("vertex_radius", D), ("segment_length_per_vertex_diameter", D),
+                ("rotation", I32), ("precision", I32)]
+
+
 # name -> argtypes (all return int status unless listed in _RESTYPES)
 SIGNATURES = {
     "dpg_create": [C.POINTER(Params), VP, C.POINTER(VP)],
@@ -95,6 +101,29 @@ SIGNATURES = {
     "dpg_save_state": [VP],
     "dpg_restore_state": [VP],
     "dpg_profile_loop": [VP, I32, I32, D, DP, I64P],
+    "dpg_bumpy_create": [C.POINTER(BumpyParams), VP, C.POINTER(VP)],
+    "dpg_bumpy_destroy": [VP],
+    "dpg_bumpy_set_bodies": [VP, DP, DP, DP, DP, DP, DP, DP, I32P],
+    "dpg_bumpy_set_vertices": [VP, DP, DP],
+    "dpg_bumpy_set_mass": [VP, D],
+    "dpg_bumpy_get_bodies": [VP] + [DP] * 11,
+    "dpg_bumpy_get_vertices": [VP, DP, DP],
+    "dpg_bumpy_setup_neighbors": [VP, C.POINTER(NeighborConfig), C.POINTER(NeighborInfo)],
+    "dpg_bumpy_neighbor_info_get": [VP, C.POINTER(NeighborInfo), IP],
+    "dpg_bumpy_check_neighbors": [VP, IP],
+    "dpg_bumpy_get_vertex_neighbors": [VP, I32P, I32P, IP],
+    "dpg_bumpy_zero_forces": [VP],
+    "dpg_bumpy_compute_forces": [VP],
+    "dpg_bumpy_kick": [VP, D],
+    "dpg_bumpy_drift": [VP, D],
+    "dpg_bumpy_mix": [VP, D],
+    "dpg_bumpy_zero_velocities": [VP],
+    "dpg_bumpy_observables": [VP, DP, DP, DP, DP, DP],
+    "dpg_bumpy_nve_steps": [VP, D, I64],
+    "dpg_bumpy_fire_init": [VP, D, D],
+    "dpg_bumpy_fire_step": [VP, IP],
+    "dpg_bumpy_fire_minimize": [VP, C.POINTER(FireParams), D, C.POINTER(FireResult)],
+    "dpg_bumpy_scale_box": [VP, D],
 }
 _RESTYPES = {"dpg_last_error": C.c_char_p}
 

@@ -212,6 +212,78 @@ int dpg_scale_to_packing_fraction(dpg_handle h, double phi);
 int dpg_save_state(dpg_handle h);
 int dpg_restore_state(dpg_handle h);
 
+/* ======================================================================
+ *  Rigid bumpy bodies (src/particles/rigid_bumpy/, include/particles/rigid_bumpy/)
+ *  Bodies carry n_vertices_per_body vertex disks of one radius on a circle
+ *  of radius R - r_v; vertex-vertex harmonic contacts are reduced to body
+ *  force, torque and energy.
+ * ====================================================================== */
+typedef struct dpg_bumpy_system *dpg_bumpy_handle;
+
+typedef struct {
+    int64_t n_bodies;
+    int64_t n_vertices;  /* sum of the per-body vertex counts */
+    double box_x, box_y;
+    double e_c;          /* vertex contact energy scale (the reference's d_e_c after
+                            RigidBumpy's geometric rescaling, rigid_bumpy.cu:218-222) */
+    double n_c;
+    double vertex_radius;                      /* d_vertex_radius */
+    double segment_length_per_vertex_diameter; /* sets the rebuild threshold */
+    int rotation;                              /* RigidBumpy::rotation */
+    int precision;                             /* DPG_FP64 */
+} dpg_bumpy_params;
+
+/* RigidBumpy construction (rigid_bumpy.cu:138-230, allocation part) */
+int dpg_bumpy_create(const dpg_bumpy_params *p, void *cuda_stream, dpg_bumpy_handle *out);
+int dpg_bumpy_destroy(dpg_bumpy_handle h);
+/* Bodies in static order: positions, angles, velocities, angular velocities
+ * (may be NULL = 0), radii and vertex counts; places the vertices on each
+ * body (kernelInitializeVerticesOnParticles, kernels.cu:1137-1162). */
+int dpg_bumpy_set_bodies(dpg_bumpy_handle h, const double *x, const double *y,
+                         const double *angle, const double *vx, const double *vy,
+                         const double *omega, const double *radii,
+                         const int32_t *n_vertices_per_body);
+/* explicit vertex positions in static vertex order (vertex_positions setData) */
+int dpg_bumpy_set_vertices(dpg_bumpy_handle h, const double *vx, const double *vy);
+/* RigidBumpy::setMass (rigid_bumpy.cu:1068-1080): body mass, vertex masses, moments of inertia */
+int dpg_bumpy_set_mass(dpg_bumpy_handle h, double mass);
+/* bodies back in static order; any pointer may be NULL */
+int dpg_bumpy_get_bodies(dpg_bumpy_handle h, double *x, double *y, double *angle, double *vx,
+                         double *vy, double *omega, double *fx, double *fy, double *torque,
+                         double *pe, double *inertia);
+int dpg_bumpy_get_vertices(dpg_bumpy_handle h, double *vx, double *vy);
+/* setupNeighbors with RigidBumpy::setNeighborSize (rigid_bumpy.cu:1229-1250):
+ * body list + vertex list, then calculateForces (+=). */
+int dpg_bumpy_setup_neighbors(dpg_bumpy_handle h, const dpg_neighbor_config *cfg,
+                              dpg_neighbor_info *info);
+int dpg_bumpy_neighbor_info_get(dpg_bumpy_handle h, dpg_neighbor_info *info, int *vertex_capacity);
+/* checkForNeighborUpdate (body displacement only, as the reference) */
+int dpg_bumpy_check_neighbors(dpg_bumpy_handle h, int *rebuilt);
+/* vertex neighbour list in static vertex indices, row-major [n_vertices * cap] */
+int dpg_bumpy_get_vertex_neighbors(dpg_bumpy_handle h, int32_t *list, int32_t *counts, int *cap);
+/* zeroForceAndPotentialEnergy / calculateForces (rigid_bumpy.cu:1088-1105,1378-1381) */
+int dpg_bumpy_zero_forces(dpg_bumpy_handle h);
+int dpg_bumpy_compute_forces(dpg_bumpy_handle h);
+/* updateVelocities / updatePositions (rigid_bumpy.cu:1107-1130) */
+int dpg_bumpy_kick(dpg_bumpy_handle h, double dt);
+int dpg_bumpy_drift(dpg_bumpy_handle h, double dt);
+/* mixVelocitiesAndForces / setVelocitiesToZero (rigid_bumpy.cu:1192-1196,1256-1260) */
+int dpg_bumpy_mix(dpg_bumpy_handle h, double alpha);
+int dpg_bumpy_zero_velocities(dpg_bumpy_handle h);
+/* totals: PE, KE (translational + rotational), FIRE power (with tau.omega),
+ * max |F_b| and max |tau_b| */
+int dpg_bumpy_observables(dpg_bumpy_handle h, double *pe, double *ke, double *power,
+                          double *max_force, double *max_torque);
+int dpg_bumpy_nve_steps(dpg_bumpy_handle h, double dt, int64_t n_steps);
+int dpg_bumpy_fire_init(dpg_bumpy_handle h, double alpha_init, double dt);
+int dpg_bumpy_fire_step(dpg_bumpy_handle h, int *stopped);
+/* minimizeFire with the rigid overrides; p->fmax_target > 0 stops at
+ * max|F_b| <= fmax_target and max|tau_b| <= tmax_target */
+int dpg_bumpy_fire_minimize(dpg_bumpy_handle h, const dpg_fire_params *p, double tmax_target,
+                            dpg_fire_result *r);
+/* scalePositionsFull (rigid_bumpy.cu:1044-1048) with the box: Particle::scaleBox */
+int dpg_bumpy_scale_box(dpg_bumpy_handle h, double factor);
+
 /* ---- measurement ------------------------------------------------------ */
 /* Runs `iters` iterations of a device loop (kind 0 = FIRE from the current
  * state, as dpg_fire_minimize's body; kind 1 = NVE with step dt) as plain

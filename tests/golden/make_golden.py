@@ -22,8 +22,8 @@ HERE = Path(__file__).resolve().parent
 ROOT = HERE.parent.parent
 sys.path.insert(0, str(ROOT))
 
-from oracle.oracle import (DiskOracle, build_reference, disk_packing, fill_normal,  # noqa: E402
-                           fill_uniform)
+from oracle.oracle import (BumpyOracle, DiskOracle, build_reference, bumpy_packing,  # noqa: E402
+                           disk_packing, fill_normal, fill_uniform)
 
 CUT_MULT = 1.7 / 1.4  # r_c = d_max + skin 0.3 with d_max = 1.4
 
@@ -142,6 +142,46 @@ def make_rng():
     np.savez_compressed(HERE / "rng_uniform.npz", **d)
 
 
+def padded_sets(sets):
+    width = max(1, max(len(x) for x in sets))
+    out = np.full((len(sets), width), -1, dtype=np.int32)
+    for i, x in enumerate(sets):
+        row = sorted(x)
+        out[i, :len(row)] = row
+    return out
+
+
+def bumpy_snapshot(b: BumpyOracle, prefix: str, d: dict):
+    bd = b.bodies()
+    for k in ("x", "y", "th", "vx", "vy", "w", "fx", "fy", "tq", "pe"):
+        d[f"{prefix}_{k}"] = bd[k]
+    d[f"{prefix}_px"], d[f"{prefix}_py"] = b.vertices()
+
+
+def make_bumpy(nb, phi, seed, name):
+    """Rigid bumpy bodies (cfg4 parity variant: 20 / 28 vertices, seg 0.9)."""
+    d = {}
+    st = bumpy_packing(nb, phi, seed, kind="reference")
+    b = BumpyOracle(nb, st["nv"], st["box"], st["e_c"], 2.0, st["rv"], st["seg"], True,
+                    kind="reference")
+    b.set_bodies(st["x"], st["y"], st["th"], st["r"], st["nvb"])
+    b.init_vertices()
+    b.set_mass(1.0)
+    d.update(x0=st["x"], y0=st["y"], th0=st["th"], r=st["r"], nvb=st["nvb"], box=st["box"],
+             rv=st["rv"], e_c=st["e_c"], seg=st["seg"])
+    d["px0"], d["py0"] = b.vertices()
+    d["I"] = b.bodies()["I"]
+    d["method"] = b.setup_neighbors(0, 1.5, 0.2, 8.0, 0.5)
+    bumpy_snapshot(b, "setup", d)
+    d["setup_vneighbors"] = padded_sets(b.vertex_neighbor_sets())
+    b.fire_init(0.1, 1e-2)
+    for _ in range(60):
+        b.fire_step()
+    bumpy_snapshot(b, "fire60", d)
+    d["fire60_info"] = np.array([b.neighbor_info()["n_rebuilds"], b.neighbor_info()["n_cell_rebuilds"]])
+    np.savez_compressed(HERE / name, **d)
+
+
 if __name__ == "__main__":
     if build_reference() is None:
         sys.exit("reference tree not available; cannot regenerate fixtures")
@@ -149,4 +189,6 @@ if __name__ == "__main__":
     make_small()
     make_cfg1()
     make_fire_min()
+    make_bumpy(64, 0.80, 3, "bumpy_n64_verlet.npz")
+    make_bumpy(256, 0.80, 5, "bumpy_n256_cell.npz")
     print("fixtures written to", HERE)
