@@ -28,8 +28,14 @@ __device__ __forceinline__ double disk_pair(double xi, double yi, double ri, dou
     if (d2 >= rs * rs) { fx = 0.0; fy = 0.0; return 0.0; }
     double d = sqrt(d2);
     double ov = 1.0 - (d / rs);
-    double ovp = (n_c == 2.0) ? ov : pow(ov, n_c - 1);
-    double energy = e_c * ov * ovp / (2.0 * n_c);
+    double ovp, energy;
+    if (n_c == 2.0) {  // pow(ov, 1) == ov, and x / 4 == x * 0.25 exactly
+        ovp = ov;
+        energy = e_c * ov * ovp * 0.25;
+    } else {
+        ovp = pow(ov, n_c - 1);
+        energy = e_c * ov * ovp / (2.0 * n_c);
+    }
     double fm = e_c * ovp / (rs * d);
     fx = fm * dx;
     fy = fm * dy;

@@ -89,7 +89,11 @@ struct dpg_system {
     double chunk_dt = 0.0;
     int kernel_launches = 0;  // launches issued by the last loop call (bench bookkeeping)
 
-    int grid(int count) const { return std::max(1, (count + kTPB - 1) / kTPB); }
+    // threads per block of the per-particle kernels: small systems use small
+    // blocks so the grid still spreads over every SM
+    int tpb = kTPB;
+    int grid(int count) const { return std::max(1, (count + tpb - 1) / tpb); }
+    int grid_full(int count) const { return std::max(1, (count + kTPB - 1) / kTPB); }
 };
 
 static int dalloc(dpg_system *s, void **p, size_t bytes) {
@@ -160,6 +164,12 @@ extern "C" int dpg_create(const dpg_params *p, void *cuda_stream, dpg_handle *ou
     if (m && !strcmp(m, "stream")) s->mode = kModeStream;
     else if (m && !strcmp(m, "graph")) s->mode = kModeGraph;
     const size_t n = s->n;
+    int dev = 0, nsm = 148;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    s->tpb = kTPB;
+    while (s->tpb > 32 && (long long)s->n < (long long)s->tpb * 2 * nsm) s->tpb >>= 1;
+    const char *tp = getenv("DPG_TPB");
+    if (tp && atoi(tp) >= 32 && atoi(tp) <= kTPB) s->tpb = atoi(tp) & ~31;
     int rc = DPG_OK;
     auto A = [&](void **pp, size_t b) { if (rc == DPG_OK) rc = dalloc(s, pp, b); };
     DevView &v = s->h.v;
@@ -172,7 +182,7 @@ extern "C" int dpg_create(const dpg_params *p, void *cuda_stream, dpg_handle *ou
     A((void **)&w.pos_n, n * 16); A((void **)&w.pos_c, n * 16); A((void **)&w.pe, n * 8);
     A((void **)&w.count, n * 4); A((void **)&w.cell_raw, n * 4); A((void **)&w.cell_of, n * 4);
     A((void **)&w.perm, n * 4);
-    w.max_blocks = s->grid(s->n);
+    w.max_blocks = std::max(s->grid(s->n), s->grid_full(s->n));
     A((void **)&w.partials, (size_t)w.max_blocks * 8 * 8);
     A((void **)&w.s_pos, n * 16); A((void **)&w.s_vel, n * 16); A((void **)&w.s_frc, n * 16);
     A((void **)&w.s_rad, n * 8); A((void **)&w.s_mass, n * 8); A((void **)&w.s_sidx, n * 4);
@@ -189,7 +199,7 @@ extern "C" int dpg_create(const dpg_params *p, void *cuda_stream, dpg_handle *ou
     memset(&s->h.s, 0, sizeof(DevState));
     rc = [&]() -> int {
         CK(cudaMemcpyAsync(s->d, &s->h, sizeof(DevSys), cudaMemcpyHostToDevice, s->stream));
-        LAUNCH(k_iota_sidx, s->grid(s->n), kTPB, s->d);
+        LAUNCH(k_iota_sidx, s->grid(s->n), s->tpb, s->d);
         CK(cudaStreamSynchronize(s->stream));
         return DPG_OK;
     }();
@@ -236,7 +246,7 @@ static int put_xy(dpg_system *s, int which, const double *x, const double *y, in
     const double *dx, *dy;
     TRY(stage_in(s, x, where, 0, &dx));
     TRY(stage_in(s, y, where, 1, &dy));
-    LAUNCH(k_put_xy, s->grid(s->n), kTPB, s->d, which, dx, dy);
+    LAUNCH(k_put_xy, s->grid(s->n), s->tpb, s->d, which, dx, dy);
     if (where == DPG_HOST) CK(cudaStreamSynchronize(s->stream));
     return DPG_OK;
 }
@@ -253,7 +263,7 @@ extern "C" int dpg_set_state(dpg_handle s, const double *x, const double *y, con
         if (!scal[k]) continue;
         const double *dp;
         TRY(stage_in(s, scal[k], where, 0, &dp));
-        LAUNCH(k_put_scalar, s->grid(s->n), kTPB, s->d, k, dp);
+        LAUNCH(k_put_scalar, s->grid(s->n), s->tpb, s->d, k, dp);
         if (where == DPG_HOST) CK(cudaStreamSynchronize(s->stream));
     }
     if (radii) {
@@ -283,10 +293,10 @@ extern "C" int dpg_get_state(dpg_handle s, double *x, double *y, double *vx, dou
         double *ox = outs[k][0], *oy = outs[k][1];
         if (!ox && !oy) continue;
         if (where == DPG_DEVICE) {
-            LAUNCH(k_get_xy, s->grid(s->n), kTPB, s->d, k, ox, oy);
+            LAUNCH(k_get_xy, s->grid(s->n), s->tpb, s->d, k, ox, oy);
         } else {
             double *sx = s->xfer, *sy = s->xfer + s->n;
-            LAUNCH(k_get_xy, s->grid(s->n), kTPB, s->d, k, ox ? sx : nullptr, oy ? sy : nullptr);
+            LAUNCH(k_get_xy, s->grid(s->n), s->tpb, s->d, k, ox ? sx : nullptr, oy ? sy : nullptr);
             if (ox) CK(cudaMemcpyAsync(ox, sx, nb, cudaMemcpyDeviceToHost, s->stream));
             if (oy) CK(cudaMemcpyAsync(oy, sy, nb, cudaMemcpyDeviceToHost, s->stream));
             CK(cudaStreamSynchronize(s->stream));
@@ -294,7 +304,7 @@ extern "C" int dpg_get_state(dpg_handle s, double *x, double *y, double *vx, dou
     }
     if (pe) {
         double *dst = where == DPG_DEVICE ? pe : s->xfer;
-        LAUNCH(k_get_pe, s->grid(s->n), kTPB, s->d, dst);
+        LAUNCH(k_get_pe, s->grid(s->n), s->tpb, s->d, dst);
         if (where == DPG_HOST) {
             CK(cudaMemcpyAsync(pe, dst, nb, cudaMemcpyDeviceToHost, s->stream));
             CK(cudaStreamSynchronize(s->stream));
@@ -363,7 +373,7 @@ static bool set_cell_size(dpg_system *s, double ppc, double cdm) {
 
 static int set_method(dpg_system *s, int m) {
     s->method = m;
-    LAUNCH(k_iota_sidx, s->grid(s->n), kTPB, s->d);
+    LAUNCH(k_iota_sidx, s->grid(s->n), s->tpb, s->d);
     if (m == DPG_NEIGH_ALL) {
         double diag = std::sqrt(s->h.p.box[0] * s->h.p.box[0] + s->h.p.box[1] * s->h.p.box[1]);
         set_neighbor_size(s, 2.0 * diag / max_diameter(s), 0.0);
@@ -397,19 +407,19 @@ static int alloc_nbr(dpg_system *s, int cap) {
 }
 
 static int enqueue_nlist(dpg_system *s) {
-    if (s->method == DPG_NEIGH_CELL) LAUNCH(k_nlist_cell, s->grid(s->n), kTPB, s->d);
-    else LAUNCH(k_nlist_all, s->grid(s->n), kTPB, s->d);
+    if (s->method == DPG_NEIGH_CELL) LAUNCH(k_nlist_cell, s->grid(s->n), s->tpb, s->d);
+    else LAUNCH(k_nlist_all, s->grid_full(s->n), kTPB, s->d);
     return DPG_OK;
 }
 
 // the rebuild kernels; each one checks DevState.rebuild itself
 static int enqueue_rebuild(dpg_system *s) {
     if (s->method == DPG_NEIGH_CELL) {
-        LAUNCH(k_cell_index, s->grid(s->n), kTPB, s->d);
+        LAUNCH(k_cell_index, s->grid(s->n), s->tpb, s->d);
         LAUNCH(k_cell_scan, 1, kScanTPB, s->d);
-        LAUNCH(k_cell_scatter, s->grid(s->n), kTPB, s->d);
-        LAUNCH(k_cell_sort, s->grid(s->ncells), kTPB, s->d);
-        LAUNCH(k_reorder, s->grid(s->n), kTPB, s->d);
+        LAUNCH(k_cell_scatter, s->grid(s->n), s->tpb, s->d);
+        LAUNCH(k_cell_sort, s->grid(s->ncells), s->tpb, s->d);
+        LAUNCH(k_reorder, s->grid(s->n), s->tpb, s->d);
     }
     return enqueue_nlist(s);
 }
@@ -488,7 +498,7 @@ extern "C" int dpg_setup_neighbors(dpg_handle s, const dpg_neighbor_config *cfg,
     TRY(rebuild_now(s, s->method == DPG_NEIGH_CELL ? 2 : 1));
     s->have_neighbors = true;
     // setupNeighbors ends with calculateForces (accumulating)
-    LAUNCH(k_force_acc, s->grid(s->n), kTPB, s->d);
+    LAUNCH(k_force_acc, s->grid(s->n), s->tpb, s->d);
     CK(cudaStreamSynchronize(s->stream));
     if (info) return dpg_neighbor_info_get(s, info);
     return DPG_OK;
@@ -540,7 +550,7 @@ extern "C" int dpg_get_neighbors(dpg_handle s, int32_t *list, int32_t *counts, i
     int *dl = nullptr, *dc = nullptr;
     CK(cudaMalloc((void **)&dl, (size_t)s->n * cap_out * sizeof(int)));
     CK(cudaMalloc((void **)&dc, (size_t)s->n * sizeof(int)));
-    k_get_nbrs<<<s->grid(s->n), kTPB, 0, s->stream>>>(s->d, dl, dc, cap_out);
+    k_get_nbrs<<<s->grid(s->n), s->tpb, 0, s->stream>>>(s->d, dl, dc, cap_out);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemcpyAsync(list, dl, (size_t)s->n * cap_out * 4, cudaMemcpyDeviceToHost, s->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(counts, dc, (size_t)s->n * 4, cudaMemcpyDeviceToHost, s->stream);
@@ -558,7 +568,7 @@ extern "C" int dpg_get_cells(dpg_handle s, int64_t *cell_index, int64_t *cell_st
     CK(cudaMalloc((void **)&d, 2 * nci + ncs));
     long long *dci = d, *dsi = d + s->n, *dcs = d + 2 * (size_t)s->n;
     int g = s->grid(std::max(s->n, s->ncells + 1));
-    k_get_cells<<<g, kTPB, 0, s->stream>>>(s->d, dci, s->method == DPG_NEIGH_CELL ? dcs : nullptr, dsi);
+    k_get_cells<<<g, s->tpb, 0, s->stream>>>(s->d, dci, s->method == DPG_NEIGH_CELL ? dcs : nullptr, dsi);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess && cell_index) e = cudaMemcpyAsync(cell_index, dci, nci, cudaMemcpyDeviceToHost, s->stream);
     if (e == cudaSuccess && static_index) e = cudaMemcpyAsync(static_index, dsi, nci, cudaMemcpyDeviceToHost, s->stream);
@@ -575,42 +585,42 @@ extern "C" int dpg_get_cells(dpg_handle s, int64_t *cell_index, int64_t *cell_st
 // ---------------------------------------------------------------------------
 extern "C" int dpg_zero_forces(dpg_handle s) {
     if (!s) return set_err(DPG_ERR_ARG, "null handle");
-    LAUNCH(k_zero_force, s->grid(s->n), kTPB, s->d);
+    LAUNCH(k_zero_force, s->grid(s->n), s->tpb, s->d);
     return DPG_OK;
 }
 
 extern "C" int dpg_compute_forces(dpg_handle s) {
     TRY(need_neighbors(s));
-    LAUNCH(k_force_acc, s->grid(s->n), kTPB, s->d);
+    LAUNCH(k_force_acc, s->grid(s->n), s->tpb, s->d);
     return DPG_OK;
 }
 
 extern "C" int dpg_kick(dpg_handle s, double dt) {
     if (!s) return set_err(DPG_ERR_ARG, "null handle");
-    LAUNCH(k_kick, s->grid(s->n), kTPB, s->d, dt);
+    LAUNCH(k_kick, s->grid(s->n), s->tpb, s->d, dt);
     return DPG_OK;
 }
 
 extern "C" int dpg_drift(dpg_handle s, double dt) {
     if (!s) return set_err(DPG_ERR_ARG, "null handle");
-    LAUNCH(k_drift, s->grid(s->n), kTPB, s->d, dt);
+    LAUNCH(k_drift, s->grid(s->n), s->tpb, s->d, dt);
     return DPG_OK;
 }
 
 extern "C" int dpg_mix(dpg_handle s, double alpha) {
     if (!s) return set_err(DPG_ERR_ARG, "null handle");
-    LAUNCH(k_mix, s->grid(s->n), kTPB, s->d, alpha);
+    LAUNCH(k_mix, s->grid(s->n), s->tpb, s->d, alpha);
     return DPG_OK;
 }
 
 extern "C" int dpg_zero_velocities(dpg_handle s) {
     if (!s) return set_err(DPG_ERR_ARG, "null handle");
-    LAUNCH(k_zero_vel, s->grid(s->n), kTPB, s->d);
+    LAUNCH(k_zero_vel, s->grid(s->n), s->tpb, s->d);
     return DPG_OK;
 }
 
 static int observe(dpg_system *s) {
-    LAUNCH(k_observables, s->grid(s->n), kTPB, s->d);
+    LAUNCH(k_observables, s->grid(s->n), s->tpb, s->d);
     return pull_state(s);
 }
 
@@ -639,7 +649,7 @@ extern "C" int dpg_force_stats(dpg_handle s, double *max_force, double *balance)
 
 extern "C" int dpg_pressure(dpg_handle s, double *pressure, double stress[4]) {
     TRY(need_neighbors(s));
-    LAUNCH(k_stress, s->grid(s->n), kTPB, s->d);
+    LAUNCH(k_stress, s->grid(s->n), s->tpb, s->d);
     TRY(pull_state(s));
     if (stress) for (int k = 0; k < 4; k++) stress[k] = s->hs->stress[k];
     if (pressure) *pressure = (s->hs->stress[0] + s->hs->stress[3]) / 2;
@@ -648,7 +658,7 @@ extern "C" int dpg_pressure(dpg_handle s, double *pressure, double stress[4]) {
 
 extern "C" int dpg_contact_count(dpg_handle s, double *contacts) {
     TRY(need_neighbors(s));
-    LAUNCH(k_contacts, s->grid(s->n), kTPB, s->d);
+    LAUNCH(k_contacts, s->grid(s->n), s->tpb, s->d);
     TRY(pull_state(s));
     if (contacts) *contacts = s->hs->contacts;
     return DPG_OK;
@@ -672,7 +682,7 @@ static int update_cell_size(dpg_system *s) {
 extern "C" int dpg_scale_box(dpg_handle s, double factor) {
     if (!s) return set_err(DPG_ERR_ARG, "null handle");
     if (!(factor > 0)) return set_err(DPG_ERR_ARG, "factor must be > 0");
-    LAUNCH(k_scale_pos, s->grid(s->n), kTPB, s->d, factor);
+    LAUNCH(k_scale_pos, s->grid(s->n), s->tpb, s->d, factor);
     double l = std::pow(box_area(s), 1.0 / 2);
     double nl = l * factor;
     s->h.p.box[0] = nl;
@@ -686,7 +696,7 @@ extern "C" int dpg_scale_to_packing_fraction(dpg_handle s, double phi) {
     double new_l = std::pow(particle_area(s) / phi, 1.0 / 2);
     double l = std::pow(box_area(s), 1.0 / 2);
     double f = new_l / l;
-    LAUNCH(k_scale_pos, s->grid(s->n), kTPB, s->d, f);
+    LAUNCH(k_scale_pos, s->grid(s->n), s->tpb, s->d, f);
     s->h.p.box[0] = new_l;
     s->h.p.box[1] = new_l;
     return update_cell_size(s);
@@ -694,7 +704,7 @@ extern "C" int dpg_scale_to_packing_fraction(dpg_handle s, double phi) {
 
 extern "C" int dpg_save_state(dpg_handle s) {
     if (!s) return set_err(DPG_ERR_ARG, "null handle");
-    LAUNCH(k_snapshot, s->grid(s->n), kTPB, s->d, 0);
+    LAUNCH(k_snapshot, s->grid(s->n), s->tpb, s->d, 0);
     s->h.w.s_box[0] = s->h.p.box[0];
     s->h.w.s_box[1] = s->h.p.box[1];
     return DPG_OK;
@@ -704,7 +714,7 @@ extern "C" int dpg_save_state(dpg_handle s) {
 // (neighbour list only; the cell arrays are left as they are, like the reference).
 extern "C" int dpg_restore_state(dpg_handle s) {
     TRY(need_neighbors(s));
-    LAUNCH(k_snapshot, s->grid(s->n), kTPB, s->d, 1);
+    LAUNCH(k_snapshot, s->grid(s->n), s->tpb, s->d, 1);
     s->h.p.box[0] = s->h.w.s_box[0];
     s->h.p.box[1] = s->h.w.s_box[1];
     TRY(push_params(s));
@@ -729,7 +739,7 @@ extern "C" int dpg_adam_step(dpg_handle s, int64_t step, double alpha, double b1
     if (!s->adam_ready) return set_err(DPG_ERR_STATE, "call dpg_adam_init first");
     double c1 = 1 - std::pow(b1, step + 1);
     double c2 = 1 - std::pow(b2, step + 1);
-    LAUNCH(k_adam, s->grid(s->n), kTPB, s->d, alpha, b1, b2, c1, c2, eps);
+    LAUNCH(k_adam, s->grid(s->n), s->tpb, s->d, alpha, b1, b2, c1, c2, eps);
     return DPG_OK;
 }
 
@@ -744,10 +754,10 @@ extern "C" int dpg_adam_minimize(dpg_handle s, double alpha, double b1, double b
     int64_t step = 0;
     double dof = (double)(2 * (int64_t)s->n), last = 0.0;
     while (step < max_steps) {
-        LAUNCH(k_zero_force, s->grid(s->n), kTPB, s->d);
+        LAUNCH(k_zero_force, s->grid(s->n), s->tpb, s->d);
         int rb = 0;
         TRY(dpg_check_neighbors(s, &rb));
-        LAUNCH(k_force_acc, s->grid(s->n), kTPB, s->d);
+        LAUNCH(k_force_acc, s->grid(s->n), s->tpb, s->d);
         TRY(dpg_adam_step(s, step, alpha, b1, b2, eps));
         TRY(observe(s));
         double avg = s->hs->pe / dof;
@@ -773,14 +783,14 @@ static std::vector<KNode> rebuild_nodes(const dpg_system *s) {
     std::vector<KNode> rb;
     int G = s->grid(s->n);
     if (s->method == DPG_NEIGH_CELL) {
-        rb.push_back({(void *)k_cell_index, G, kTPB});
+        rb.push_back({(void *)k_cell_index, G, s->tpb});
         rb.push_back({(void *)k_cell_scan, 1, kScanTPB});
-        rb.push_back({(void *)k_cell_scatter, G, kTPB});
-        rb.push_back({(void *)k_cell_sort, s->grid(s->ncells), kTPB});
-        rb.push_back({(void *)k_reorder, G, kTPB});
-        rb.push_back({(void *)k_nlist_cell, G, kTPB});
+        rb.push_back({(void *)k_cell_scatter, G, s->tpb});
+        rb.push_back({(void *)k_cell_sort, s->grid(s->ncells), s->tpb});
+        rb.push_back({(void *)k_reorder, G, s->tpb});
+        rb.push_back({(void *)k_nlist_cell, G, s->tpb});
     } else {
-        rb.push_back({(void *)k_nlist_all, G, kTPB});
+        rb.push_back({(void *)k_nlist_all, s->grid_full(s->n), kTPB});
     }
     return rb;
 }
@@ -788,11 +798,11 @@ static std::vector<KNode> rebuild_nodes(const dpg_system *s) {
 // Launch one iteration directly on the stream (modes stream / chunked graph).
 static int enqueue_iteration(dpg_system *s, int kind) {
     int G = s->grid(s->n);
-    if (kind == kLoopFire) LAUNCH(k_fire_move, G, kTPB, s->d);
-    else LAUNCH(k_nve_first, G, kTPB, s->d, 0.5 * s->chunk_dt, s->chunk_dt);
+    if (kind == kLoopFire) LAUNCH(k_fire_move, G, s->tpb, s->d);
+    else LAUNCH(k_nve_first, G, s->tpb, s->d, 0.5 * s->chunk_dt, s->chunk_dt);
     TRY(enqueue_rebuild(s));
-    if (kind == kLoopFire) LAUNCH(k_fire_force, G, kTPB, s->d, 0);
-    else LAUNCH(k_nve_second, G, kTPB, s->d, 0.5 * s->chunk_dt);
+    if (kind == kLoopFire) LAUNCH(k_fire_force, G, s->tpb, s->d, 0);
+    else LAUNCH(k_nve_second, G, s->tpb, s->d, 0.5 * s->chunk_dt);
     return DPG_OK;
 }
 
@@ -853,8 +863,8 @@ static int build_cond_graph(dpg_system *s, int kind) {
     int G = s->grid(s->n);
     cudaGraphNode_t last = nullptr;
     if (err == cudaSuccess) {
-        if (kind == kLoopFire) last = add_kernel(body, nullptr, (void *)k_fire_move, G, kTPB, a_d, &err);
-        else last = add_kernel(body, nullptr, (void *)k_nve_first, G, kTPB, a_nve1, &err);
+        if (kind == kLoopFire) last = add_kernel(body, nullptr, (void *)k_fire_move, G, s->tpb, a_d, &err);
+        else last = add_kernel(body, nullptr, (void *)k_nve_first, G, s->tpb, a_nve1, &err);
     }
     cudaGraphNodeParams ip = {};
     ip.type = cudaGraphNodeTypeConditional;
@@ -868,8 +878,8 @@ static int build_cond_graph(dpg_system *s, int kind) {
         cudaGraphNode_t prev = nullptr;
         for (auto &k : rebuild_nodes(s)) prev = add_kernel(ib, prev, k.fn, k.blocks, k.threads, a_d, &err);
         last = inode;
-        if (kind == kLoopFire) last = add_kernel(body, last, (void *)k_fire_force, G, kTPB, a_ff, &err);
-        else last = add_kernel(body, last, (void *)k_nve_second, G, kTPB, a_nve2, &err);
+        if (kind == kLoopFire) last = add_kernel(body, last, (void *)k_fire_force, G, s->tpb, a_ff, &err);
+        else last = add_kernel(body, last, (void *)k_nve_second, G, s->tpb, a_nve2, &err);
         last = add_kernel(body, last, (void *)k_loop_guard, 1, 1, a_d, &err);
     }
     if (err == cudaSuccess) err = cudaGraphInstantiate(&s->loop_exec[kind], g, 0);
@@ -921,8 +931,8 @@ static int run_loop(dpg_system *s, int kind, int *halted_overflow) {
 // run the interrupted iteration's second half.
 static int finish_after_overflow(dpg_system *s, int kind) {
     TRY(resolve_overflow(s));
-    if (kind == kLoopFire) LAUNCH(k_fire_force, s->grid(s->n), kTPB, s->d, 0);
-    else LAUNCH(k_nve_second, s->grid(s->n), kTPB, s->d, 0.5 * s->chunk_dt);
+    if (kind == kLoopFire) LAUNCH(k_fire_force, s->grid(s->n), s->tpb, s->d, 0);
+    else LAUNCH(k_nve_second, s->grid(s->n), s->tpb, s->d, 0.5 * s->chunk_dt);
     return pull_state(s);
 }
 
@@ -983,11 +993,11 @@ extern "C" int dpg_fire_get(dpg_handle s, double *alpha, double *dt, int64_t *n_
 extern "C" int dpg_fire_step(dpg_handle s, int *stopped) {
     TRY(need_neighbors(s));
     TRY(put_field(s, &s->d->s.flags, 0));
-    LAUNCH(k_fire_power_decide, s->grid(s->n), kTPB, s->d);
-    LAUNCH(k_fire_move, s->grid(s->n), kTPB, s->d);
+    LAUNCH(k_fire_power_decide, s->grid(s->n), s->tpb, s->d);
+    LAUNCH(k_fire_move, s->grid(s->n), s->tpb, s->d);
     TRY(enqueue_rebuild(s));
     TRY(resolve_overflow(s));
-    LAUNCH(k_fire_force, s->grid(s->n), kTPB, s->d, 2);
+    LAUNCH(k_fire_force, s->grid(s->n), s->tpb, s->d, 2);
     TRY(pull_state(s));
     if (stopped) *stopped = s->hs->f_stopped;
     TRY(put_field(s, &s->d->s.flags, 0));
@@ -1015,11 +1025,11 @@ extern "C" int dpg_fire_minimize(dpg_handle s, const dpg_fire_params *p, dpg_fir
     st.h_rb = 0;
     CK(cudaMemcpyAsync(&s->d->s, &st, sizeof(DevState), cudaMemcpyHostToDevice, s->stream));
     // minimizeFire setup: v = 0, zero, neighbour check, forces, last PE
-    LAUNCH(k_zero_vel, s->grid(s->n), kTPB, s->d);
+    LAUNCH(k_zero_vel, s->grid(s->n), s->tpb, s->d);
     LAUNCH(k_decide_rebuild, 1, 1, s->d);
     TRY(enqueue_rebuild(s));
     TRY(resolve_overflow(s));
-    LAUNCH(k_fire_force, s->grid(s->n), kTPB, s->d, 1);
+    LAUNCH(k_fire_force, s->grid(s->n), s->tpb, s->d, 1);
     for (int guard = 0; guard < 64; guard++) {
         TRY(pull_state(s));
         if (s->hs->flags & kDone) break;
@@ -1033,7 +1043,7 @@ extern "C" int dpg_fire_minimize(dpg_handle s, const dpg_fire_params *p, dpg_fir
     TRY(pull_state(s));
     if (!(s->hs->flags & kDone)) return set_err(DPG_ERR_STATE, "FIRE loop did not finish");
     // minimizeFire ends with setVelocitiesToZero
-    LAUNCH(k_zero_vel, s->grid(s->n), kTPB, s->d);
+    LAUNCH(k_zero_vel, s->grid(s->n), s->tpb, s->d);
     TRY(observe(s));
     if (r) {
         r->steps = s->hs->result_step;
@@ -1065,11 +1075,11 @@ extern "C" int dpg_profile_loop(dpg_handle s, int kind, int iters, double dt, do
         st.flags = 0; st.iter = 0; st.max_steps = p.max_steps; st.pe_target = 0; st.pe_diff_target = 0;
         st.fmax_target = 0; st.dof = (double)s->n; st.h_loop = 0; st.h_rb = 0;
         CK(cudaMemcpyAsync(&s->d->s, &st, sizeof(DevState), cudaMemcpyHostToDevice, s->stream));
-        LAUNCH(k_zero_vel, s->grid(s->n), kTPB, s->d);
+        LAUNCH(k_zero_vel, s->grid(s->n), s->tpb, s->d);
         LAUNCH(k_decide_rebuild, 1, 1, s->d);
         TRY(enqueue_rebuild(s));
         TRY(resolve_overflow(s));
-        LAUNCH(k_fire_force, s->grid(s->n), kTPB, s->d, 1);
+        LAUNCH(k_fire_force, s->grid(s->n), s->tpb, s->d, 1);
     } else {
         TRY(put_field(s, &s->d->s.flags, 0));
         TRY(put_field(s, &s->d->s.nve_steps_done, 0LL));
@@ -1081,13 +1091,13 @@ extern "C" int dpg_profile_loop(dpg_handle s, int kind, int iters, double dt, do
     int G = s->grid(s->n);
     for (int i = 0; i < iters && rc == DPG_OK; i++) {
         cudaEventRecord(ev[4 * i + 0], s->stream);
-        if (kind == 0) k_fire_move<<<G, kTPB, 0, s->stream>>>(s->d);
-        else k_nve_first<<<G, kTPB, 0, s->stream>>>(s->d, 0.5 * dt, dt);
+        if (kind == 0) k_fire_move<<<G, s->tpb, 0, s->stream>>>(s->d);
+        else k_nve_first<<<G, s->tpb, 0, s->stream>>>(s->d, 0.5 * dt, dt);
         cudaEventRecord(ev[4 * i + 1], s->stream);
         rc = enqueue_rebuild(s);
         cudaEventRecord(ev[4 * i + 2], s->stream);
-        if (kind == 0) k_fire_force<<<G, kTPB, 0, s->stream>>>(s->d, 0);
-        else k_nve_second<<<G, kTPB, 0, s->stream>>>(s->d, 0.5 * dt);
+        if (kind == 0) k_fire_force<<<G, s->tpb, 0, s->stream>>>(s->d, 0);
+        else k_nve_second<<<G, s->tpb, 0, s->stream>>>(s->d, 0.5 * dt);
         cudaEventRecord(ev[4 * i + 3], s->stream);
     }
     cudaError_t e = cudaStreamSynchronize(s->stream);

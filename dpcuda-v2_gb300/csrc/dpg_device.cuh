@@ -105,9 +105,13 @@ struct DevSys {
 
 // ---- shared arithmetic (reference order, see oracle/dpg_oracle.c) ----------
 
-// minimum image: include/particles/base/kernels.cuh:65-72
+// minimum image: include/particles/base/kernels.cuh:65-72, d - L * round(d / L).
+// For |d| < L/4 the quotient rounds to +-0, so the result is d (or +0 for
+// d = -0): returning d + 0.0 there is bit-identical and skips the FP64
+// division, which is expensive on GB300's FP64 pipe.
 __device__ __forceinline__ double pbc_dist(double a, double b, double L) {
     double d = a - b;
+    if (fabs(d) < 0.25 * L) return d + 0.0;
     return d - L * round(d / L);
 }
 
