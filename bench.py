@@ -356,7 +356,6 @@ def large_n_roofline(dpg, dev, sptr, peak):
     from oracle.oracle import fill_normal, fill_uniform
     n = 1 << 20
     r = fill_uniform(n, 0.4, 0.6, 7 * n, 5)
-    a = 0.0
     area = float(np.sum(r * r)) * np.pi
     L = (area / 0.84) ** 0.5
     x = fill_uniform(n, 0.0, L, 0, 5)
@@ -368,7 +367,8 @@ def large_n_roofline(dpg, dev, sptr, peak):
     vy -= vy.mean()
     s = dpg.Disk(n, L, stream=sptr)
     s.setState(x, y, vx, vy, r, np.ones(n))
-    info = s.setupNeighbors("cell", 1.5 / 1.2, 0.25, 8.0, 0.5)
+    # rebuild at half-skin: sqrt(3) |dr| > disp_mult * r_c with |dr| = 0.15, r_c = 1.5
+    info = s.setupNeighbors("cell", 1.5 / 1.2, 0.1732, 8.0, 0.5)
     prof = profile(dpg, s, kind=1, iters=200)
     k_mean = float(np.mean(s.getNeighbors()[1]))
     # k_nve_second per particle: read pos 16, rad 8, count 4, indices 4k, vel 16,
@@ -384,6 +384,32 @@ def large_n_roofline(dpg, dev, sptr, peak):
             "cutoff": info["cutoff"]}
 
 
+def ncu_case(which):
+    """Small fixed workloads for ncu captures (plain stream launches, a few
+    hundred kernels): 'fire' = 64 FIRE iterations of the 16384-disk system,
+    'nve_large' = 8 NVE steps of the 2^20-disk system."""
+    os.environ["DPG_LOOP_MODE"] = "stream"
+    import dpcuda_gb300 as dpg
+    if which == "fire":
+        st = packing(1)
+        s = dpg.Disk(N_PART, st["box"])
+        s.setState(st["x"], st["y"], None, None, st["r"], st["m"])
+        s.setupNeighbors("cell", CUT_MULT, 0.2, 8.0, 0.5)
+        r = dpg.minimizeFire(s, FIRE_ALPHA0, FIRE_DT0, 0.0, 0.0, 64, fmax_target=FMAX)
+        print(json.dumps({"ncu_case": which, "steps": r["steps"]}))
+    else:
+        from oracle.oracle import fill_uniform
+        n = 1 << 20
+        r = fill_uniform(n, 0.4, 0.6, 7 * n, 5)
+        L = (float(np.sum(r * r)) * np.pi / 0.84) ** 0.5
+        s = dpg.Disk(n, L)
+        s.setState(fill_uniform(n, 0.0, L, 0, 5), fill_uniform(n, 0.0, L, n, 5), None, None, r,
+                   np.ones(n))
+        s.setupNeighbors("cell", 1.5 / 1.2, 0.1732, 8.0, 0.5)
+        s.nveSteps(1e-2, 8)
+        print(json.dumps({"ncu_case": which, "steps": 8}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -391,7 +417,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--ncu-case", choices=["fire", "nve_large"], default=None,
+                    help="run a small fixed workload for ncu captures and exit")
     args = ap.parse_args()
+    if args.ncu_case:
+        ncu_case(args.ncu_case)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -222,6 +222,14 @@ extern "C" int dpg_destroy(dpg_handle s) {
     return DPG_OK;
 }
 
+extern "C" int dpg_get_params(dpg_handle s, dpg_params *p) {
+    if (!s || !p) return set_err(DPG_ERR_ARG, "null argument");
+    *p = s->prm;
+    p->box_x = s->h.p.box[0];
+    p->box_y = s->h.p.box[1];
+    return DPG_OK;
+}
+
 extern "C" int dpg_synchronize(dpg_handle s) {
     if (!s) return set_err(DPG_ERR_ARG, "null handle");
     CK(cudaStreamSynchronize(s->stream));
@@ -340,6 +348,22 @@ static double particle_area(const dpg_system *s) {
     double a = 0.0;
     for (double r : s->h_rad) a += r * r;
     return a * 3.141592653589793238462643383279502884197;
+}
+
+// Disk::getParticleArea (src/particles/disk/disk.cu:205-207) sums r^2 over the
+// CURRENT (cell-sorted) order, so the box scalings that use it round like the
+// reference only when the sum runs in that order.
+static int current_area(dpg_system *s, double *area) {
+    DevView v;
+    CK(cudaMemcpyAsync(&v, &s->d->v, sizeof(DevView), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    std::vector<double> r(s->n);
+    CK(cudaMemcpyAsync(r.data(), v.rad, sizeof(double) * s->n, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    double a = 0.0;
+    for (double x : r) a += x * x;
+    *area = a * 3.141592653589793238462643383279502884197;
+    return DPG_OK;
 }
 
 static double box_area(const dpg_system *s) { return 1.0 * s->h.p.box[0] * s->h.p.box[1]; }
@@ -666,7 +690,9 @@ extern "C" int dpg_contact_count(dpg_handle s, double *contacts) {
 
 extern "C" int dpg_packing_fraction(dpg_handle s, double *phi) {
     if (!s || !phi) return set_err(DPG_ERR_ARG, "null argument");
-    *phi = particle_area(s) / box_area(s);
+    double a;
+    TRY(current_area(s, &a));
+    *phi = a / box_area(s);
     return DPG_OK;
 }
 
@@ -693,7 +719,9 @@ extern "C" int dpg_scale_box(dpg_handle s, double factor) {
 extern "C" int dpg_scale_to_packing_fraction(dpg_handle s, double phi) {
     if (!s) return set_err(DPG_ERR_ARG, "null handle");
     if (!(phi > 0)) return set_err(DPG_ERR_ARG, "phi must be > 0");
-    double new_l = std::pow(particle_area(s) / phi, 1.0 / 2);
+    double a;
+    TRY(current_area(s, &a));
+    double new_l = std::pow(a / phi, 1.0 / 2);
     double l = std::pow(box_area(s), 1.0 / 2);
     double f = new_l / l;
     LAUNCH(k_scale_pos, s->grid(s->n), s->tpb, s->d, f);

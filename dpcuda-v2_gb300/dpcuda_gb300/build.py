@@ -25,6 +25,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", str(REP
 UNITS = [
     ("disk_system.cu", ["--fmad=false"]),
     ("bumpy_system.cu", ["--fmad=false"]),
+    ("jam.cpp", []),
 ]
 
 
@@ -35,6 +36,7 @@ def _nvcc() -> str:
 
 def sources() -> list[Path]:
     return sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cuh")) + sorted(CSRC.glob("*.h")) + \
+        sorted(CSRC.glob("*.cpp")) + \
         [REPO_ROOT / "include" / "dpg.h"]
 
 

@@ -58,10 +58,31 @@ class BumpyParams(C.Structure):
                 ("rotation", I32), ("precision", I32)]
 
 
+class JamParams(C.Structure):
+    _fields_ = [("pressure_low", D), ("pressure_high", D), ("compression_rate", D),
+                ("length_tolerance", D), ("decompress_factor", D), ("max_compression_steps", I64),
+                ("fire", FireParams), ("neighbors", NeighborConfig)]
+
+
+class JamResult(C.Structure):
+    _fields_ = [("packing_fraction", D), ("pressure", D), ("box_length", D), ("contacts", D),
+                ("compression_steps", I64), ("fire_steps_total", I64), ("status", I32),
+                ("reserved", I32)]
+
+
+class JamPhiParams(C.Structure):
+    _fields_ = [("avg_pe_tolerance", D), ("avg_pe_diff_tolerance", D), ("phi_tolerance", D),
+                ("compression_increment", D), ("delta_phi_stability", D),
+                ("max_compression_steps", I64)]
+
+
 # name -> argtypes (all return int status unless listed in _RESTYPES)
 SIGNATURES = {
     "dpg_create": [C.POINTER(Params), VP, C.POINTER(VP)],
     "dpg_destroy": [VP],
+    "dpg_get_params": [VP, C.POINTER(Params)],
+    "dpg_jam_pressure": [VP, C.POINTER(JamParams), C.POINTER(JamResult)],
+    "dpg_jam_phi": [VP, C.POINTER(JamPhiParams), C.POINTER(JamResult)],
     "dpg_last_error": [],
     "dpg_version": [],
     "dpg_set_state": [VP, DP, DP, DP, DP, DP, DP, I32],

@@ -115,6 +115,8 @@ typedef struct {
  * (src/particles/disk/disk.cu:98-170).  stream may be NULL (own stream). */
 int dpg_create(const dpg_params *p, void *cuda_stream, dpg_handle *out);
 int dpg_destroy(dpg_handle h);
+/* the parameters the handle was created with, box updated (Particle::n_particles, e_c, n_c) */
+int dpg_get_params(dpg_handle h, dpg_params *p);
 const char *dpg_last_error(void);
 int dpg_version(void);
 
@@ -211,6 +213,49 @@ int dpg_scale_to_packing_fraction(dpg_handle h, double phi);
  * (src/particles/base/particle.cu:956-991) */
 int dpg_save_state(dpg_handle h);
 int dpg_restore_state(dpg_handle h);
+
+/* ---- jamming drivers (host control flow over the entry points above) ----- */
+/* Pressure-band jamming by bisection on the box length:
+ * scripts/runArthurJamWithFire.cpp:36-106.  Decompress (scaleBox by
+ * decompress_factor) until P < pressure_low; then minimise, measure P, and
+ * compress by compression_rate while unjammed, bisect on L once jammed
+ * (P > pressure_high), reloading the last unjammed state; stop when
+ * pressure_low <= P <= pressure_high and contacts > 2N. */
+typedef struct {
+    double pressure_low, pressure_high;
+    double compression_rate;        /* L <- L * rate while unjammed without a bracket */
+    double length_tolerance;        /* |L_low / L_high - 1| below this: give up */
+    double decompress_factor;       /* initial scaleBox factor (1.01 in the reference) */
+    int64_t max_compression_steps;
+    dpg_fire_params fire;           /* each minimisation (minimizeFire defaults in the reference) */
+    dpg_neighbor_config neighbors;  /* used to reload the saved state */
+} dpg_jam_params;
+
+typedef struct {
+    double packing_fraction;
+    double pressure;
+    double box_length;
+    double contacts;
+    int64_t compression_steps;
+    int64_t fire_steps_total;
+    int status;  /* 0 final state reached, 1 length tolerance hit, 2 out of steps */
+    int reserved;
+} dpg_jam_result;
+
+int dpg_jam_pressure(dpg_handle h, const dpg_jam_params *p, dpg_jam_result *r);
+
+/* Energy-criterion jamming by bisection on phi: scripts/runJam.cpp:25-106
+ * (decompress until PE/N < avg_pe_tolerance; compress by compression_increment;
+ * jammed when PE/N > tolerance after FIRE; revertToLastState; bisect until
+ * |phi_high / phi_low - 1| < phi_tolerance, then the stability check
+ * scripts/runJam.cpp:15-23). */
+typedef struct {
+    double avg_pe_tolerance, avg_pe_diff_tolerance;
+    double phi_tolerance, compression_increment, delta_phi_stability;
+    int64_t max_compression_steps;
+} dpg_jam_phi_params;
+
+int dpg_jam_phi(dpg_handle h, const dpg_jam_phi_params *p, dpg_jam_result *r);
 
 /* ======================================================================
  *  Rigid bumpy bodies (src/particles/rigid_bumpy/, include/particles/rigid_bumpy/)
