@@ -762,6 +762,13 @@ __global__ void k_get_xy(DevSys *ds, int which, double *x, double *y) {
     if (y) y[k] = o.y;
 }
 
+// which: 0 radii, 1 masses (static order out)
+__global__ void k_get_scalar(DevSys *ds, int which, double *out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ds->p.n) return;
+    out[ds->v.sidx[i]] = (which == 0 ? ds->v.rad : ds->v.mass)[i];
+}
+
 __global__ void k_get_pe(DevSys *ds, double *out) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= ds->p.n) return;

@@ -286,6 +286,28 @@ extern "C" int dpg_set_state(dpg_handle s, const double *x, const double *y, con
     return DPG_OK;
 }
 
+extern "C" int dpg_load_state(dpg_handle s, const double *x, const double *y, const double *vx,
+                              const double *vy, const double *radii, const double *masses,
+                              int where) {
+    if (!s || !x || !y || !radii || !masses) return set_err(DPG_ERR_ARG, "dpg_load_state: null argument");
+    LAUNCH(k_iota_sidx, s->grid(s->n), s->tpb, s->d);
+    LAUNCH(k_zero_force, s->grid(s->n), s->tpb, s->d);
+    LAUNCH(k_zero_vel, s->grid(s->n), s->tpb, s->d);
+    return dpg_set_state(s, x, y, vx, vy, radii, masses, where);
+}
+
+extern "C" int dpg_get_static_params(dpg_handle s, double *radii, double *masses) {
+    if (!s) return set_err(DPG_ERR_ARG, "null handle");
+    double *outs[2] = {radii, masses};
+    for (int k = 0; k < 2; k++) {
+        if (!outs[k]) continue;
+        LAUNCH(k_get_scalar, s->grid(s->n), s->tpb, s->d, k, s->xfer);
+        CK(cudaMemcpyAsync(outs[k], s->xfer, sizeof(double) * s->n, cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+    }
+    return DPG_OK;
+}
+
 extern "C" int dpg_set_forces(dpg_handle s, const double *fx, const double *fy, int where) {
     if (!s) return set_err(DPG_ERR_ARG, "null handle");
     return put_xy(s, 2, fx, fy, where);

@@ -22,22 +22,22 @@ double box_length(dpg_handle h) {
     return std::pow(1.0 * bx * by, 1.0 / 2);
 }
 
-// write_restart_file("last_state"): positions, radii, masses, box (static order)
+// write_restart_file("last_state"): positions, velocities, radii, masses,
+// box, all in static order (src/io/state_log.cu:27-66)
 int save(dpg_handle h, int64_t n, Saved &s) {
     s.x.resize(n); s.y.resize(n); s.r.resize(n); s.m.resize(n);
     DPG_TRY(dpg_get_state(h, s.x.data(), s.y.data(), nullptr, nullptr, nullptr, nullptr, nullptr, DPG_HOST));
+    DPG_TRY(dpg_get_static_params(h, s.r.data(), s.m.data()));
     DPG_TRY(dpg_get_box(h, &s.bx, &s.by));
     return DPG_OK;
 }
 
-// Disk::load("last_state") (src/particles/disk/disk.cu:35-96): arrays, box,
-// then setupNeighbors (full neighbour initialisation, forces accumulated)
+// Disk::load("last_state") (src/particles/disk/disk.cu:35-96): arrays in
+// static order, box, then setupNeighbors (full neighbour initialisation)
 int load(dpg_handle h, const Saved &s, const dpg_neighbor_config &cfg) {
     std::vector<double> z(s.x.size(), 0.0);
     DPG_TRY(dpg_set_box(h, s.bx, s.by));
-    DPG_TRY(dpg_set_state(h, s.x.data(), s.y.data(), z.data(), z.data(), nullptr, nullptr, DPG_HOST));
-    DPG_TRY(dpg_set_forces(h, z.data(), z.data(), DPG_HOST));
-    DPG_TRY(dpg_zero_forces(h));
+    DPG_TRY(dpg_load_state(h, s.x.data(), s.y.data(), z.data(), z.data(), s.r.data(), s.m.data(), DPG_HOST));
     DPG_TRY(dpg_setup_neighbors(h, &cfg, nullptr));
     return DPG_OK;
 }

@@ -327,3 +327,35 @@ def minimizeAdam(particle: Disk, alpha=1e-4, beta1=0.9, beta2=0.999, epsilon=1e-
                                          float(avg_pe_diff_target), int(num_steps),
                                          C.byref(steps)))
     return steps.value
+
+
+def jamPressure(particle: Disk, pressure_low, pressure_high, compression_rate=0.99,
+                length_tolerance=1e-10, decompress_factor=1.01, max_compression_steps=1000,
+                fire=(0.1, 1e-2, 1e-16, 1e-16, 100000), neighbors=("cell", 1.5, 0.2, 8.0, 0.5)):
+    """Pressure-band jamming (scripts/runArthurJamWithFire.cpp) through the C ABI."""
+    from .lib import JamParams, JamResult
+    m = _METHODS.get(neighbors[0], neighbors[0])
+    prm = JamParams(float(pressure_low), float(pressure_high), float(compression_rate),
+                    float(length_tolerance), float(decompress_factor), int(max_compression_steps),
+                    FireParams(float(fire[0]), float(fire[1]), float(fire[2]), float(fire[3]),
+                               int(fire[4]), 0.0),
+                    NeighborConfig(int(m), *[float(v) for v in neighbors[1:]]))
+    r = JamResult()
+    check(particle.lib.dpg_jam_pressure(particle.h, C.byref(prm), C.byref(r)))
+    return dict(packing_fraction=r.packing_fraction, pressure=r.pressure, box_length=r.box_length,
+                contacts=r.contacts, compression_steps=r.compression_steps,
+                fire_steps_total=r.fire_steps_total, status=r.status)
+
+
+def jamPhi(particle: Disk, avg_pe_tolerance, avg_pe_diff_tolerance, phi_tolerance,
+           compression_increment, delta_phi_stability, max_compression_steps=1000):
+    """Energy-criterion jamming (scripts/runJam.cpp) through the C ABI."""
+    from .lib import JamPhiParams, JamResult
+    prm = JamPhiParams(float(avg_pe_tolerance), float(avg_pe_diff_tolerance), float(phi_tolerance),
+                       float(compression_increment), float(delta_phi_stability),
+                       int(max_compression_steps))
+    r = JamResult()
+    check(particle.lib.dpg_jam_phi(particle.h, C.byref(prm), C.byref(r)))
+    return dict(packing_fraction=r.packing_fraction, pressure=r.pressure, box_length=r.box_length,
+                contacts=r.contacts, compression_steps=r.compression_steps,
+                fire_steps_total=r.fire_steps_total, status=r.status)

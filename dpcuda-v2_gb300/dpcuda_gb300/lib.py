@@ -88,6 +88,8 @@ SIGNATURES = {
     "dpg_set_state": [VP, DP, DP, DP, DP, DP, DP, I32],
     "dpg_get_state": [VP, DP, DP, DP, DP, DP, DP, DP, I32],
     "dpg_set_forces": [VP, DP, DP, I32],
+    "dpg_load_state": [VP, DP, DP, DP, DP, DP, DP, I32],
+    "dpg_get_static_params": [VP, DP, DP],
     "dpg_set_box": [VP, D, D],
     "dpg_get_box": [VP, DP, DP],
     "dpg_synchronize": [VP],

@@ -130,6 +130,14 @@ int dpg_set_state(dpg_handle h, const double *x, const double *y, const double *
 int dpg_get_state(dpg_handle h, double *x, double *y, double *vx, double *vy, double *fx,
                   double *fy, double *pe, int where);
 int dpg_set_forces(dpg_handle h, const double *fx, const double *fy, int where);
+/* radii and masses in static order to host arrays (getArrayData "radii", "masses") */
+int dpg_get_static_params(dpg_handle h, double *radii, double *masses);
+/* Disk::load (src/particles/disk/disk.cu:35-96): replace positions,
+ * velocities, radii and masses from static-order arrays AND reset the internal
+ * slot order to the static order (forces and PE zeroed).  Call
+ * dpg_setup_neighbors afterwards, as load() does. */
+int dpg_load_state(dpg_handle h, const double *x, const double *y, const double *vx,
+                   const double *vy, const double *radii, const double *masses, int where);
 /* Particle::setBoxSize / getBoxSize (src/particles/base/particle.cu:694-709) */
 int dpg_set_box(dpg_handle h, double box_x, double box_y);
 int dpg_get_box(dpg_handle h, double *box_x, double *box_y);

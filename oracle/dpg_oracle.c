@@ -981,3 +981,129 @@ void orc_fill_normal(double *out, int64_t n, double mean, double stddev, int64_t
         out[i] = fma(stddev * s3, orc_erfcinv(2 * p), mean);
     }
 }
+
+/* ======================================================================
+ *  Jamming drivers: the run scripts' control flow restated
+ * ====================================================================== */
+
+/* Disk::load (src/particles/disk/disk.cu:35-96): arrays in static order, the
+ * slot order becomes the static order, velocities / forces / PE zero. */
+void orc_load_state(orc_sys *s, const double *x, const double *y, const double *r,
+                    const double *m) {
+    for (int64_t i = 0; i < s->n; i++) {
+        s->pidx[i] = i; s->sidx[i] = i;
+        s->x[i] = x[i]; s->y[i] = y[i]; s->r[i] = r[i]; s->m[i] = m[i];
+        s->vx[i] = 0; s->vy[i] = 0; s->fx[i] = 0; s->fy[i] = 0; s->pe[i] = 0;
+    }
+}
+
+static double jam_box_length(const orc_sys *s) { return pow(box_area(s), 1.0 / 2); }
+
+/* scripts/runArthurJamWithFire.cpp:36-106 */
+void orc_jam_pressure(orc_sys *s, double p_low, double p_high, double rate, double length_tol,
+                      double decompress, int64_t max_steps, double fa, double fdt, double pet,
+                      double pedt, int64_t fsteps, int method, double cm, double dm, double ppc,
+                      double cdm, orc_jam_result *r) {
+    int64_t total = 0, n = s->n;
+    double P;
+    for (int guard = 0; guard < 10000; guard++) {
+        total += orc_minimize_fire(s, fa, fdt, 1e-16, 0.0, fsteps, 0.0, NULL) + 1;
+        P = orc_pressure(s);
+        if (P < p_low) break;
+        orc_scale_box(s, decompress);
+    }
+    double *sx = dalloc(n), *sy = dalloc(n), *sr = dalloc(n), *sm = dalloc(n);
+    double sbx = 0, sby = 0;
+    double L_low = -1, L_high = -1, L_last = -1, contacts = 0;
+    int64_t step = 0;
+    int status = 2;
+    while (step < max_steps) {
+        total += orc_minimize_fire(s, fa, fdt, pet, pedt, fsteps, 0.0, NULL) + 1;
+        P = orc_pressure(s);
+        contacts = orc_contact_count(s);
+        double L = jam_box_length(s), L_prior = L;
+        if (P < p_low) {
+            L_low = L;
+            orc_get_arrays(s, sx, sy, NULL, NULL, NULL, NULL, NULL, sr, sm);
+            sbx = s->box[0]; sby = s->box[1];
+            L_last = L;
+            if (L_high != -1) { L = (L_high + L_low) / 2; L_high = -1; }
+            else L = L * rate;
+        } else {
+            if (P > p_high) {
+                L_high = L;
+                s->box[0] = sbx; s->box[1] = sby;
+                orc_load_state(s, sx, sy, sr, sm);
+                orc_setup_neighbors(s, method, cm, dm, ppc, cdm);
+                L_prior = L_last;
+                L = (L_high + L_low) / 2;
+            } else if (contacts > 2 * n) {
+                status = 0;
+                break;
+            }
+        }
+        if (L_low > 0 && L_high > 0 && fabs(L_low / L_high - 1) < length_tol) { status = 1; break; }
+        orc_scale_box(s, L / L_prior);
+        step++;
+    }
+    free(sx); free(sy); free(sr); free(sm);
+    r->pressure = orc_pressure(s);
+    r->contacts = orc_contact_count(s);
+    r->packing_fraction = orc_packing_fraction(s);
+    r->box_length = jam_box_length(s);
+    r->compression_steps = step;
+    r->fire_steps_total = total;
+    r->status = status;
+}
+
+/* scripts/runJam.cpp:15-106 */
+void orc_jam_phi(orc_sys *s, double tol, double dtol, double phi_tol, double inc, double dstab,
+                 int64_t max_steps, orc_jam_result *r) {
+    int64_t total = 0;
+    double dof = (double)s->n;
+    for (int guard = 0; guard < 10000; guard++) {
+        total += orc_minimize_fire(s, 0.1, 1e-2, tol, dtol, 100000, 0.0, NULL) + 1;
+        if (orc_total_pe(s) / dof < tol) break;
+        orc_scale_box(s, 1.1);
+    }
+    orc_set_last_state(s);
+    double phi_low = orc_packing_fraction(s), phi, phi_high = -1.0;
+    int64_t step = 0;
+    int status = 2;
+    while (step < max_steps) {
+        phi = orc_packing_fraction(s);
+        total += orc_minimize_fire(s, 0.1, 1e-2, tol, dtol, 1000000, 0.0, NULL) + 1;
+        double pe = orc_total_pe(s) / dof;
+        if (pe > tol) {
+            phi_high = phi;
+            phi = (phi_high + phi_low) / 2.0;
+            orc_revert_to_last_state(s);
+        } else {
+            orc_set_last_state(s);
+            phi_low = phi;
+            if (phi_high > 0) phi = (phi_high + phi_low) / 2.0;
+            else phi += inc;
+        }
+        if (fabs(phi_high / phi_low - 1) < phi_tol) {
+            orc_set_last_state(s);
+            orc_scale_to_packing_fraction(s, orc_packing_fraction(s) + dstab);
+            total += orc_minimize_fire(s, 0.1, 1e-2, tol, dtol, 100000, 0.0, NULL) + 1;
+            double fin = orc_total_pe(s) / dof;
+            orc_revert_to_last_state(s);
+            if (fin > 1e-1 * pow(dstab, s->n_c)) { status = 0; break; }
+            phi_low = phi;
+            phi_high = -1.0;
+            phi = orc_packing_fraction(s);
+            orc_set_last_state(s);
+        }
+        orc_scale_to_packing_fraction(s, phi);
+        step++;
+    }
+    r->pressure = orc_pressure(s);
+    r->contacts = orc_contact_count(s);
+    r->packing_fraction = orc_packing_fraction(s);
+    r->box_length = jam_box_length(s);
+    r->compression_steps = step;
+    r->fire_steps_total = total;
+    r->status = status;
+}

@@ -103,6 +103,22 @@ void orc_scale_box(orc_sys *s, double factor);
 void orc_set_last_state(orc_sys *s);
 void orc_revert_to_last_state(orc_sys *s);
 
+/* ---- jamming drivers (scripts/runArthurJamWithFire.cpp, scripts/runJam.cpp) */
+void orc_load_state(orc_sys *s, const double *x, const double *y, const double *r,
+                    const double *m); /* Disk::load: static order, slot order reset */
+typedef struct {
+    double packing_fraction, pressure, box_length, contacts;
+    int64_t compression_steps, fire_steps_total;
+    int status;
+} orc_jam_result;
+void orc_jam_pressure(orc_sys *s, double p_low, double p_high, double compression_rate,
+                      double length_tol, double decompress_factor, int64_t max_steps,
+                      double fire_alpha, double fire_dt, double pe_target, double pe_diff_target,
+                      int64_t fire_max_steps, int method, double cm, double dm, double ppc,
+                      double cdm, orc_jam_result *r);
+void orc_jam_phi(orc_sys *s, double tol, double dtol, double phi_tol, double increment,
+                 double dphi_stab, int64_t max_steps, orc_jam_result *r);
+
 /* ---- seeded initialisation (include/functors.h:17-50) ------------------ */
 void orc_fill_uniform(double *out, int64_t n, double lo, double hi, int64_t seed_offset,
                       int64_t seed);

@@ -570,3 +570,41 @@ def bumpy_packing(n_bodies, phi, seed, n_small=20, seg=0.9, size_ratio=1.4, coun
     rv = bumpy_vertex_radius(d_min, n_small, seg)
     e_c = 1.0 * (2.0 * rv / d_min) ** 2
     return dict(x=x, y=y, th=th, r=r, nvb=nvb, nv=int(nvb.sum()), box=L, rv=rv, e_c=e_c, seg=seg)
+
+
+class _OrcJamResult(C.Structure):
+    _fields_ = [("packing_fraction", D), ("pressure", D), ("box_length", D), ("contacts", D),
+                ("compression_steps", I64), ("fire_steps_total", I64), ("status", C.c_int)]
+
+
+def _jam_result(r):
+    return dict(packing_fraction=r.packing_fraction, pressure=r.pressure,
+                box_length=r.box_length, contacts=r.contacts,
+                compression_steps=r.compression_steps, fire_steps_total=r.fire_steps_total,
+                status=r.status)
+
+
+def jam_pressure(o: DiskOracle, p_low, p_high, compression_rate=0.99, length_tol=1e-10,
+                 decompress=1.01, max_steps=1000, fire=(0.1, 1e-2, 1e-16, 1e-16, 100000),
+                 neighbors=(0, 1.5, 0.2, 8.0, 0.5)):
+    """scripts/runArthurJamWithFire.cpp control flow on the oracle."""
+    lib = o.lib
+    fn = lib.orc_jam_pressure
+    fn.restype = None
+    fn.argtypes = [P, D, D, D, D, D, I64, D, D, D, D, I64, C.c_int, D, D, D, D,
+                   C.POINTER(_OrcJamResult)]
+    r = _OrcJamResult()
+    fn(o.h, p_low, p_high, compression_rate, length_tol, decompress, int(max_steps),
+       float(fire[0]), float(fire[1]), float(fire[2]), float(fire[3]), int(fire[4]),
+       int(neighbors[0]), *[float(v) for v in neighbors[1:]], C.byref(r))
+    return _jam_result(r)
+
+
+def jam_phi(o: DiskOracle, tol, dtol, phi_tol, increment, dphi_stab, max_steps=1000):
+    """scripts/runJam.cpp control flow on the oracle."""
+    fn = o.lib.orc_jam_phi
+    fn.restype = None
+    fn.argtypes = [P, D, D, D, D, D, I64, C.POINTER(_OrcJamResult)]
+    r = _OrcJamResult()
+    fn(o.h, tol, dtol, phi_tol, increment, dphi_stab, int(max_steps), C.byref(r))
+    return _jam_result(r)
