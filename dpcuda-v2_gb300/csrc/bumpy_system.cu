@@ -398,6 +398,8 @@ static int resolve_overflow(BS *s) {
         if (body) {
             TRY(put(s, &s->d->b.s.rebuild, 1));
             TRY(put(s, &s->d->b.s.n_rebuilds, s->hs->n_rebuilds - 1));
+            // the vertex list was built from the truncated body list: rebuild it too
+            TRY(put(s, &s->d->x.vlist_built, -1LL));
             if (s->method == DPG_NEIGH_CELL) LAUNCH(k_nlist_cell, s->gb(s->nb), kTPB, &s->d->b);
             else LAUNCH(k_nlist_all, s->gb(s->nb), kTPB, &s->d->b);
         } else {
