@@ -1,0 +1,627 @@
+// ensemble_kernels.cuh -- the batched form: many independent disk systems of
+// uneven size advanced together, every kernel launch covering all of them.
+//
+// Layout.  System s owns the slot range [off[s], off[s] + n[s]) of the shared
+// per-slot arrays; ranges are padded to whole blocks, so every block belongs to
+// exactly one system and per-system reductions are deterministic (block
+// partials, then the last block of the system to finish sums them in a fixed
+// order, with a compensated (Kahan) sum).  Slots are never re-sorted: each
+// system has its own cell grid, rebuilt into per-cell item lists whenever that
+// system's neighbour list is rebuilt.
+//
+// Precision.  Each system carries prec = 0 (mixed) or 1 (FP64):
+//  - mixed: positions are FP64; for the pair loop each particle also keeps an
+//    FP32 offset from the origin of its cell (cell size < 4 units, so the
+//    offset carries ~1e-7 absolute precision) and its cell coordinates; a pair
+//    displacement is (o_i - o_j) + dc * cell_size in FP32 with the periodic
+//    wrap done on the integer cell coordinates, the pair force is FP32, and
+//    the per-particle sums are FP64.  One 16-byte load per neighbour.
+//  - FP64: the reference's pair arithmetic (disk_pair).
+//  Mixed systems switch to FP64 when max|F| falls below switch_fmax (or FIRE
+//  stalls), for the final refinement.
+//
+// Control.  Per-system FIRE state, convergence tests and the pressure-band
+// jamming state machine (scripts/runArthurJamWithFire.cpp) live on the device;
+// finished systems are masked out.  One CUDA-graph WHILE loop drives
+// move -> IF(any rebuild){cells, lists} -> force -> transition -> guard.
+#pragma once
+#include "disk_kernels.cuh"
+
+namespace dpg {
+namespace {
+
+constexpr int kEB = 128;  // threads per block (slot ranges are padded to this)
+
+enum EPhase : int { kIdle = 0, kSetup = 1, kMinimize = 2 };
+enum EAction : int { kActNone = 0, kActDecompress = 1, kActCompress = 2, kActRevertScale = 3 };
+
+struct ESys {
+    // geometry
+    int off, n, blk0, nblk;
+    int ncd, cell_off;       // cell grid (ncd x ncd) and its first global cell
+    double L, cs;
+    float cs_f;
+    // loop
+    int phase, rebuild, prec, done;
+    int uphill, stopped, converged, pending;
+    long long iter, fire_total, rebuilds;
+    double dt, alpha, last_avg_pe;
+    long long ngood, nbad;
+    // results of the last force pass
+    double pe, power, fmax2, virial, contacts, max_d2;
+    // jamming (scripts/runArthurJamWithFire.cpp:36-106)
+    int jam_stage;           // 0 decompressing, 1 compressing
+    int jam_status;          // 0 final state, 1 length tolerance, 2 out of steps, -1 running
+    long long jam_step;
+    double L_low, L_high, L_last, L_saved, scale, pressure;
+    int minimizations;
+    unsigned ticket_a, ticket_b;
+};
+
+struct EParams {
+    int S, T, nblocks, cap, total_cells;
+    double e_c, n_c;
+    double cutoff2, half_skin2;
+    float cutoff2_f;
+    // FIRE
+    double alpha0, dt0, pe_target, pe_diff_target, fmax_target, switch_fmax;
+    long long max_steps;
+    // jamming
+    int jam;                 // 0: plain minimisation, 1: jamming protocol
+    double p_low, p_high, compression_rate, length_tol, decompress;
+    long long max_compressions;
+};
+
+struct EDev {
+    EParams p;
+    ESys *sys;
+    int *blk_sys;            // block -> system
+    int *slot_sys;           // slot -> system (-1 padding)
+    double2 *pos, *vel, *frc, *pos_ref, *pos_save;
+    double *rad, *mass, *pe, *vir;
+    float4 *pk;              // {offset x, offset y, radius, cell code}
+    int *cellc;              // wrapped cell code (cx | cy << 16) of each slot
+    int2 *cellu;             // unwrapped cell indices (offsets are taken from these)
+    int *nbr, *cnt;          // neighbour list [cap][T], counts
+    int *cell_cnt, *cell_start, *cell_cur, *cell_items;
+    double *part;            // [nblocks][8] block partials
+    int n_flagged, max_count, overflow, active;
+    unsigned ticket;
+    long long guard, guard_limit;
+    unsigned long long h_loop, h_rb;
+};
+
+__device__ __forceinline__ int code_of(int cx, int cy) { return cx | (cy << 16); }
+__device__ __forceinline__ int code_x(int c) { return c & 0xffff; }
+__device__ __forceinline__ int code_y(int c) { return c >> 16; }
+
+// Kahan-compensated sum of the system's block partials k (fixed order)
+__device__ double sys_sum(const EDev *e, const ESys &s, int k) {
+    double sum = 0.0, c = 0.0;
+    for (int b = 0; b < s.nblk; b++) {
+        double y = __ldcg(&e->part[(size_t)(s.blk0 + b) * 8 + k]) - c;
+        double t = sum + y;
+        c = (t - sum) - y;
+        sum = t;
+    }
+    return sum;
+}
+
+__device__ double sys_max(const EDev *e, const ESys &s, int k) {
+    double m = 0.0;
+    for (int b = 0; b < s.nblk; b++) m = fmax(m, __ldcg(&e->part[(size_t)(s.blk0 + b) * 8 + k]));
+    return m;
+}
+
+// Publish a block's partials; returns true (on thread 0) in the last block of
+// the system to arrive.  Every thread of the block must call it.
+template <int K>
+__device__ bool sys_publish(EDev *e, ESys &s, double (&v)[K], const int (&ops)[K], unsigned *ticket) {
+    __shared__ double sm[32 * K];
+    __shared__ int last;
+    block_reduce<K>(v, ops, sm);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < K; k++) e->part[(size_t)blockIdx.x * 8 + k] = v[k];
+        __threadfence();
+        unsigned t = atomicAdd(ticket, 1u);
+        last = (t == (unsigned)s.nblk - 1);
+        if (last) *ticket = 0;
+    }
+    __syncthreads();
+    if (last) __threadfence();
+    return last && threadIdx.x == 0;
+}
+
+__device__ __forceinline__ bool grid_last(EDev *e) {
+    __shared__ int last;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        unsigned t = atomicAdd(&e->ticket, 1u);
+        last = (t == gridDim.x - 1);
+        if (last) e->ticket = 0;
+    }
+    __syncthreads();
+    return last && threadIdx.x == 0;
+}
+
+// ---- FIRE decision (src/integrator/fire.cu:13-34), per system -----------------
+__device__ void e_fire_decide(const EParams &p, ESys &s, double power) {
+    if (power > 0) {
+        s.ngood++;
+        s.nbad = 0;
+        if (s.ngood > 5) {
+            s.dt = fmin(s.dt * 1.1, 10.0 * p.dt0);
+            s.alpha *= 0.99;
+        }
+        s.uphill = 0;
+    } else {
+        s.ngood = 0;
+        s.nbad++;
+        if (s.nbad > 10) {
+            s.stopped = 1;
+            s.uphill = 0;
+            return;
+        }
+        s.dt = fmax(s.dt * 0.5, 0.001 * p.dt0);
+        s.alpha = p.alpha0;
+        s.uphill = 1;
+    }
+}
+
+// ---- move -------------------------------------------------------------------
+__global__ void __launch_bounds__(kEB) e_move(EDev *e) {
+    const int sid = e->blk_sys[blockIdx.x];
+    ESys &s = e->sys[sid];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool live = s.phase == kMinimize;
+    double v[1] = {0.0};
+    if (live && i < s.off + s.n) {
+        const double dt = s.dt, alpha = s.alpha;
+        double2 u = e->vel[i], f = e->frc[i], x = e->pos[i];
+        if (s.uphill) {
+            double back = -dt / 2.0;
+            x.x = x.x + u.x * back;
+            x.y = x.y + u.y * back;
+            u = make_double2(0.0, 0.0);
+        }
+        double dtm = (dt / 2.0) / e->mass[i];
+        u.x = u.x + f.x * dtm;
+        u.y = u.y + f.y * dtm;
+        u = fire_mix(u, f, alpha);
+        x.x = x.x + u.x * dt;
+        x.y = x.y + u.y * dt;
+        e->vel[i] = u;
+        e->pos[i] = x;
+        double2 r = e->pos_ref[i];
+        double ddx = x.x - r.x, ddy = x.y - r.y;
+        v[0] = ddx * ddx + ddy * ddy;
+        if (s.prec == 0) {  // FP32 offset from the particle's (unwrapped) cell origin
+            int2 cu = e->cellu[i];
+            float4 k = e->pk[i];
+            k.x = (float)(x.x - cu.x * s.cs);
+            k.y = (float)(x.y - cu.y * s.cs);
+            e->pk[i] = k;
+        }
+    }
+    const int ops[1] = {1};
+    if (sys_publish<1>(e, s, v, ops, &s.ticket_a)) {
+        if (live) {
+            s.max_d2 = sys_max(e, s, 0);
+            if (s.max_d2 > e->p.half_skin2) s.rebuild = 1;
+        }
+        if (s.rebuild && s.phase != kIdle) atomicAdd(&e->n_flagged, 1);
+    }
+    if (grid_last(e)) {
+        int any = e->n_flagged > 0;
+        if (e->h_rb) cudaGraphSetConditional(e->h_rb, any ? 1u : 0u);
+    }
+}
+
+// ---- per-system cell lists and neighbour lists -------------------------------
+__device__ __forceinline__ bool flagged(const ESys &s) { return s.rebuild && s.phase != kIdle; }
+
+__device__ __forceinline__ int wrap_int(long long c, int ncd) {
+    long long m = c % ncd;
+    return (int)(m < 0 ? m + ncd : m);
+}
+
+__global__ void __launch_bounds__(kEB) e_cell_count(EDev *e) {
+    const int sid = e->blk_sys[blockIdx.x];
+    const ESys &s = e->sys[sid];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (!flagged(s) || i >= s.off + s.n) return;
+    double2 x = e->pos[i];
+    long long ux = __double2ll_rd(x.x / s.cs), uy = __double2ll_rd(x.y / s.cs);
+    int cx = wrap_int(ux, s.ncd), cy = wrap_int(uy, s.ncd);
+    e->cellc[i] = code_of(cx, cy);
+    e->cellu[i] = make_int2((int)ux, (int)uy);
+    atomicAdd(&e->cell_cnt[s.cell_off + cx + cy * s.ncd], 1);
+}
+
+__global__ void __launch_bounds__(kScanTPB) e_cell_scan(EDev *e) {
+    __shared__ int wsum[kScanTPB / 32];
+    __shared__ int carry_s;
+    const int nc = e->p.total_cells;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int carry = 0;
+    for (int base = 0; base < nc; base += kScanTPB) {
+        int idx = base + threadIdx.x;
+        int a = idx < nc ? e->cell_cnt[idx] : 0;
+        int incl = a;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, incl, off);
+            if (lane >= off) incl += y;
+        }
+        if (lane == 31) wsum[wid] = incl;
+        __syncthreads();
+        if (wid == 0) {
+            int w = wsum[lane], wi = w;
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                int y = __shfl_up_sync(0xffffffffu, wi, off);
+                if (lane >= off) wi += y;
+            }
+            wsum[lane] = wi - w;
+            if (lane == 31) carry_s = wi;
+        }
+        __syncthreads();
+        if (idx < nc) e->cell_start[idx] = carry + wsum[wid] + incl - a;
+        carry += carry_s;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) e->cell_start[nc] = carry;
+}
+
+__global__ void __launch_bounds__(kEB) e_cell_fill(EDev *e) {
+    const int sid = e->blk_sys[blockIdx.x];
+    const ESys &s = e->sys[sid];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (!flagged(s) || i >= s.off + s.n) return;
+    int c = e->cellc[i];
+    int g = s.cell_off + code_x(c) + code_y(c) * s.ncd;
+    int slot = e->cell_start[g] + atomicAdd(&e->cell_cur[g], 1);
+    e->cell_items[slot] = i;
+}
+
+// ascending slot order inside each cell (deterministic lists); clears counters
+__global__ void e_cell_sort(EDev *e) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= e->p.total_cells) return;
+    int b = e->cell_start[g], en = e->cell_start[g + 1];
+    int *it = e->cell_items;
+    for (int k = b + 1; k < en; k++) {
+        int key = it[k];
+        int j = k - 1;
+        while (j >= b && it[j] > key) { it[j + 1] = it[j]; j--; }
+        it[j + 1] = key;
+    }
+    e->cell_cnt[g] = 0;
+    e->cell_cur[g] = 0;
+}
+
+__global__ void __launch_bounds__(kEB) e_nlist(EDev *e) {
+    const int sid = e->blk_sys[blockIdx.x];
+    ESys &s = e->sys[sid];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool on = flagged(s);
+    int cnt = 0;
+    if (on && i < s.off + s.n) {
+        const int T = e->p.T, cap = e->p.cap, ncd = s.ncd;
+        const double L = s.L, c2 = e->p.cutoff2;
+        double2 xi = e->pos[i];
+        int c = e->cellc[i];
+        int cx = code_x(c), cy = code_y(c);
+        if (ncd >= 3 && s.cs * s.cs >= c2) {
+            for (int oy = -1; oy <= 1; oy++) {
+                int yy = pmod(cy + oy, ncd);
+                for (int ox = -1; ox <= 1; ox++) {
+                    int g = s.cell_off + pmod(cx + ox, ncd) + yy * ncd;
+                    for (int k = e->cell_start[g]; k < e->cell_start[g + 1]; k++) {
+                        int j = e->cell_items[k];
+                        if (j == i) continue;
+                        double2 xj = e->pos[j];
+                        double dx = pbc_dist(xi.x, xj.x, L), dy = pbc_dist(xi.y, xj.y, L);
+                        if (dx * dx + dy * dy < c2) {
+                            if (cnt < cap) e->nbr[(size_t)cnt * T + i] = j;
+                            cnt++;
+                        }
+                    }
+                }
+            }
+        } else {  // grid too coarse for a 3x3 stencil: all pairs of the system
+            for (int j = s.off; j < s.off + s.n; j++) {
+                if (j == i) continue;
+                double2 xj = e->pos[j];
+                double dx = pbc_dist(xi.x, xj.x, L), dy = pbc_dist(xi.y, xj.y, L);
+                if (dx * dx + dy * dy < c2) {
+                    if (cnt < cap) e->nbr[(size_t)cnt * T + i] = j;
+                    cnt++;
+                }
+            }
+        }
+        e->cnt[i] = cnt;
+        e->pos_ref[i] = xi;
+        int2 cu = e->cellu[i];
+        float4 k;
+        k.x = (float)(xi.x - cu.x * s.cs);
+        k.y = (float)(xi.y - cu.y * s.cs);
+        k.z = (float)e->rad[i];
+        k.w = __int_as_float(c);
+        e->pk[i] = k;
+    }
+    double v[1] = {(double)cnt};
+    const int ops[1] = {1};
+    if (sys_publish<1>(e, s, v, ops, &s.ticket_b)) {
+        if (on) {
+            int mx = (int)sys_max(e, s, 0);
+            atomicMax(&e->max_count, mx);
+            if (mx > e->p.cap) atomicExch(&e->overflow, 1);
+            s.rebuild = 0;
+            s.rebuilds++;
+        }
+    }
+    if (grid_last(e)) e->n_flagged = 0;
+}
+
+// ---- forces -------------------------------------------------------------------
+// FP32 pair force from offsets: displacement (o_i - o_j) + dc * cs with the
+// periodic wrap applied to the integer cell difference.
+__device__ __forceinline__ void pair_f32(const float4 a, const float4 b, int ncd, float cs,
+                                        float e_c, float &fx, float &fy, float &en, float &w,
+                                        int &contact) {
+    int ca = __float_as_int(a.w), cb = __float_as_int(b.w);
+    int dcx = code_x(ca) - code_x(cb), dcy = code_y(ca) - code_y(cb);
+    if (dcx > ncd / 2) dcx -= ncd; else if (dcx < -(ncd / 2)) dcx += ncd;
+    if (dcy > ncd / 2) dcy -= ncd; else if (dcy < -(ncd / 2)) dcy += ncd;
+    float dx = (a.x - b.x) + (float)dcx * cs;
+    float dy = (a.y - b.y) + (float)dcy * cs;
+    float rs = a.z + b.z;
+    float d2 = dx * dx + dy * dy;
+    fx = 0.f; fy = 0.f; en = 0.f; w = 0.f; contact = 0;
+    if (d2 >= rs * rs) return;
+    float d = sqrtf(d2);
+    float ov = 1.0f - d / rs;
+    float fm = e_c * ov / (rs * d);
+    fx = fm * dx;
+    fy = fm * dy;
+    en = 0.25f * e_c * ov * ov;
+    w = fx * dx + fy * dy;
+    contact = 1;
+}
+
+__global__ void __launch_bounds__(kEB) e_force(EDev *e) {
+    if (e->overflow) return;  // lists truncated: the host grows them and reruns this pass
+    const int sid = e->blk_sys[blockIdx.x];
+    ESys &s = e->sys[sid];
+    const EParams &p = e->p;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool live = s.phase != kIdle;
+    const bool setup = s.phase == kSetup;
+    // partials: 0 PE, 1 power, 2 max|F|^2, 3 virial, 4 contacts
+    double v[5] = {0, 0, 0, 0, 0};
+    if (live && i < s.off + s.n) {
+        const int T = p.T;
+        int cnt = min(e->cnt[i], p.cap);
+        double ax = 0.0, ay = 0.0, en = 0.0, wv = 0.0, nc = 0.0;
+        if (s.prec == 0) {
+            const float4 a = e->pk[i];
+            const float ecf = (float)p.e_c;
+            for (int k = 0; k < cnt; k++) {
+                int j = __ldg(&e->nbr[(size_t)k * T + i]);
+                float4 b = e->pk[j];
+                float fx, fy, ef, wf;
+                int ct;
+                pair_f32(a, b, s.ncd, s.cs_f, ecf, fx, fy, ef, wf, ct);
+                ax += (double)fx;
+                ay += (double)fy;
+                en += (double)ef;
+                wv += (double)wf;
+                nc += ct;
+            }
+        } else {
+            const double2 xi = e->pos[i];
+            const double ri = e->rad[i];
+            for (int k = 0; k < cnt; k++) {
+                int j = __ldg(&e->nbr[(size_t)k * T + i]);
+                double2 xj = e->pos[j];
+                double fx, fy;
+                double ee = disk_pair(xi.x, xi.y, ri, xj.x, xj.y, e->rad[j], s.L, s.L, p.e_c, p.n_c, fx, fy);
+                ax += fx;
+                ay += fy;
+                en += ee;
+                if (fx != 0.0 || fy != 0.0) {
+                    double dx = pbc_dist(xi.x, xj.x, s.L), dy = pbc_dist(xi.y, xj.y, s.L);
+                    wv += fx * dx + fy * dy;
+                    nc += 1.0;
+                }
+            }
+        }
+        double2 f = make_double2(ax, ay);
+        e->frc[i] = f;
+        e->pe[i] = en;
+        double2 u = e->vel[i];
+        if (!setup) {
+            double dtm = (s.dt / 2.0) / e->mass[i];
+            u.x = u.x + f.x * dtm;
+            u.y = u.y + f.y * dtm;
+            e->vel[i] = u;
+        }
+        v[0] = en;
+        v[1] = f.x * u.x + f.y * u.y;
+        v[2] = f.x * f.x + f.y * f.y;
+        v[3] = wv;
+        v[4] = nc;
+    }
+    const int ops[5] = {0, 0, 1, 0, 0};
+    if (!sys_publish<5>(e, s, v, ops, &s.ticket_a)) return;
+    if (!live) return;
+    // ---- per-system epilogue: minimizeFire tests and the next FIRE decision ----
+    s.pe = sys_sum(e, s, 0);
+    s.power = sys_sum(e, s, 1);
+    s.fmax2 = sys_max(e, s, 2);
+    s.virial = sys_sum(e, s, 3);
+    s.contacts = sys_sum(e, s, 4);
+    double avg = s.pe / (double)s.n;
+    s.fire_total++;
+    bool finished = false;
+    if (setup) {
+        s.last_avg_pe = avg;
+        s.phase = kMinimize;
+        s.iter = 0;
+        e_fire_decide(p, s, s.power);
+        return;
+    }
+    double fmax = sqrt(s.fmax2);
+    // mixed systems hand over to FP64 pair arithmetic for the final refinement
+    if (s.prec == 0 && (fmax <= p.switch_fmax || s.nbad > 5)) {
+        s.prec = 1;
+    }
+    double diff = fabs(avg / s.last_avg_pe - 1);
+    s.last_avg_pe = avg;
+    long long it = s.iter;
+    const bool decompressing = p.jam && s.jam_stage == 0;
+    const double pe_t = decompressing ? 1e-16 : p.pe_target;
+    const double pe_dt = decompressing ? 0.0 : p.pe_diff_target;
+    if (avg < pe_t || (s.prec == 1 && diff < pe_dt)) finished = true;
+    else if (p.fmax_target > 0 && fmax <= p.fmax_target && s.prec == 1) finished = true;
+    else if (it + 1 >= p.max_steps) finished = true;
+    else {
+        s.iter = it + 1;
+        e_fire_decide(p, s, s.power);
+        if (s.stopped) finished = true;
+    }
+    if (!finished) return;
+    s.converged = 1;
+    s.minimizations++;
+    if (!p.jam) { s.phase = kIdle; s.done = 1; atomicSub(&e->active, 1); return; }
+    // ---- jamming state machine (scripts/runArthurJamWithFire.cpp:36-106) ----
+    // pressure with v = 0: sum_ij r_ij . f_ij / (4 A)
+    double A = s.L * s.L;
+    s.pressure = s.virial / (4.0 * A);
+    double L = s.L;
+    if (s.jam_stage == 0) {  // decompress until P < p_low
+        if (s.pressure < p.p_low) {
+            s.jam_stage = 1;
+            // the compression loop starts with a minimisation of this state
+            s.pending = kActCompress;
+            s.scale = 1.0;
+        } else {
+            s.pending = kActDecompress;
+            s.scale = p.decompress;
+        }
+        return;
+    }
+    double L_prior = L;
+    double Lnew = L;
+    if (s.pressure < p.p_low) {
+        s.L_low = L;
+        s.L_saved = L;  // the transition kernel saves positions
+        s.L_last = L;
+        if (s.L_high != -1) { Lnew = (s.L_high + s.L_low) / 2; s.L_high = -1; }
+        else Lnew = L * p.compression_rate;
+        s.pending = kActCompress;
+    } else if (s.pressure > p.p_high) {
+        s.L_high = L;
+        L_prior = s.L_last;
+        Lnew = (s.L_high + s.L_low) / 2;
+        s.pending = kActRevertScale;
+    } else if (s.contacts > 2.0 * s.n) {
+        s.jam_status = 0;
+    } else {
+        s.pending = kActCompress;  // inside the band without enough contacts: minimise again
+    }
+    if (s.jam_status < 0 && s.L_low > 0 && s.L_high > 0 && fabs(s.L_low / s.L_high - 1) < p.length_tol)
+        s.jam_status = 1;
+    if (s.jam_status < 0 && ++s.jam_step >= p.max_compressions) s.jam_status = 2;
+    if (s.jam_status >= 0) {
+        s.pending = kActNone;
+        s.phase = kIdle;
+        s.done = 1;
+        atomicSub(&e->active, 1);
+        return;
+    }
+    s.scale = Lnew / L_prior;
+}
+
+// ---- transitions between minimisations (save / restore / scale, FIRE reset) ----
+__global__ void __launch_bounds__(kEB) e_transition(EDev *e) {
+    if (e->overflow) return;
+    const int sid = e->blk_sys[blockIdx.x];
+    ESys &s = e->sys[sid];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int act = s.pending;
+    if (act != kActNone && i < s.off + s.n) {
+        double2 x = e->pos[i];
+        if (act == kActCompress && s.pressure < e->p.p_low && s.jam_stage == 1 && s.L_saved == s.L)
+            e->pos_save[i] = x;  // write_restart_file("last_state")
+        if (act == kActRevertScale) x = e->pos_save[i];  // load("last_state")
+        x.x *= s.scale;
+        x.y *= s.scale;
+        e->pos[i] = x;
+        e->vel[i] = make_double2(0.0, 0.0);
+    }
+    double v[1] = {0.0};
+    const int ops[1] = {0};
+    if (sys_publish<1>(e, s, v, ops, &s.ticket_b) && act != kActNone) {
+        double L0 = act == kActRevertScale ? s.L_last : s.L;
+        s.L = L0 * s.scale;
+        s.cs = s.L / s.ncd;
+        s.cs_f = (float)s.cs;
+        s.pending = kActNone;
+        s.phase = kSetup;
+        s.rebuild = 1;
+        s.dt = e->p.dt0;
+        s.alpha = e->p.alpha0;
+        s.ngood = 0;
+        s.nbad = 0;
+        s.stopped = 0;
+        s.uphill = 0;
+        s.converged = 0;
+        s.iter = 0;
+        s.prec = (e->p.switch_fmax > 0 && s.ncd >= 3) ? 0 : 1;
+    }
+}
+
+// WHILE-body guard: continue while any system is active and the budget lasts
+__global__ void e_guard(EDev *e) {
+    long long g = ++e->guard;
+    int go = (e->active > 0) && (g < e->guard_limit) && !e->overflow;
+    if (e->h_loop) cudaGraphSetConditional(e->h_loop, go ? 1u : 0u);
+}
+
+// ---- transfers ------------------------------------------------------------------
+__global__ void e_put(EDev *e, const double *x, const double *y, const double *r, const double *m,
+                      const int *src_index) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= e->p.T) return;
+    int k = src_index[i];
+    if (k < 0) {
+        e->pos[i] = make_double2(0.0, 0.0);
+        e->rad[i] = 0.0;
+        e->mass[i] = 1.0;
+        return;
+    }
+    e->pos[i] = make_double2(x[k], y[k]);
+    e->rad[i] = r[k];
+    e->mass[i] = m[k];
+    e->vel[i] = make_double2(0.0, 0.0);
+    e->frc[i] = make_double2(0.0, 0.0);
+}
+
+__global__ void e_get(EDev *e, double *x, double *y, double *fx, double *fy, const int *src_index) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= e->p.T) return;
+    int k = src_index[i];
+    if (k < 0) return;
+    double2 p = e->pos[i], f = e->frc[i];
+    if (x) x[k] = p.x;
+    if (y) y[k] = p.y;
+    if (fx) fx[k] = f.x;
+    if (fy) fy[k] = f.y;
+}
+
+}  // namespace
+}  // namespace dpg

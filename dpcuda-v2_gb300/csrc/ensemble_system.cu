@@ -1,0 +1,413 @@
+// ensemble_system.cu -- host side of the batched form (dpg_ensemble_* in
+// include/dpg.h): S disk systems of uneven size in shared, block-padded slot
+// arrays; the whole minimisation / jamming run of all systems is one CUDA
+// graph (WHILE node; the rebuild kernels sit under an IF node set by the move
+// kernel when any system needs new lists).  Compiled with --fmad=false.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "ensemble_kernels.cuh"
+#include "host_common.h"
+
+using namespace dpg;
+
+#define CK DPG_CK
+#define TRY DPG_TRY
+#define set_err dpg::set_error
+
+struct dpg_ensemble_system {
+    dpg_ensemble_params prm{};
+    int S = 0, T = 0, nblocks = 0, total_cells = 0, cap = 32;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    std::vector<ESys> sys;      // host copy
+    std::vector<int> src_index;  // slot -> input index (-1 padding)
+    std::vector<long long> n;
+    EDev h{};                    // host mirror of the device block
+    EDev *d = nullptr;
+    ESys *d_sys = nullptr;
+    int *d_src = nullptr;
+    std::vector<void *> allocs;
+    double *xfer = nullptr;
+    size_t n_total = 0;
+    cudaGraphExec_t exec = nullptr;
+    cudaGraphConditionalHandle h_loop = 0, h_rb = 0;
+    bool have_state = false;
+    int mode = 2;
+};
+
+typedef dpg_ensemble_system ES;
+
+#define LAUNCH(kern, blocks, threads, ...)                        \
+    do {                                                          \
+        kern<<<(blocks), (threads), 0, s->stream>>>(__VA_ARGS__); \
+        CK(cudaGetLastError());                                   \
+    } while (0)
+
+static int ealloc(ES *s, void **p, size_t bytes) {
+    CK(cudaMalloc(p, bytes > 0 ? bytes : 16));
+    CK(cudaMemsetAsync(*p, 0, bytes > 0 ? bytes : 16, s->stream));
+    s->allocs.push_back(*p);
+    return DPG_OK;
+}
+
+extern "C" int dpg_ensemble_destroy(dpg_ensemble s) {
+    if (!s) return DPG_OK;
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    if (s->exec) cudaGraphExecDestroy(s->exec);
+    for (void *p : s->allocs) cudaFree(p);
+    if (s->h.nbr) cudaFree(s->h.nbr);
+    if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+    return DPG_OK;
+}
+
+static int alloc_nbr(ES *s, int cap) {
+    CK(cudaStreamSynchronize(s->stream));
+    if (s->h.nbr) CK(cudaFree(s->h.nbr));
+    CK(cudaMalloc((void **)&s->h.nbr, (size_t)s->T * cap * sizeof(int)));
+    s->cap = cap;
+    s->h.p.cap = cap;
+    return DPG_OK;
+}
+
+extern "C" int dpg_ensemble_create(const dpg_ensemble_params *p, const int64_t *n_particles,
+                                   const double *box, void *cuda_stream, dpg_ensemble *out) {
+    if (!p || !n_particles || !box || !out) return set_err(DPG_ERR_ARG, "dpg_ensemble_create: null argument");
+    if (p->n_systems <= 0 || p->n_systems > (1 << 20)) return set_err(DPG_ERR_ARG, "bad n_systems");
+    if (!(p->cutoff > 0) || !(p->skin > 0)) return set_err(DPG_ERR_ARG, "cutoff and skin must be > 0");
+    if (p->precision != DPG_FP64 && p->precision != DPG_MIXED) return set_err(DPG_ERR_ARG, "bad precision");
+    ES *s = new ES();
+    s->prm = *p;
+    s->S = (int)p->n_systems;
+    if (cuda_stream) s->stream = (cudaStream_t)cuda_stream;
+    else {
+        cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) { delete s; return set_err(DPG_ERR_CUDA, "stream: %s", cudaGetErrorString(e)); }
+        s->own_stream = true;
+    }
+    const char *m = getenv("DPG_LOOP_MODE");
+    if (m && (!strcmp(m, "stream") || !strcmp(m, "graph"))) s->mode = 0;
+    // layout: each system padded to whole blocks; its own cell grid
+    s->sys.assign(s->S, ESys{});
+    int slot = 0, blk = 0, cell = 0;
+    size_t in = 0;
+    for (int k = 0; k < s->S; k++) {
+        if (n_particles[k] <= 0 || !(box[k] > 0)) { delete s; return set_err(DPG_ERR_ARG, "system %d: bad size or box", k); }
+        ESys &y = s->sys[k];
+        y.off = slot;
+        y.n = (int)n_particles[k];
+        y.blk0 = blk;
+        y.nblk = (y.n + kEB - 1) / kEB;
+        y.L = box[k];
+        // cells at least 10% larger than the cutoff, so compression keeps them valid
+        y.ncd = std::max(1, (int)std::floor(y.L / (p->cutoff * 1.1)));
+        y.cell_off = cell;
+        y.cs = y.L / y.ncd;
+        y.cs_f = (float)y.cs;
+        y.jam_status = -1;
+        y.L_low = y.L_high = y.L_last = -1;
+        for (int i = 0; i < y.nblk * kEB; i++) s->src_index.push_back(i < y.n ? (int)(in + i) : -1);
+        in += y.n;
+        slot += y.nblk * kEB;
+        blk += y.nblk;
+        cell += y.ncd * y.ncd;
+        s->n.push_back(y.n);
+    }
+    s->T = slot;
+    s->nblocks = blk;
+    s->total_cells = cell;
+    s->n_total = in;
+    int rc = DPG_OK;
+    auto A = [&](void **pp, size_t b) { if (rc == DPG_OK) rc = ealloc(s, pp, b); };
+    EDev &h = s->h;
+    const size_t T = s->T;
+    A((void **)&s->d, sizeof(EDev));
+    A((void **)&s->d_sys, sizeof(ESys) * s->S);
+    A((void **)&h.blk_sys, 4 * (size_t)s->nblocks);
+    A((void **)&s->d_src, 4 * T);
+    A((void **)&h.pos, 16 * T); A((void **)&h.vel, 16 * T); A((void **)&h.frc, 16 * T);
+    A((void **)&h.pos_ref, 16 * T); A((void **)&h.pos_save, 16 * T);
+    A((void **)&h.rad, 8 * T); A((void **)&h.mass, 8 * T); A((void **)&h.pe, 8 * T);
+    A((void **)&h.pk, 16 * T); A((void **)&h.cellc, 4 * T); A((void **)&h.cellu, 8 * T);
+    A((void **)&h.cnt, 4 * T);
+    A((void **)&h.cell_cnt, 4 * ((size_t)s->total_cells + 1));
+    A((void **)&h.cell_start, 4 * ((size_t)s->total_cells + 1));
+    A((void **)&h.cell_cur, 4 * ((size_t)s->total_cells + 1));
+    A((void **)&h.cell_items, 4 * T);
+    A((void **)&h.part, 8 * 8 * (size_t)s->nblocks);
+    A((void **)&s->xfer, 8 * 4 * std::max<size_t>(s->n_total, 1));
+    if (rc == DPG_OK) rc = alloc_nbr(s, s->cap);
+    if (rc != DPG_OK) { dpg_ensemble_destroy(s); return rc; }
+    h.sys = s->d_sys;
+    h.p.S = s->S; h.p.T = s->T; h.p.nblocks = s->nblocks; h.p.cap = s->cap;
+    h.p.total_cells = s->total_cells;
+    h.p.e_c = p->e_c; h.p.n_c = p->n_c;
+    h.p.cutoff2 = p->cutoff * p->cutoff;
+    h.p.cutoff2_f = (float)h.p.cutoff2;
+    h.p.half_skin2 = (p->skin / 2) * (p->skin / 2);
+    h.p.switch_fmax = p->precision == DPG_MIXED ? (p->switch_fmax > 0 ? p->switch_fmax : 1e-7) : 0.0;
+    std::vector<int> bs(s->nblocks);
+    for (int k = 0; k < s->S; k++)
+        for (int b = 0; b < s->sys[k].nblk; b++) bs[s->sys[k].blk0 + b] = k;
+    cudaError_t e = cudaMemcpyAsync(h.blk_sys, bs.data(), 4 * bs.size(), cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(s->d_src, s->src_index.data(), 4 * T, cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(s->d_sys, s->sys.data(), sizeof(ESys) * s->S, cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(s->d, &h, sizeof(EDev), cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) { dpg_ensemble_destroy(s); return set_err(DPG_ERR_CUDA, "ensemble create: %s", cudaGetErrorString(e)); }
+    *out = s;
+    return DPG_OK;
+}
+
+extern "C" int dpg_ensemble_set_state(dpg_ensemble s, const double *x, const double *y,
+                                      const double *radii, const double *masses) {
+    if (!s || !x || !y || !radii || !masses) return set_err(DPG_ERR_ARG, "null argument");
+    const size_t n = s->n_total;
+    const double *src[4] = {x, y, radii, masses};
+    for (int k = 0; k < 4; k++)
+        CK(cudaMemcpyAsync(s->xfer + k * n, src[k], 8 * n, cudaMemcpyHostToDevice, s->stream));
+    LAUNCH(e_put, (s->T + 255) / 256, 256, s->d, s->xfer, s->xfer + n, s->xfer + 2 * n, s->xfer + 3 * n, s->d_src);
+    CK(cudaStreamSynchronize(s->stream));
+    s->have_state = true;
+    return DPG_OK;
+}
+
+extern "C" int dpg_ensemble_get_state(dpg_ensemble s, double *x, double *y, double *fx, double *fy) {
+    if (!s) return set_err(DPG_ERR_ARG, "null handle");
+    const size_t n = s->n_total;
+    double *dst[4] = {x, y, fx, fy};
+    LAUNCH(e_get, (s->T + 255) / 256, 256, s->d, x ? s->xfer : nullptr, y ? s->xfer + n : nullptr,
+           fx ? s->xfer + 2 * n : nullptr, fy ? s->xfer + 3 * n : nullptr, s->d_src);
+    for (int k = 0; k < 4; k++)
+        if (dst[k]) CK(cudaMemcpyAsync(dst[k], s->xfer + k * n, 8 * n, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return DPG_OK;
+}
+
+// ---------------------------------------------------------------------------
+static cudaGraphNode_t addk(cudaGraph_t g, cudaGraphNode_t dep, void *fn, int blocks, int threads,
+                            void **args, cudaError_t *err) {
+    cudaKernelNodeParams kp = {};
+    kp.func = fn;
+    kp.gridDim = dim3(blocks);
+    kp.blockDim = dim3(threads);
+    kp.kernelParams = args;
+    cudaGraphNode_t node = nullptr;
+    cudaError_t e = cudaGraphAddKernelNode(&node, g, dep ? &dep : nullptr, dep ? 1 : 0, &kp);
+    if (e != cudaSuccess && *err == cudaSuccess) *err = e;
+    return node;
+}
+
+static int enqueue_rebuild(ES *s) {
+    LAUNCH(e_cell_count, s->nblocks, kEB, s->d);
+    LAUNCH(e_cell_scan, 1, kScanTPB, s->d);
+    LAUNCH(e_cell_fill, s->nblocks, kEB, s->d);
+    LAUNCH(e_cell_sort, (s->total_cells + 255) / 256, 256, s->d);
+    LAUNCH(e_nlist, s->nblocks, kEB, s->d);
+    return DPG_OK;
+}
+
+static int enqueue_iteration(ES *s) {
+    LAUNCH(e_move, s->nblocks, kEB, s->d);
+    TRY(enqueue_rebuild(s));
+    LAUNCH(e_force, s->nblocks, kEB, s->d);
+    LAUNCH(e_transition, s->nblocks, kEB, s->d);
+    return DPG_OK;
+}
+
+static int build_graph(ES *s) {
+    if (s->exec) return DPG_OK;
+    cudaGraph_t g;
+    CK(cudaGraphCreate(&g, 0));
+    cudaError_t err = cudaGraphConditionalHandleCreate(&s->h_loop, g, 1, cudaGraphCondAssignDefault);
+    cudaGraphNodeParams wp = {};
+    wp.type = cudaGraphNodeTypeConditional;
+    wp.conditional.handle = s->h_loop;
+    wp.conditional.type = cudaGraphCondTypeWhile;
+    wp.conditional.size = 1;
+    cudaGraphNode_t wnode = nullptr;
+    if (err == cudaSuccess) err = cudaGraphAddNode(&wnode, g, nullptr, nullptr, 0, &wp);
+    cudaGraph_t body = err == cudaSuccess ? wp.conditional.phGraph_out[0] : nullptr;
+    if (err == cudaSuccess) err = cudaGraphConditionalHandleCreate(&s->h_rb, body, 0, 0);
+    EDev *dp = s->d;
+    void *a[] = {&dp};
+    cudaGraphNode_t last = nullptr;
+    if (err == cudaSuccess) last = addk(body, nullptr, (void *)e_move, s->nblocks, kEB, a, &err);
+    cudaGraphNodeParams ip = {};
+    ip.type = cudaGraphNodeTypeConditional;
+    ip.conditional.handle = s->h_rb;
+    ip.conditional.type = cudaGraphCondTypeIf;
+    ip.conditional.size = 1;
+    cudaGraphNode_t inode = nullptr;
+    if (err == cudaSuccess) err = cudaGraphAddNode(&inode, body, &last, nullptr, 1, &ip);
+    if (err == cudaSuccess) {
+        cudaGraph_t ib = ip.conditional.phGraph_out[0];
+        cudaGraphNode_t prev = nullptr;
+        prev = addk(ib, prev, (void *)e_cell_count, s->nblocks, kEB, a, &err);
+        prev = addk(ib, prev, (void *)e_cell_scan, 1, kScanTPB, a, &err);
+        prev = addk(ib, prev, (void *)e_cell_fill, s->nblocks, kEB, a, &err);
+        prev = addk(ib, prev, (void *)e_cell_sort, (s->total_cells + 255) / 256, 256, a, &err);
+        prev = addk(ib, prev, (void *)e_nlist, s->nblocks, kEB, a, &err);
+        last = addk(body, inode, (void *)e_force, s->nblocks, kEB, a, &err);
+        last = addk(body, last, (void *)e_transition, s->nblocks, kEB, a, &err);
+        last = addk(body, last, (void *)e_guard, 1, 1, a, &err);
+    }
+    if (err == cudaSuccess) err = cudaGraphInstantiate(&s->exec, g, 0);
+    cudaGraphDestroy(g);
+    if (err != cudaSuccess) {
+        s->exec = nullptr;
+        return set_err(DPG_ERR_CUDA, "ensemble graph: %s", cudaGetErrorString(err));
+    }
+    return DPG_OK;
+}
+
+template <class T>
+static int put(ES *s, T *dev, const T &v) {
+    CK(cudaMemcpyAsync(dev, &v, sizeof(T), cudaMemcpyHostToDevice, s->stream));
+    return DPG_OK;
+}
+
+static int pull_dev(ES *s, EDev *out) {
+    CK(cudaMemcpyAsync(out, s->d, sizeof(EDev), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return DPG_OK;
+}
+
+static int pull_sys(ES *s) {
+    CK(cudaMemcpyAsync(s->sys.data(), s->d_sys, sizeof(ESys) * s->S, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return DPG_OK;
+}
+
+static int pow2ceil(int x) { return (int)std::pow(2, std::ceil(std::log2((double)x))); }
+
+// Run the loop until every system is done.  Overflow of a neighbour list halts
+// the force pass; the host grows the lists, rebuilds them for every live system
+// and finishes that iteration before resuming.
+static int run(ES *s, long long guard_limit) {
+    for (int attempt = 0; attempt < 64; attempt++) {
+        EDev cur;
+        TRY(pull_dev(s, &cur));
+        if (cur.active <= 0) return DPG_OK;
+        TRY(put(s, &s->d->guard, 0LL));
+        TRY(put(s, &s->d->guard_limit, guard_limit));
+        bool ran = false;
+        if (s->mode == 2 && build_graph(s) == DPG_OK) {
+            TRY(put(s, &s->d->h_loop, (unsigned long long)s->h_loop));
+            TRY(put(s, &s->d->h_rb, (unsigned long long)s->h_rb));
+            CK(cudaGraphLaunch(s->exec, s->stream));
+            TRY(put(s, &s->d->h_loop, 0ULL));
+            TRY(put(s, &s->d->h_rb, 0ULL));
+            ran = true;
+        }
+        if (!ran) {
+            s->mode = 0;
+            for (long long it = 0; it < guard_limit; it++) {
+                TRY(enqueue_iteration(s));
+                if ((it & 63) == 63) {
+                    TRY(pull_dev(s, &cur));
+                    if (cur.active <= 0 || cur.overflow) break;
+                }
+            }
+        }
+        TRY(pull_dev(s, &cur));
+        if (cur.overflow) {
+            int ncap = pow2ceil(cur.max_count);
+            if ((size_t)ncap * s->T > ((size_t)1 << 31)) return set_err(DPG_ERR_OVERFLOW, "ensemble neighbour list too large");
+            TRY(alloc_nbr(s, ncap));
+            if (s->exec) { cudaGraphExecDestroy(s->exec); s->exec = nullptr; }
+            TRY(put(s, &s->d->nbr, s->h.nbr));
+            TRY(put(s, &s->d->p.cap, ncap));
+            TRY(put(s, &s->d->overflow, 0));
+            TRY(pull_sys(s));
+            for (auto &y : s->sys) if (y.phase != kIdle) y.rebuild = 1;
+            CK(cudaMemcpyAsync(s->d_sys, s->sys.data(), sizeof(ESys) * s->S, cudaMemcpyHostToDevice, s->stream));
+            TRY(put(s, &s->d->n_flagged, 1));
+            TRY(enqueue_rebuild(s));
+            LAUNCH(e_force, s->nblocks, kEB, s->d);
+            LAUNCH(e_transition, s->nblocks, kEB, s->d);
+            TRY(pull_dev(s, &cur));
+            if (cur.overflow) continue;
+            continue;
+        }
+        if (cur.active <= 0) return DPG_OK;
+        if (cur.guard >= guard_limit) return set_err(DPG_ERR_NOT_CONVERGED, "ensemble loop budget spent");
+    }
+    return set_err(DPG_ERR_STATE, "ensemble loop did not finish");
+}
+
+static int start(ES *s, const dpg_fire_params *fp, int jam, const dpg_jam_params *jp) {
+    if (!s->have_state) return set_err(DPG_ERR_STATE, "set the state first");
+    TRY(pull_sys(s));
+    EParams &p = s->h.p;
+    p.alpha0 = fp->alpha_init; p.dt0 = fp->dt;
+    p.pe_target = fp->avg_pe_target; p.pe_diff_target = fp->avg_pe_diff_target;
+    p.fmax_target = fp->fmax_target; p.max_steps = fp->max_steps;
+    p.jam = jam;
+    if (jp) {
+        p.p_low = jp->pressure_low; p.p_high = jp->pressure_high;
+        p.compression_rate = jp->compression_rate; p.length_tol = jp->length_tolerance;
+        p.decompress = jp->decompress_factor; p.max_compressions = jp->max_compression_steps;
+    }
+    for (auto &y : s->sys) {
+        y.phase = kSetup; y.rebuild = 1; y.done = 0;
+        y.prec = (p.switch_fmax > 0 && y.ncd >= 3) ? 0 : 1;
+        y.dt = p.dt0; y.alpha = p.alpha0; y.ngood = 0; y.nbad = 0; y.uphill = 0; y.stopped = 0;
+        y.converged = 0; y.iter = 0; y.fire_total = 0; y.pending = kActNone; y.minimizations = 0;
+        y.jam_stage = 0; y.jam_status = -1; y.jam_step = 0;
+        y.L_low = y.L_high = y.L_last = -1; y.L_saved = -1; y.scale = 1.0; y.rebuilds = 0;
+        y.ticket_a = y.ticket_b = 0;
+    }
+    CK(cudaMemcpyAsync(s->d_sys, s->sys.data(), sizeof(ESys) * s->S, cudaMemcpyHostToDevice, s->stream));
+    CK(cudaMemcpyAsync(&s->d->p, &p, sizeof(EParams), cudaMemcpyHostToDevice, s->stream));
+    TRY(put(s, &s->d->active, s->S));
+    TRY(put(s, &s->d->n_flagged, 0));
+    TRY(put(s, &s->d->overflow, 0));
+    TRY(put(s, &s->d->ticket, 0u));
+    // velocities start at zero (minimizeFire's setVelocitiesToZero)
+    CK(cudaMemsetAsync(s->h.vel, 0, 16 * (size_t)s->T, s->stream));
+    long long budget = jam ? (long long)4e9 : fp->max_steps * 2 + 16;
+    TRY(run(s, budget));
+    TRY(pull_sys(s));
+    return DPG_OK;
+}
+
+static void fill_results(ES *s, dpg_ensemble_result *r) {
+    if (!r) return;
+    for (int k = 0; k < s->S; k++) {
+        const ESys &y = s->sys[k];
+        dpg_ensemble_result &o = r[k];
+        o.avg_pe = y.pe / y.n;
+        o.max_force = std::sqrt(y.fmax2);
+        o.pressure = y.virial / (4.0 * y.L * y.L);
+        o.box_length = y.L;
+        o.contacts = y.contacts;
+        o.fire_steps = y.fire_total;
+        o.minimizations = y.minimizations;
+        o.rebuilds = y.rebuilds;
+        o.status = y.jam_status;
+        o.converged = y.converged;
+        o.packing_fraction = 0.0;  // filled by the caller, who knows the radii
+    }
+}
+
+extern "C" int dpg_ensemble_fire_minimize(dpg_ensemble s, const dpg_fire_params *p, dpg_ensemble_result *r) {
+    if (!s || !p) return set_err(DPG_ERR_ARG, "null argument");
+    if (p->max_steps <= 0) return set_err(DPG_ERR_ARG, "max_steps must be > 0");
+    TRY(start(s, p, 0, nullptr));
+    fill_results(s, r);
+    return DPG_OK;
+}
+
+extern "C" int dpg_ensemble_jam(dpg_ensemble s, const dpg_jam_params *p, dpg_ensemble_result *r) {
+    if (!s || !p) return set_err(DPG_ERR_ARG, "null argument");
+    TRY(start(s, &p->fire, 1, p));
+    fill_results(s, r);
+    return DPG_OK;
+}

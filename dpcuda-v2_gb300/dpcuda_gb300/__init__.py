@@ -16,3 +16,4 @@ from .lib import DpgError, load_library, library_path  # noqa: F401
 from .disk import (Disk, NVE, Fire, Adam, minimizeFire, minimizeAdam, jamPressure, jamPhi,  # noqa: F401
                    NEIGH_CELL, NEIGH_VERLET, NEIGH_ALL, FP64, MIXED)
 from .bumpy import RigidBumpy  # noqa: F401
+from .ensemble import Ensemble  # noqa: F401

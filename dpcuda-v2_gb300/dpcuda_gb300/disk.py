@@ -338,7 +338,7 @@ def jamPressure(particle: Disk, pressure_low, pressure_high, compression_rate=0.
     prm = JamParams(float(pressure_low), float(pressure_high), float(compression_rate),
                     float(length_tolerance), float(decompress_factor), int(max_compression_steps),
                     FireParams(float(fire[0]), float(fire[1]), float(fire[2]), float(fire[3]),
-                               int(fire[4]), 0.0),
+                               int(fire[4]), float(fire[5]) if len(fire) > 5 else 0.0),
                     NeighborConfig(int(m), *[float(v) for v in neighbors[1:]]))
     r = JamResult()
     check(particle.lib.dpg_jam_pressure(particle.h, C.byref(prm), C.byref(r)))

@@ -1,0 +1,89 @@
+"""Batched form: S independent disk systems advanced together (include/dpg.h,
+dpg_ensemble_*).  Each system keeps its own box, neighbour list, FIRE state and
+convergence flags; every kernel launch covers all systems and the whole run is
+one CUDA graph."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from .disk import _METHODS
+from .lib import (DP, EnsembleParams, EnsembleResult, FireParams, I64P, JamParams, NeighborConfig,
+                  check, load_library)
+
+FP64, MIXED = 0, 1
+
+
+class Ensemble:
+    def __init__(self, n_particles, boxes, cutoff, skin, e_c=1.0, n_c=2.0, precision=MIXED,
+                 switch_fmax=1e-7, stream=None):
+        self.lib = load_library()
+        self.n = np.ascontiguousarray(n_particles, dtype=np.int64)
+        self.boxes = np.ascontiguousarray(boxes, dtype=np.float64)
+        self.S = len(self.n)
+        prm = EnsembleParams(self.S, float(e_c), float(n_c), float(cutoff), float(skin),
+                             int(precision), 0, float(switch_fmax))
+        h = C.c_void_p()
+        check(self.lib.dpg_ensemble_create(C.byref(prm), self.n.ctypes.data_as(I64P),
+                                           self.boxes.ctypes.data_as(DP),
+                                           C.c_void_p(stream) if stream else None, C.byref(h)))
+        self.h = h
+        self.radii = None
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.dpg_ensemble_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def setState(self, x, y, radii, masses):
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (x, y, radii, masses)]
+        self.radii = arrs[2]
+        check(self.lib.dpg_ensemble_set_state(self.h, *[a.ctypes.data_as(DP) for a in arrs]))
+
+    def getState(self):
+        tot = int(self.n.sum())
+        out = {k: np.zeros(tot) for k in ("x", "y", "fx", "fy")}
+        check(self.lib.dpg_ensemble_get_state(self.h, *[out[k].ctypes.data_as(DP) for k in
+                                                         ("x", "y", "fx", "fy")]))
+        return out
+
+    def _results(self, res):
+        out = []
+        starts = np.concatenate([[0], np.cumsum(self.n)])
+        for k in range(self.S):
+            r = res[k]
+            area = float(np.sum(self.radii[starts[k]:starts[k + 1]] ** 2)) * np.pi
+            out.append(dict(avg_pe=r.avg_pe, max_force=r.max_force, pressure=r.pressure,
+                            box_length=r.box_length, contacts=r.contacts,
+                            packing_fraction=area / r.box_length ** 2, fire_steps=r.fire_steps,
+                            minimizations=r.minimizations, rebuilds=r.rebuilds, status=r.status,
+                            converged=r.converged))
+        return out
+
+    def minimizeFire(self, alpha_init=0.1, dt=1e-2, avg_pe_target=1e-16, avg_pe_diff_target=1e-16,
+                     num_steps=100000, fmax_target=0.0):
+        prm = FireParams(float(alpha_init), float(dt), float(avg_pe_target),
+                         float(avg_pe_diff_target), int(num_steps), float(fmax_target))
+        res = (EnsembleResult * self.S)()
+        check(self.lib.dpg_ensemble_fire_minimize(self.h, C.byref(prm), res))
+        return self._results(res)
+
+    def jam(self, pressure_low, pressure_high, compression_rate=0.99, length_tolerance=1e-10,
+            decompress_factor=1.01, max_compression_steps=1000,
+            fire=(0.1, 1e-2, 1e-16, 1e-16, 100000, 0.0)):
+        prm = JamParams(float(pressure_low), float(pressure_high), float(compression_rate),
+                        float(length_tolerance), float(decompress_factor),
+                        int(max_compression_steps),
+                        FireParams(float(fire[0]), float(fire[1]), float(fire[2]), float(fire[3]),
+                                   int(fire[4]), float(fire[5])),
+                        NeighborConfig(0, 1.5, 0.2, 8.0, 0.5))
+        res = (EnsembleResult * self.S)()
+        check(self.lib.dpg_ensemble_jam(self.h, C.byref(prm), res))
+        return self._results(res)

@@ -76,6 +76,17 @@ class JamPhiParams(C.Structure):
                 ("max_compression_steps", I64)]
 
 
+class EnsembleParams(C.Structure):
+    _fields_ = [("n_systems", I64), ("e_c", D), ("n_c", D), ("cutoff", D), ("skin", D),
+                ("precision", I32), ("reserved", I32), ("switch_fmax", D)]
+
+
+class EnsembleResult(C.Structure):
+    _fields_ = [("avg_pe", D), ("max_force", D), ("pressure", D), ("packing_fraction", D),
+                ("box_length", D), ("contacts", D), ("fire_steps", I64), ("minimizations", I64),
+                ("rebuilds", I64), ("status", I32), ("converged", I32)]
+
+
 # name -> argtypes (all return int status unless listed in _RESTYPES)
 SIGNATURES = {
     "dpg_create": [C.POINTER(Params), VP, C.POINTER(VP)],
@@ -124,6 +135,12 @@ SIGNATURES = {
     "dpg_save_state": [VP],
     "dpg_restore_state": [VP],
     "dpg_profile_loop": [VP, I32, I32, D, DP, I64P],
+    "dpg_ensemble_create": [C.POINTER(EnsembleParams), I64P, DP, VP, C.POINTER(VP)],
+    "dpg_ensemble_destroy": [VP],
+    "dpg_ensemble_set_state": [VP, DP, DP, DP, DP],
+    "dpg_ensemble_get_state": [VP, DP, DP, DP, DP],
+    "dpg_ensemble_fire_minimize": [VP, C.POINTER(FireParams), C.POINTER(EnsembleResult)],
+    "dpg_ensemble_jam": [VP, C.POINTER(JamParams), C.POINTER(EnsembleResult)],
     "dpg_bumpy_create": [C.POINTER(BumpyParams), VP, C.POINTER(VP)],
     "dpg_bumpy_destroy": [VP],
     "dpg_bumpy_set_bodies": [VP, DP, DP, DP, DP, DP, DP, DP, I32P],

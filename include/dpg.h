@@ -337,6 +337,50 @@ int dpg_bumpy_fire_minimize(dpg_bumpy_handle h, const dpg_fire_params *p, double
 /* scalePositionsFull (rigid_bumpy.cu:1044-1048) with the box: Particle::scaleBox */
 int dpg_bumpy_scale_box(dpg_bumpy_handle h, double factor);
 
+/* ======================================================================
+ *  Ensembles: the batched form.  Many independent disk systems of uneven
+ *  size (each with its own box, neighbour list, FIRE dt/alpha/counters and
+ *  convergence state) advanced together: every kernel launch covers all
+ *  systems, finished systems are masked out, and the whole loop is one CUDA
+ *  graph.  No reference counterpart as an API: the reference runs one system
+ *  per process (its state lives in __constant__ symbols); an ensemble runs
+ *  the same per-system algorithms (minimizeFire, the pressure-band jamming of
+ *  scripts/runArthurJamWithFire.cpp) for S systems at once.
+ * ====================================================================== */
+typedef struct dpg_ensemble_system *dpg_ensemble;
+
+typedef struct {
+    int64_t n_systems;
+    double e_c, n_c;
+    double cutoff;      /* neighbour cutoff (absolute, e.g. d_max + skin) */
+    double skin;        /* lists rebuilt when a particle moved more than skin / 2 */
+    int precision;      /* DPG_FP64, or DPG_MIXED (FP32 pair forces, then FP64 refinement) */
+    int reserved;
+    double switch_fmax; /* DPG_MIXED: FP32 pair forces until max|F| <= switch_fmax */
+} dpg_ensemble_params;
+
+typedef struct {
+    double avg_pe, max_force, pressure, packing_fraction, box_length, contacts;
+    int64_t fire_steps;     /* force passes over the whole run */
+    int64_t minimizations;
+    int64_t rebuilds;
+    int status;             /* jamming: 0 final state, 1 length tolerance, 2 out of steps */
+    int converged;
+} dpg_ensemble_result;
+
+/* n_particles[s], box[s] (square boxes) */
+int dpg_ensemble_create(const dpg_ensemble_params *p, const int64_t *n_particles, const double *box,
+                        void *cuda_stream, dpg_ensemble *out);
+int dpg_ensemble_destroy(dpg_ensemble e);
+/* host arrays, system after system (sum of n_particles entries each) */
+int dpg_ensemble_set_state(dpg_ensemble e, const double *x, const double *y, const double *radii,
+                           const double *masses);
+int dpg_ensemble_get_state(dpg_ensemble e, double *x, double *y, double *fx, double *fy);
+/* minimizeFire on every system (p->fmax_target > 0 adds the max|F_i| stop) */
+int dpg_ensemble_fire_minimize(dpg_ensemble e, const dpg_fire_params *p, dpg_ensemble_result *per_system);
+/* pressure-band jamming of every system (the dpg_jam_pressure control flow) */
+int dpg_ensemble_jam(dpg_ensemble e, const dpg_jam_params *p, dpg_ensemble_result *per_system);
+
 /* ---- measurement ------------------------------------------------------ */
 /* Runs `iters` iterations of a device loop (kind 0 = FIRE from the current
  * state, as dpg_fire_minimize's body; kind 1 = NVE with step dt) as plain
