@@ -1,21 +1,28 @@
 """Benchmark: FIRE minimisations of bidisperse disks, N = 16384, phi = 0.86, run
-to max|F_i| <= 1e-13 (the 16384-disk FIRE workload), plus the per-kernel
-roofline and the CPU baseline.
+to max|F_i| <= 1e-13 (the 16384-disk FIRE workload): the mixed-precision
+batched form against the plain FP64 drop-in, plus the per-kernel roofline and
+the CPU baseline.
 
-A step is one complete FIRE minimisation of one seeded random packing (cell
+A solve is one complete FIRE minimisation of one seeded random packing (cell
 list + neighbour list build, initial forces, then FIRE until max|F_i| <= 1e-13).
-Every step uses a different seed; all arms use the same seeds.
+A step is one call of the batched form on 8 such systems (8 distinct seeds,
+FP32 pair forces with FP64 accumulation, each system switching to the FP64
+pair arithmetic below max|F| = 1e-7 for the final refinement).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 --impl ours (default): the GB300 library through its C ABI.  `value` = solves/s
-with the initial packings resident in HBM; `e2e` = the same through host
-buffers (positions/radii/masses in, positions/PE out).  L2 (126 MB) is flushed
-between timed steps (a 512 MiB write) since one 16384-disk system fits in L2.
+of the batched mixed form with the initial packings resident in HBM; `e2e` =
+the same through host buffers (positions/radii/masses in, positions/forces
+out).  The plain FP64 path (one system per call, bit-identical to the
+reference arithmetic) is timed on the same starts and reported in
+extra.plain_fp64.  L2 (126 MB) is flushed between timed solves (a 512 MiB
+write).
 --impl reference: the CPU restatement of the reference algorithm (the oracle,
-oracle/dpg_oracle.c, OpenMP over all host cores) running full minimisations
-of the same seeds.  Under torchrun (N > 1) each rank solves its own seeds
-(independent replicas, weak scaling); only rank 0 runs the reference arm.
+oracle/dpg_oracle.c, FP64, OpenMP over all host cores) running full
+minimisations of the same seeds, one per step.  Under torchrun (N > 1) each
+rank solves its own seeds (independent replicas, weak scaling); only rank 0
+runs the reference arm.
 """
 from __future__ import annotations
 
@@ -43,6 +50,28 @@ CUT_MULT = 1.7 / 1.4        # r_c = d_max + skin 0.3
 MAX_STEPS = 1_000_000
 FIRE_ALPHA0, FIRE_DT0 = 0.1, 1e-2
 L2_FLUSH_BYTES = 512 << 20
+BATCH = 8                   # systems per step of the batched form
+CUTOFF, SKIN = 1.7, 0.3     # neighbour cutoff d_max + skin, and the skin
+SWITCH_FMAX = 1e-6          # mixed systems switch to FP64 pair forces below this max|F|
+PLAIN_SOLVES = 2            # timed solves of the plain FP64 path (after one untimed)
+PROFILE_ITERS = 300
+
+
+def step_seeds(rank, k):
+    """Seeds of the BATCH systems of step k on this rank (every start distinct)."""
+    return [100000 * rank + BATCH * k + b + 1 for b in range(BATCH)]
+
+
+def reduce_max(x: float, device=None) -> float:
+    """Max of x over the ranks of the default process group (x itself when
+    not distributed): the job's time is its slowest rank's."""
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
 
 
 def workload_config():
@@ -52,12 +81,14 @@ def workload_config():
             "fire": {"alpha0": FIRE_ALPHA0, "dt0": FIRE_DT0, "dt_max": 10 * FIRE_DT0,
                      "f_inc": 1.1, "f_dec": 0.5, "f_alpha": 0.99, "n_min": 5},
             "neighbors": {"method": "cell", "cutoff": 1.7, "skin": 0.3, "particles_per_cell": 8},
-            "precision": "fp64", "l2": "flushed between steps (512 MiB write)",
-            "seeds": "1000*rank + step + 1"}
+            "form": f"mixed precision (FP32 pairs, FP64 accumulation, FP64 pair refinement "
+                    f"below max|F| = {SWITCH_FMAX:g}), {BATCH} systems per step",
+            "l2": "flushed between steps (512 MiB write)",
+            "seeds": f"step k on rank r: 100000*r + {BATCH}*k + 1 .. + {BATCH}"}
 
 
 def packing(seed):
-    from oracle.oracle import disk_packing  # input generator = the reference's RandomUniform
+    from dpcuda_gb300.init import disk_packing  # the reference's RandomUniform stream
     return disk_packing(N_PART, PHI, seed)
 
 
@@ -171,7 +202,7 @@ def run_reference(args):
         o.minimize_fire(FIRE_ALPHA0, FIRE_DT0, 0.0, 0.0, 200, FMAX)
     times, iters = [], []
     for k in range(args.steps):
-        dt, steps, fmax = cpu_solve(k + 1, threads)
+        dt, steps, fmax = cpu_solve(step_seeds(0, args.warmup + k)[0], threads)
         times.append(dt)
         iters.append(steps)
     total = sum(times)
@@ -183,8 +214,9 @@ def run_reference(args):
             "config": workload_config(),
             "cpu_baseline": {"value": value, "unit": "FIRE solves/s", "cores": threads,
                              "kind": "port",
-                             "sample": f"{args.steps} full minimisations (seeds 1..{args.steps}) of "
-                                       f"the oracle restatement, OpenMP {threads} threads"},
+                             "sample": f"{args.steps} full minimisations (the first start of each "
+                                       f"timed step) of the oracle restatement (FP64), OpenMP "
+                                       f"{threads} threads"},
             "e2e": {"value": value, "unit": "FIRE solves/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
             "extra": {"fire_iterations_per_solve": float(np.mean(iters)),
@@ -215,130 +247,182 @@ def run_ours(args):
             import torch.distributed as dist
             dist.barrier()
 
+    def max_over_ranks(x):
+        return reduce_max(x, dev)
+
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
 
     def l2_flush():
         with torch.cuda.stream(stream):
             flush.fill_(1.0)
 
-    # inputs for every step, resident in HBM before the timed region
-    n_sys = args.warmup + args.steps
-    seeds = [1000 * rank + k + 1 for k in range(n_sys)]
-    systems = []
-    for sd in seeds:
-        st = packing(sd)
-        s = dpg.Disk(N_PART, st["box"], stream=sptr)
-        dev_arrays = {k: torch.from_numpy(st[k]).to(dev) for k in ("x", "y", "r", "m")}
-        systems.append((s, st, dev_arrays))
+    def timed(fn):
+        l2_flush()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        out = fn()
+        e1.record(stream)
+        e1.synchronize()
+        return out, e0.elapsed_time(e1)
+
+    # ---- inputs of every step, resident in HBM before the timed region -------
+    n_step = args.warmup + args.steps
+    batches = []
+    for k in range(n_step):
+        sts = [packing(sd) for sd in step_seeds(rank, k)]
+        e = dpg.Ensemble([N_PART] * BATCH, [st["box"] for st in sts], CUTOFF, SKIN,
+                         precision=dpg.MIXED, switch_fmax=SWITCH_FMAX, stream=sptr)
+        e.setState(*[np.concatenate([st[c] for st in sts]) for c in ("x", "y", "r", "m")])
+        batches.append((e, sts))
     torch.cuda.synchronize()
 
-    def solve(s, st, arr):
-        s.setState(arr["x"], arr["y"], None, None, arr["r"], arr["m"])
-        s.setupNeighbors("cell", CUT_MULT, 0.2, 8.0, 0.5)
-        return dpg.minimizeFire(s, FIRE_ALPHA0, FIRE_DT0, 0.0, 0.0, MAX_STEPS, fmax_target=FMAX)
+    def solve_batch(e):
+        return e.minimizeFire(FIRE_ALPHA0, FIRE_DT0, 0.0, 0.0, MAX_STEPS, fmax_target=FMAX)
 
     for k in range(args.warmup):
-        solve(*systems[k])
+        solve_batch(batches[k][0])
+        batches[k][0].setState(*[np.concatenate([st[c] for st in batches[k][1]])
+                                 for c in ("x", "y", "r", "m")])
     torch.cuda.synchronize()
 
+    # ---- headline: mixed precision, BATCH systems per step --------------------
     sampler = ClockSampler(dev.index or 0)
     results, ev_ms, launches = [], [], 0
     barrier()
     torch.cuda.synchronize()
     sampler.start()
     t_wall0 = time.perf_counter()
-    for k in range(args.warmup, n_sys):
-        l2_flush()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        s, st, arr = systems[k]
-        r = solve(s, st, arr)
-        e1.record(stream)
-        e1.synchronize()
-        ev_ms.append(e0.elapsed_time(e1))
-        info = s.neighborInfo()
-        # kernels per solve: setup (cell build 6 + nlist + force) + per iteration
-        # move/force/guard, plus 5 cell kernels per cell rebuild and 1 per list rebuild
-        launches += 10 + 3 * (r["steps"] + 1) + 5 * info["n_cell_rebuilds"] + info["n_rebuilds"]
-        results.append(r)
+    for k in range(args.warmup, n_step):
+        e, _ = batches[k]
+        res, ms = timed(lambda: solve_batch(e))
+        ev_ms.append(ms)
+        results.append(res)
+        # kernels per iteration of the graph loop: move, force, transition,
+        # guard; 5 rebuild kernels on iterations where any system rebuilt
+        iters = max(r["fire_steps"] for r in res)
+        launches += 4 * (iters + 1) + 5 * max(r["rebuilds"] for r in res)
     torch.cuda.synchronize()
     t_wall = time.perf_counter() - t_wall0
     barrier()
     clocks = sampler.stop()
-    total_ms = float(np.sum(ev_ms))
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * args.steps / (total_ms / 1e3)
-    iters = [r["steps"] for r in results]
-    ok = all(r["converged"] and r["max_force"] <= FMAX for r in results)
+    total_ms = max_over_ranks(float(np.sum(ev_ms)))
+    value = world * args.steps * BATCH / (total_ms / 1e3)
+    flat = [r for res in results for r in res]
+    ok = all(r["converged"] and r["max_force"] <= FMAX for r in flat)
 
-    # ---- e2e: host buffers in, host results out, through the C ABI -----------------
+    # ---- e2e: host arrays in, host positions/forces out, through the C ABI ---
     e2e_ms = []
-    h2d = N_PART * 8 * 4   # x, y, radii, masses
-    d2h = N_PART * 8 * 3   # x, y, pe
-    for k in range(args.warmup, n_sys):
-        s, st, _ = systems[k]
+    h2d = BATCH * N_PART * 8 * 4   # x, y, radii, masses
+    d2h = BATCH * N_PART * 8 * 4   # x, y, fx, fy
+    for k in range(args.warmup, n_step):
+        e, sts = batches[k]
+        host = [np.concatenate([st[c] for st in sts]) for c in ("x", "y", "r", "m")]
         l2_flush()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        s.setState(st["x"], st["y"], np.zeros(N_PART), np.zeros(N_PART), st["r"], st["m"])
-        s.setupNeighbors("cell", CUT_MULT, 0.2, 8.0, 0.5)
-        dpg.minimizeFire(s, FIRE_ALPHA0, FIRE_DT0, 0.0, 0.0, MAX_STEPS, fmax_target=FMAX)
-        out = s.getState()
-        _ = float(out["pe"].sum())
+        e.setState(*host)
+        solve_batch(e)
+        out = e.getState()
+        _ = float(np.abs(out["fx"]).max())
         e2e_ms.append(1e3 * (time.perf_counter() - t0))
-    e2e_value = world * args.steps / (float(np.sum(e2e_ms)) / 1e3)
+    e2e_value = world * args.steps * BATCH / (max_over_ranks(float(np.sum(e2e_ms))) / 1e3)
 
-    # ---- roofline of the dominant kernel (forces + kick + reductions) --------
+    # ---- the plain FP64 drop-in on the same systems (one per call) -----------
+    plain = plain_fp64_leg(dpg, sptr, batches[args.warmup][1][:PLAIN_SOLVES + 1], timed)
+    # error of the mixed form against the FP64 path on the same starts
+    pe_mixed = [r["avg_pe"] for r in results[0][1:PLAIN_SOLVES + 1]]
+    plain["mixed_vs_fp64_avg_pe_rel"] = [abs(a - b) / abs(b) for a, b in
+                                         zip(pe_mixed, plain["avg_pe"])]
+
+    # ---- roofline of the dominant kernel of the headline form ----------------
     peak, peak_src = measured_peak_hbm()
-    s, st, arr = systems[-1]
-    s.setState(arr["x"], arr["y"], None, None, arr["r"], arr["m"])
-    s.setupNeighbors("cell", CUT_MULT, 0.2, 8.0, 0.5)
-    prof = profile(dpg, s, kind=0, iters=400)
-    k_mean = float(np.mean(s.getNeighbors()[1]))
-    # algorithmic bytes per particle of k_fire_force: read pos 16, rad 8, count 4,
-    # indices 4k, vel 16, mass 8; write frc 16, pe 8, vel 16 (neighbour data reused from cache)
-    bytes_force = N_PART * (92 + 4 * k_mean)
+    e, sts = batches[-1]
+    e.setState(*[np.concatenate([st[c] for st in sts]) for c in ("x", "y", "r", "m")])
+    prof = e.profileLoop(PROFILE_ITERS, FIRE_ALPHA0, FIRE_DT0, FMAX)
+    k_mean = plain["mean_neighbors"]
+    # e_force (mixed phase) per particle: read pk[i] 16, count 4, neighbour
+    # indices 4k, vel 16, mass 8; write frc 16, pe 8, vel 16 (neighbours' pk
+    # gathered from cache) -> 84 + 4k
+    bytes_force = BATCH * N_PART * (84 + 4 * k_mean)
     achieved = bytes_force / (prof["force_us"] * 1e-6) / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": None, "kernel": "k_fire_force",
+                "frac": achieved / peak, "traffic": None, "kernel": "e_force",
                 "peak_source": peak_src, "bytes_per_launch": bytes_force,
-                "launch_us": prof["force_us"],
-                "note": "16384-disk working set (3 MB) is L2-resident; see roofline_large"}
+                "launch_us": prof["force_us"], "profile_us_per_iter": prof,
+                "note": "8 x 16384 disks, FP32 pair phase; working set (25 MB) is L2-resident, "
+                        "so the kernel is latency/L2-bound, not HBM-bound"}
 
-    # ---- large-N force kernel (N = 2^20 NVE), where HBM bounds the kernel ----
+    # ---- large-N force kernel (N = 2^20 NVE, plain FP64) -----------------------
     large = large_n_roofline(dpg, dev, sptr, peak)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        dt, steps, fmax = cpu_solve(seeds[args.warmup], threads)
+        sd = step_seeds(rank, args.warmup)[0]
+        dt, steps, fmax = cpu_solve(sd, threads)
         cpu = {"value": 1.0 / dt, "unit": "FIRE solves/s", "cores": threads, "kind": "port",
-               "sample": f"1 full minimisation (seed {seeds[args.warmup]}, {steps} FIRE iterations) "
-                         f"of the oracle restatement, OpenMP {threads} threads"}
+               "sample": f"1 full minimisation (seed {sd}, {steps} FIRE iterations) of the "
+                         f"oracle restatement (FP64), OpenMP {threads} threads"}
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "FIRE solves/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-                "dtype": "f64", "data": "synthetic", "config": workload_config(),
+                "dtype": "f32+f64", "data": "synthetic", "config": workload_config(),
                 "roofline": roofline, "cpu_baseline": cpu,
                 "e2e": {"value": e2e_value, "unit": "FIRE solves/s", "h2d_bytes_per_step": h2d,
                         "d2h_bytes_per_step": d2h},
                 "gpu_launches": launches, "clocks": clocks,
-                "extra": {"fire_iterations_per_solve": float(np.mean(iters)),
-                          "particle_steps_per_s": N_PART * float(np.sum(iters)) / (total_ms / 1e3),
+                "extra": {"form": "mixed+batched", "systems_per_step": BATCH,
+                          "fire_iterations_per_solve": float(np.mean([r["fire_steps"] for r in flat])),
+                          "particle_steps_per_s": N_PART * float(sum(r["fire_steps"] for r in flat))
+                          / (total_ms / 1e3),
                           "all_converged_to_fmax": ok,
-                          "max_force": float(max(r["max_force"] for r in results)),
-                          "wall_s_timed": t_wall, "profile_us_per_iter": prof,
+                          "max_force": float(max(r["max_force"] for r in flat)),
+                          "wall_s_timed": t_wall,
+                          "plain_fp64": plain,
+                          "mixed_batched_over_plain_fp64": value / plain["value"],
                           "roofline_large": large}}
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def plain_fp64_leg(dpg, sptr, sts, timed):
+    """The drop-in FP64 path (bit-identical to the reference arithmetic): one
+    system per call, first start untimed (warm-up), the rest timed."""
+    import torch
+    dev = torch.device("cuda", torch.cuda.current_device())
+    out = {"solves": 0, "ms": [], "fire_iterations": [], "avg_pe": [], "max_force": []}
+    for k, st in enumerate(sts):
+        s = dpg.Disk(N_PART, st["box"], stream=sptr)
+        arr = {c: torch.from_numpy(st[c]).to(dev) for c in ("x", "y", "r", "m")}
+        torch.cuda.synchronize()
+
+        def solve():
+            s.setState(arr["x"], arr["y"], None, None, arr["r"], arr["m"])
+            s.setupNeighbors("cell", CUT_MULT, 0.2, 8.0, 0.5)
+            return dpg.minimizeFire(s, FIRE_ALPHA0, FIRE_DT0, 0.0, 0.0, MAX_STEPS, fmax_target=FMAX)
+
+        r, ms = timed(solve)
+        if k == 0:
+            s.setState(arr["x"], arr["y"], None, None, arr["r"], arr["m"])
+            s.setupNeighbors("cell", CUT_MULT, 0.2, 8.0, 0.5)
+            out["mean_neighbors"] = float(np.mean(s.getNeighbors()[1]))
+            s.close()
+            continue
+        out["solves"] += 1
+        out["ms"].append(ms)
+        out["fire_iterations"].append(r["steps"])
+        out["avg_pe"].append(s.totalPotentialEnergy() / N_PART)
+        out["max_force"].append(r["max_force"])
+        s.close()
+    out["value"] = out["solves"] / (float(np.sum(out["ms"])) / 1e3)
+    out["unit"] = "FIRE solves/s"
+    out["dtype"] = "f64"
+    out["force_group"] = "threads per particle chosen by the library (8 at N=16384)"
+    return out
 
 
 def profile(dpg, s, kind, iters, dt=1e-2):
@@ -353,43 +437,105 @@ def profile(dpg, s, kind, iters, dt=1e-2):
 def large_n_roofline(dpg, dev, sptr, peak):
     """N = 2^20 polydisperse disks r ~ U[0.4, 0.6], phi = 0.84, NVE dt = 1e-2:
     per-kernel device time of the fused force + kick kernel (k_nve_second)."""
-    from oracle.oracle import fill_normal, fill_uniform
+    from dpcuda_gb300.init import random_uniform
     n = 1 << 20
-    r = fill_uniform(n, 0.4, 0.6, 7 * n, 5)
+    r = random_uniform(n, 0.4, 0.6, 7 * n, 5)
     area = float(np.sum(r * r)) * np.pi
     L = (area / 0.84) ** 0.5
-    x = fill_uniform(n, 0.0, L, 0, 5)
-    y = fill_uniform(n, 0.0, L, n, 5)
+    x = random_uniform(n, 0.0, L, 0, 5)
+    y = random_uniform(n, 0.0, L, n, 5)
     T = 1e-3
-    vx = fill_normal(n, 0.0, np.sqrt(T), 2 * n, 5)
-    vy = fill_normal(n, 0.0, np.sqrt(T), 3 * n, 5)
+    rng = np.random.default_rng(5)
+    vx = rng.normal(0.0, np.sqrt(T), n)
+    vy = rng.normal(0.0, np.sqrt(T), n)
     vx -= vx.mean()
     vy -= vy.mean()
-    s = dpg.Disk(n, L, stream=sptr)
-    s.setState(x, y, vx, vy, r, np.ones(n))
-    # rebuild at half-skin: sqrt(3) |dr| > disp_mult * r_c with |dr| = 0.15, r_c = 1.5
-    info = s.setupNeighbors("cell", 1.5 / 1.2, 0.1732, 8.0, 0.5)
-    prof = profile(dpg, s, kind=1, iters=200)
-    k_mean = float(np.mean(s.getNeighbors()[1]))
-    # k_nve_second per particle: read pos 16, rad 8, count 4, indices 4k, vel 16,
-    # mass 8; write frc 16, pe 8, vel 16
-    b = n * (92 + 4 * k_mean)
-    ach = b / (prof["force_us"] * 1e-6) / 1e9
-    step_us = prof["move_us"] + prof["rebuild_us"] + prof["force_us"]
-    return {"workload": "NVE, N=2^20 polydisperse disks U[0.4,0.6], phi=0.84, dt=1e-2, T=1e-3",
-            "kernel": "k_nve_second", "achieved": ach, "peak": peak, "unit": "GB/s",
-            "frac": ach / peak, "bytes_per_launch": b, "launch_us": prof["force_us"],
-            "mean_neighbors": k_mean, "profile_us_per_step": prof,
-            "particle_steps_per_s_stream_launch": n / (step_us * 1e-6),
-            "cutoff": info["cutoff"]}
+    out = {"workload": "NVE, N=2^20 polydisperse disks U[0.4,0.6], phi=0.84, dt=1e-2, T=1e-3",
+           "kernel": "k_nve_second", "peak": peak, "unit": "GB/s"}
+    for form, prec in (("fp64", dpg.FP64), ("mixed", dpg.MIXED)):
+        s = dpg.Disk(n, L, stream=sptr, precision=prec)
+        s.setState(x, y, vx, vy, r, np.ones(n))
+        # rebuild at half-skin: sqrt(3) |dr| > disp_mult * r_c with |dr| = 0.15, r_c = 1.5
+        info = s.setupNeighbors("cell", 1.5 / 1.2, 0.1732, 8.0, 0.5)
+        prof = profile(dpg, s, kind=1, iters=200)
+        k_mean = float(np.mean(s.getNeighbors()[1]))
+        # k_nve_second per particle: read count 4, indices 4k, vel 16, mass 8;
+        # write frc 16, pe 8, vel 16; plus pos 16 + rad 8 (FP64) or the packed
+        # offsets 16 (mixed)
+        b = n * ((92 if form == "fp64" else 84) + 4 * k_mean)
+        ach = b / (prof["force_us"] * 1e-6) / 1e9
+        step_us = prof["move_us"] + prof["rebuild_us"] + prof["force_us"]
+        out[form] = {"achieved": ach, "frac": ach / peak, "bytes_per_launch": b,
+                     "launch_us": prof["force_us"], "mean_neighbors": k_mean,
+                     "profile_us_per_step": prof,
+                     "particle_steps_per_s_stream_launch": n / (step_us * 1e-6),
+                     "cutoff": info["cutoff"]}
+        s.close()
+    return out
+
+
+def jam_ensemble(args):
+    """The batched jamming workload (not the default line): S bidisperse
+    systems with N drawn log-uniformly in [64, 4096] from a seed, each
+    starting at phi = 0.80, compressed by box scaling with a FIRE
+    minimisation (the reference's minimizeFire defaults: PE targets 1e-16,
+    at most 1e5 steps) after each step and bisected on the box length until
+    the pressure is 1e-7 +- 1e-9 (scripts/runArthurJamWithFire.cpp flow).
+    Prints one JSON line: systems jammed per second for the mixed and FP64
+    ensembles and |phi_J(mixed) - phi_J(FP64)| over the systems."""
+    import dpcuda_gb300 as dpg
+    from dpcuda_gb300.init import disk_packing
+    S = args.jam_systems
+    rng = np.random.default_rng(2024)
+    sizes = np.floor(np.exp(rng.uniform(np.log(64), np.log(4096), S))).astype(int)
+    sts = [disk_packing(int(n), 0.80, 7000 + k) for k, n in enumerate(sizes)]
+    cat = [np.concatenate([st[c] for st in sts]) for c in ("x", "y", "r", "m")]
+    band = (1e-7 - 1e-9, 1e-7 + 1e-9)
+    fire = (0.1, 1e-2, 1e-16, 1e-16, 100000, 0.0)
+    out = {}
+    for form, prec in (("mixed", dpg.MIXED), ("fp64", dpg.FP64)):
+        e = dpg.Ensemble(sizes, [st["box"] for st in sts], CUTOFF, SKIN, precision=prec,
+                         switch_fmax=SWITCH_FMAX)
+        e.setState(*cat)
+        t0 = time.perf_counter()
+        res = e.jam(*band, compression_rate=0.99, length_tolerance=1e-10, decompress_factor=1.01,
+                    max_compression_steps=args.jam_max_compressions, fire=fire)
+        dt = time.perf_counter() - t0
+        out[form] = {"s": dt, "systems_per_s": S / dt,
+                     "phi": [r["packing_fraction"] for r in res],
+                     "in_band": int(sum(band[0] <= r["pressure"] <= band[1] for r in res)),
+                     "status": [r["status"] for r in res],
+                     "fire_steps_max": int(max(r["fire_steps"] for r in res)),
+                     "minimizations_max": int(max(r["minimizations"] for r in res))}
+        e.close()
+    d = np.abs(np.array(out["mixed"]["phi"]) - np.array(out["fp64"]["phi"]))
+    line = {"metric": "batched jamming: systems jammed/s, mixed vs FP64", "unit": "systems/s",
+            "value": out["mixed"]["systems_per_s"], "n_gpus": 1, "higher_is_better": True,
+            "config": {"workload": f"{S} systems, N log-uniform [64, 4096], phi0 0.80, "
+                                   "P = 1e-7 +- 1e-9, FIRE 1e-16/1e-16/1e5",
+                       "sizes_sum": int(sizes.sum())},
+            "fp64_systems_per_s": out["fp64"]["systems_per_s"],
+            "dphi_J": {"median": float(np.median(d)), "max": float(d.max()),
+                       "frac_below_1e-6": float(np.mean(d <= 1e-6))},
+            "detail": out}
+    print(json.dumps(line), flush=True)
 
 
 def ncu_case(which):
     """Small fixed workloads for ncu captures (plain stream launches, a few
     hundred kernels): 'fire' = 64 FIRE iterations of the 16384-disk system,
-    'nve_large' = 8 NVE steps of the 2^20-disk system."""
+    'nve_large' = 8 NVE steps of the 2^20-disk system, 'ensemble' = 64 FIRE
+    iterations of the batched mixed form on 8 x 16384 disks."""
     os.environ["DPG_LOOP_MODE"] = "stream"
     import dpcuda_gb300 as dpg
+    if which == "ensemble":
+        sts = [packing(sd) for sd in step_seeds(0, 0)]
+        e = dpg.Ensemble([N_PART] * BATCH, [st["box"] for st in sts], CUTOFF, SKIN,
+                         precision=dpg.MIXED, switch_fmax=SWITCH_FMAX)
+        e.setState(*[np.concatenate([st[c] for st in sts]) for c in ("x", "y", "r", "m")])
+        r = e.minimizeFire(FIRE_ALPHA0, FIRE_DT0, 0.0, 0.0, 64, fmax_target=FMAX)
+        print(json.dumps({"ncu_case": which, "steps": max(x["fire_steps"] for x in r)}))
+        return
     if which == "fire":
         st = packing(1)
         s = dpg.Disk(N_PART, st["box"])
@@ -398,12 +544,12 @@ def ncu_case(which):
         r = dpg.minimizeFire(s, FIRE_ALPHA0, FIRE_DT0, 0.0, 0.0, 64, fmax_target=FMAX)
         print(json.dumps({"ncu_case": which, "steps": r["steps"]}))
     else:
-        from oracle.oracle import fill_uniform
+        from dpcuda_gb300.init import random_uniform
         n = 1 << 20
-        r = fill_uniform(n, 0.4, 0.6, 7 * n, 5)
+        r = random_uniform(n, 0.4, 0.6, 7 * n, 5)
         L = (float(np.sum(r * r)) * np.pi / 0.84) ** 0.5
         s = dpg.Disk(n, L)
-        s.setState(fill_uniform(n, 0.0, L, 0, 5), fill_uniform(n, 0.0, L, n, 5), None, None, r,
+        s.setState(random_uniform(n, 0.0, L, 0, 5), random_uniform(n, 0.0, L, n, 5), None, None, r,
                    np.ones(n))
         s.setupNeighbors("cell", 1.5 / 1.2, 0.1732, 8.0, 0.5)
         s.nveSteps(1e-2, 8)
@@ -417,9 +563,16 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--ncu-case", choices=["fire", "nve_large"], default=None,
+    ap.add_argument("--ncu-case", choices=["fire", "nve_large", "ensemble"], default=None,
                     help="run a small fixed workload for ncu captures and exit")
+    ap.add_argument("--jam-ensemble", action="store_true",
+                    help="run the batched jamming workload instead of the default line")
+    ap.add_argument("--jam-systems", type=int, default=256)
+    ap.add_argument("--jam-max-compressions", type=int, default=2000)
     args = ap.parse_args()
+    if args.jam_ensemble:
+        jam_ensemble(args)
+        return
     if args.ncu_case:
         ncu_case(args.ncu_case)
         return

@@ -32,6 +32,7 @@ struct BumpyExt {
     int *vbody, *vbody_t, *svidx, *svidx_t;
     int *o2n;                // old -> new body slot during a re-sort
     int *vnbr, *vcount;      // vertex neighbour list, column-major [capv][nv]
+    float4 *vpk;             // mixed form: packed FP32 vertex offsets (see mixed_pack)
     long long vlist_built;   // n_rebuilds value at the last vertex-list build
     double tmax2, power_rot;
     // snapshot of the rotational state (setLastState)
@@ -100,7 +101,9 @@ __device__ __forceinline__ void body_move(BumpySys *bs, int b, int lane, double 
         double2 q = x.vpos[f + k];
         double rx = q.x - p.x, ry = q.y - p.y;
         double rxr = rx * ca - ry * sa, ryr = rx * sa + ry * ca;
-        x.vpos[f + k] = make_double2(nx + rxr, ny + ryr);
+        double2 nq = make_double2(nx + rxr, ny + ryr);
+        x.vpos[f + k] = nq;
+        if (d.p.precision == kMixed) x.vpk[f + k] = mixed_pack(d.p, nq, x.rv);
     }
 }
 
@@ -124,6 +127,7 @@ __device__ __forceinline__ void body_forces(const BumpySys *__restrict__ bs, int
     const double bx = d.p.box[0], by = d.p.box[1], e_c = d.p.e_c, n_c = d.p.n_c, rv = x.rv;
     const double2 c = d.v.pos[b];
     const int f = x.start[b], nvb = x.nvb[b];
+    const bool mixed = d.p.precision == kMixed && !d.s.fp64_now;
     bfx = 0.0; bfy = 0.0; btq = 0.0; bpe = 0.0;
     for (int base = 0; base < nvb; base += 32) {
         int k = base + lane;
@@ -133,14 +137,29 @@ __device__ __forceinline__ void body_forces(const BumpySys *__restrict__ bs, int
             double2 q = x.vpos[v];
             int cnt = min(x.vcount[v], capv);
             double ax = 0.0, ay = 0.0, en = 0.0;
-            for (int t = 0; t < cnt; t++) {
-                int u = __ldg(&x.vnbr[(size_t)t * nv + v]);
-                double2 o = x.vpos[u];
-                double fx, fy;
-                double e = disk_pair(q.x, q.y, rv, o.x, o.y, rv, bx, by, e_c, n_c, fx, fy);
-                ax += fx;
-                ay += fy;
-                en += e;
+            if (mixed) {  // FP32 vertex pairs; torque and body sums stay FP64
+                const float4 a = x.vpk[v];
+                float sx = 0.f, sy = 0.f, se = 0.f;
+                for (int t = 0; t < cnt; t++) {
+                    int u = __ldg(&x.vnbr[(size_t)t * nv + v]);
+                    float fx, fy;
+                    se += mixed_pair(d.p, a, x.vpk[u], (float)e_c, (float)n_c, fx, fy);
+                    sx += fx;
+                    sy += fy;
+                }
+                ax = (double)sx;
+                ay = (double)sy;
+                en = (double)se;
+            } else {
+                for (int t = 0; t < cnt; t++) {
+                    int u = __ldg(&x.vnbr[(size_t)t * nv + v]);
+                    double2 o = x.vpos[u];
+                    double fx, fy;
+                    double e = disk_pair(q.x, q.y, rv, o.x, o.y, rv, bx, by, e_c, n_c, fx, fy);
+                    ax += fx;
+                    ay += fy;
+                    en += e;
+                }
             }
             if (cnt > 0) {
                 vfx = 0.0 + ax;
@@ -157,6 +176,13 @@ __device__ __forceinline__ void body_forces(const BumpySys *__restrict__ bs, int
             bpe += __shfl_sync(0xffffffffu, vpe, l);
         }
     }
+}
+
+// mixed form: packed offsets of every vertex from the current vertex positions
+__global__ void kb_mixed_refresh(BumpySys *bs) {
+    int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= bs->x.nv) return;
+    bs->x.vpk[v] = mixed_pack(bs->b.p, bs->x.vpos[v], bs->x.rv);
 }
 
 // drop-in calculateForces (+= into the body arrays)
@@ -275,6 +301,7 @@ __global__ void kb_vlist(BumpySys *bs) {
             }
             x.vcount[v] = cnt;
             mxc = max(mxc, cnt);
+            if (d.p.precision == kMixed) x.vpk[v] = mixed_pack(d.p, q, x.rv);
         }
     }
     double val[1] = {(double)mxc};
@@ -520,10 +547,18 @@ __global__ void kb_fire_force(BumpySys *bs, int mode, double tmax_target) {
     double diff = fabs(avg / s.last_avg_pe - 1);
     s.last_avg_pe = avg;
     long long it = s.iter;
-    if (diff < s.pe_diff_target || avg < s.pe_target) {
+    // mixed form: FP32 vertex pairs until the switch (as k_fire_force), then FP64
+    bool fp64 = true;
+    if (ds->p.precision == kMixed && !s.fp64_now) {
+        double g2 = fmax(v[2], v[3]);
+        if (g2 < 0.81 * s.best_f2) { s.best_f2 = g2; s.best_it = it; }
+        if (sqrt(g2) <= s.switch_fmax || s.f_nbad > 5 || it - s.best_it > 2000) s.fp64_now = 1;
+        fp64 = false;
+    }
+    if ((fp64 && diff < s.pe_diff_target) || avg < s.pe_target) {
         s.result_step = it; s.f_converged = 1; s.flags |= kDone; return;
     }
-    if (s.fmax_target > 0 && sqrt(v[2]) <= s.fmax_target && sqrt(v[3]) <= tmax_target) {
+    if (fp64 && s.fmax_target > 0 && sqrt(v[2]) <= s.fmax_target && sqrt(v[3]) <= tmax_target) {
         s.result_step = it; s.f_converged = 1; s.flags |= kDone; return;
     }
     if (it + 1 >= s.max_steps) { s.result_step = s.max_steps; s.flags |= kDone; return; }

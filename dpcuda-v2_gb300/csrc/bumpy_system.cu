@@ -43,6 +43,7 @@ struct dpg_bumpy_system {
     cudaGraphExec_t loop_exec[2] = {nullptr, nullptr};
     cudaGraphConditionalHandle h_loop[2] = {0, 0}, h_rb[2] = {0, 0};
     double loop_dt = 0.0, loop_tmax = 0.0;
+    double switch_fmax = 1e-6;  // mixed form: FP32 vertex pairs until max(|F|, |tau|) <= this
     int gb(int count) const { return std::max(1, (count + kTPB - 1) / kTPB); }
     int gw(int bodies) const { return std::max(1, (bodies + kWarpsPerBlock - 1) / kWarpsPerBlock); }
     DevSys *ds() const { return &d->b; }
@@ -55,6 +56,16 @@ typedef dpg_bumpy_system BS;
         kern<<<(blocks), (threads), 0, s->stream>>>(__VA_ARGS__); \
         CK(cudaGetLastError());                                   \
     } while (0)
+
+// mixed form: vertex offsets from the current vertex positions, before a force
+// evaluation that follows host-side or single-operation changes (the loop
+// kernels keep them current themselves)
+static int vrefresh(BS *s) {
+    if (s->prm.precision != DPG_MIXED) return DPG_OK;
+    kb_mixed_refresh<<<(s->nv + kTPB - 1) / kTPB, kTPB, 0, s->stream>>>(s->d);
+    CK(cudaGetLastError());
+    return DPG_OK;
+}
 
 static int balloc(BS *s, void **p, size_t bytes) {
     CK(cudaMalloc(p, bytes > 0 ? bytes : 16));
@@ -104,7 +115,8 @@ extern "C" int dpg_bumpy_create(const dpg_bumpy_params *p, void *cuda_stream, dp
         return set_err(DPG_ERR_ARG, "dpg_bumpy_create: need 1 <= n_bodies <= n_vertices <= 2^30");
     if (!(p->box_x > 0) || !(p->box_y > 0) || !(p->vertex_radius > 0))
         return set_err(DPG_ERR_ARG, "dpg_bumpy_create: box and vertex radius must be > 0");
-    if (p->precision != DPG_FP64) return set_err(DPG_ERR_ARG, "dpg_bumpy_create: DPG_FP64 only");
+    if (p->precision != DPG_FP64 && p->precision != DPG_MIXED)
+        return set_err(DPG_ERR_ARG, "dpg_bumpy_create: precision must be DPG_FP64 or DPG_MIXED");
     BS *s = new BS();
     s->nb = (int)p->n_bodies;
     s->nv = (int)p->n_vertices;
@@ -141,6 +153,7 @@ extern "C" int dpg_bumpy_create(const dpg_bumpy_params *p, void *cuda_stream, dp
     A((void **)&x.vpos, nv * 16); A((void **)&x.vpos_t, nv * 16); A((void **)&x.vmass, nv * 8);
     A((void **)&x.vmass_t, nv * 8); A((void **)&x.vbody, nv * 4); A((void **)&x.vbody_t, nv * 4);
     A((void **)&x.svidx, nv * 4); A((void **)&x.svidx_t, nv * 4); A((void **)&x.vcount, nv * 4);
+    if (p->precision == DPG_MIXED) A((void **)&x.vpk, nv * 16);
     A((void **)&s->xfer, std::max(nb, nv) * 16);
     A((void **)&s->d, sizeof(BumpySys));
     if (rc == DPG_OK) {
@@ -152,6 +165,10 @@ extern "C" int dpg_bumpy_create(const dpg_bumpy_params *p, void *cuda_stream, dp
     DevParams &pp = s->h.b.p;
     pp.n = s->nb; pp.method = -1; pp.cap = 4; pp.precision = p->precision;
     pp.box[0] = p->box_x; pp.box[1] = p->box_y; pp.e_c = p->e_c; pp.n_c = p->n_c;
+    if (p->precision == DPG_MIXED) {
+        mixed_grid_init(pp);
+        mixed_grid_update(pp);
+    }
     memset(&s->h.b.s, 0, sizeof(DevState));
     x.nv = s->nv; x.capv = 4; x.rotation = p->rotation ? 1 : 0; x.rv = p->vertex_radius;
     x.vlist_built = 0;
@@ -474,6 +491,7 @@ extern "C" int dpg_bumpy_setup_neighbors(dpg_bumpy_handle s, const dpg_neighbor_
     DevParams &p = s->h.b.p;
     p.method = s->method; p.ncd = s->ncd; p.ncells = s->ncells; p.cap = s->cap;
     p.cutoff2 = s->cutoff * s->cutoff; p.cell_size = s->cs; p.nthr2 = s->nthr2; p.cthr2 = s->cthr2;
+    mixed_grid_update(p);
     CK(cudaMemcpyAsync(&s->d->b.p, &p, sizeof(DevParams), cudaMemcpyHostToDevice, s->stream));
     TRY(put(s, &s->d->x.vcut2, s->vcutoff * s->vcutoff));
     TRY(put(s, &s->d->x.vpcut2, s->vpcutoff * s->vpcutoff));
@@ -481,6 +499,7 @@ extern "C" int dpg_bumpy_setup_neighbors(dpg_bumpy_handle s, const dpg_neighbor_
     TRY(put(s, &s->d->x.vlist_built, s->hs->n_rebuilds));
     TRY(rebuild_now(s, s->method == DPG_NEIGH_CELL ? 2 : 1));
     s->have_neighbors = true;
+    TRY(vrefresh(s));
     LAUNCH(kb_force_acc, s->gw(s->nb), kTPB, s->d);
     CK(cudaStreamSynchronize(s->stream));
     if (info) return dpg_bumpy_neighbor_info_get(s, info, nullptr);
@@ -535,6 +554,7 @@ extern "C" int dpg_bumpy_zero_forces(dpg_bumpy_handle s) {
 
 extern "C" int dpg_bumpy_compute_forces(dpg_bumpy_handle s) {
     TRY(need(s));
+    TRY(vrefresh(s));
     LAUNCH(kb_force_acc, s->gw(s->nb), kTPB, s->d);
     return DPG_OK;
 }
@@ -585,6 +605,7 @@ extern "C" int dpg_bumpy_scale_box(dpg_bumpy_handle s, double factor) {
     s->h.b.p.box[0] = nl;
     s->h.b.p.box[1] = nl;
     if (s->ncd > 0) { s->cs = nl / s->ncd; s->h.b.p.cell_size = s->cs; }
+    mixed_grid_update(s->h.b.p);
     CK(cudaMemcpyAsync(&s->d->b.p, &s->h.b.p, sizeof(DevParams), cudaMemcpyHostToDevice, s->stream));
     return DPG_OK;
 }
@@ -685,6 +706,7 @@ static int build_graph(BS *s, int kind) {
 
 static int run_loop(BS *s, int kind, int *ovf) {
     *ovf = 0;
+    TRY(vrefresh(s));
     if (s->mode == 2) {
         if (build_graph(s, kind) != DPG_OK) {
             s->mode = 0;
@@ -755,10 +777,19 @@ extern "C" int dpg_bumpy_fire_step(dpg_bumpy_handle s, int *stopped) {
     LAUNCH(kb_fire_move, s->gw(s->nb), kTPB, s->d);
     TRY(enqueue_rebuild(s));
     TRY(resolve_overflow(s));
+    TRY(vrefresh(s));
     LAUNCH(kb_fire_force, s->gw(s->nb), kTPB, s->d, 2, 0.0);
     TRY(pull(s));
     if (stopped) *stopped = s->hs->f_stopped;
     TRY(put(s, &s->d->b.s.flags, 0));
+    return DPG_OK;
+}
+
+extern "C" int dpg_bumpy_set_mixed_switch(dpg_bumpy_handle s, double switch_fmax) {
+    if (!s) return set_err(DPG_ERR_ARG, "null handle");
+    if (s->prm.precision != DPG_MIXED) return set_err(DPG_ERR_STATE, "not a DPG_MIXED system");
+    if (!(switch_fmax >= 0)) return set_err(DPG_ERR_ARG, "switch_fmax must be >= 0");
+    s->switch_fmax = switch_fmax;
     return DPG_OK;
 }
 
@@ -774,11 +805,13 @@ extern "C" int dpg_bumpy_fire_minimize(dpg_bumpy_handle s, const dpg_fire_params
     st.pe_target = p->avg_pe_target; st.pe_diff_target = p->avg_pe_diff_target;
     st.fmax_target = p->fmax_target; st.dof = (double)s->nb;
     st.guard = 0; st.guard_limit = p->max_steps + 4; st.h_loop = 0; st.h_rb = 0;
+    st.fp64_now = 0; st.switch_fmax = s->switch_fmax; st.best_f2 = INFINITY; st.best_it = 0;
     CK(cudaMemcpyAsync(&s->d->b.s, &st, sizeof(DevState), cudaMemcpyHostToDevice, s->stream));
     LAUNCH(kb_zero_vel, s->gb(s->nb), kTPB, s->d);
     LAUNCH(k_decide_rebuild, 1, 1, &s->d->b);
     TRY(enqueue_rebuild(s));
     TRY(resolve_overflow(s));
+    TRY(vrefresh(s));
     LAUNCH(kb_fire_force, s->gw(s->nb), kTPB, s->d, 1, tmax);
     for (int guard = 0; guard < 64; guard++) {
         TRY(pull(s));
@@ -795,6 +828,7 @@ extern "C" int dpg_bumpy_fire_minimize(dpg_bumpy_handle s, const dpg_fire_params
     LAUNCH(kb_zero_vel, s->gb(s->nb), kTPB, s->d);
     LAUNCH(kb_observables, s->gb(s->nb), kTPB, s->d);
     TRY(pull(s));
+    TRY(put(s, &s->d->b.s.fp64_now, 0));  // later calls start in FP32 again
     if (r) {
         r->steps = s->hs->result_step;
         r->stopped = s->hs->f_stopped;

@@ -14,6 +14,8 @@
 namespace dpg {
 namespace {  // kernels have internal linkage: each translation unit owns its copy
 
+constexpr int kMixed = 1;  // DevParams.precision of the mixed form (DPG_MIXED)
+
 __device__ __forceinline__ bool halted(const DevSys *ds) { return ds->s.flags != 0; }
 
 // harmonic (power-law) contact of particle i with j, force on i:
@@ -63,6 +65,116 @@ __device__ __forceinline__ void disk_force_sum(const DevSys *__restrict__ ds, in
         ay += fy;
         en += e;
     }
+}
+
+// The same sum with G threads per particle (G a power of two <= 32, groups
+// aligned inside a warp): lane `sub` of the group evaluates neighbour slots
+// sub, sub + G, ...; the pair terms are then shuffled so that every lane of
+// the group adds them in slot order 0, 1, 2, ..., the order of the sequential
+// loop above, so the result is bit-identical to disk_force_sum.  Small systems
+// get G times more warps in flight to hide the FP64 divide / sqrt latency.
+// Every lane of the warp must call this (shuffles); `valid` is false for lanes
+// past the last particle.
+template <int G>
+__device__ __forceinline__ void disk_force_sum_g(const DevSys *__restrict__ ds, int i, bool valid,
+                                                 double &ax, double &ay, double &en) {
+    const int n = ds->p.n;
+    const double bx = ds->p.box[0], by = ds->p.box[1], e_c = ds->p.e_c, n_c = ds->p.n_c;
+    const double2 *__restrict__ pos = ds->v.pos;
+    const double *__restrict__ rad = ds->v.rad;
+    const int *__restrict__ nbr = ds->v.nbr;
+    int cnt = 0;
+    double2 pi = make_double2(0.0, 0.0);
+    double ri = 0.0;
+    if (valid) {
+        cnt = ds->w.count[i];
+        if (cnt > ds->p.cap) cnt = ds->p.cap;
+        pi = pos[i];
+        ri = rad[i];
+    }
+    const int lane = threadIdx.x & 31, sub = lane & (G - 1), lead = lane - sub;
+    const int rounds = __reduce_max_sync(0xffffffffu, (unsigned)((cnt + G - 1) / G));
+    ax = 0.0; ay = 0.0; en = 0.0;
+    for (int r = 0; r < rounds; r++) {
+        const int k = r * G + sub;
+        double fx = 0.0, fy = 0.0, e = 0.0;
+        if (k < cnt) {
+            int j = __ldg(&nbr[(size_t)k * n + i]);
+            double2 pj = pos[j];
+            e = disk_pair(pi.x, pi.y, ri, pj.x, pj.y, __ldg(&rad[j]), bx, by, e_c, n_c, fx, fy);
+        }
+#pragma unroll
+        for (int t = 0; t < G; t++) {
+            double gx = __shfl_sync(0xffffffffu, fx, lead + t);
+            double gy = __shfl_sync(0xffffffffu, fy, lead + t);
+            double ge = __shfl_sync(0xffffffffu, e, lead + t);
+            if (r * G + t < cnt) {
+                ax += gx;
+                ay += gy;
+                en += ge;
+            }
+        }
+    }
+}
+
+// Mixed form: FP32 pair forces from the packed offsets, summed in FP32 over
+// runs of 8 neighbours and in FP64 across runs and for the particle total.
+__device__ __forceinline__ void disk_force_sum_mixed(const DevSys *__restrict__ ds, int i,
+                                                     double &ax, double &ay, double &en) {
+    const int n = ds->p.n;
+    const float4 *__restrict__ pk = ds->v.pk;
+    const int *__restrict__ nbr = ds->v.nbr;
+    const float e_c = (float)ds->p.e_c, n_c = (float)ds->p.n_c;
+    int cnt = ds->w.count[i];
+    if (cnt > ds->p.cap) cnt = ds->p.cap;
+    const float4 a = pk[i];
+    ax = 0.0; ay = 0.0; en = 0.0;
+    for (int k0 = 0; k0 < cnt; k0 += 8) {
+        float sx = 0.f, sy = 0.f, se = 0.f;
+        const int k1 = min(cnt, k0 + 8);
+        for (int k = k0; k < k1; k++) {
+            int j = __ldg(&nbr[(size_t)k * n + i]);
+            float fx, fy;
+            se += mixed_pair(ds->p, a, pk[j], e_c, n_c, fx, fy);
+            sx += fx;
+            sy += fy;
+        }
+        ax += (double)sx;
+        ay += (double)sy;
+        en += (double)se;
+    }
+}
+
+// Pair sum of particle i for a force kernel with G threads per particle; the
+// mixed instantiation (M) uses FP32 pairs until the FIRE refinement switches
+// the system to FP64 (DevState.fp64_now).  All lanes of the warp call it.
+template <int G, bool M>
+__device__ __forceinline__ void force_sum(const DevSys *__restrict__ ds, int i, bool valid,
+                                          double &ax, double &ay, double &en) {
+    ax = 0.0; ay = 0.0; en = 0.0;
+    if (M && !ds->s.fp64_now) {
+        if (valid) disk_force_sum_mixed(ds, i, ax, ay, en);
+        return;
+    }
+    if (G == 1) {
+        if (valid) {
+            const double2 *__restrict__ pos = ds->v.pos;
+            disk_force_sum(ds, i, pos[i], ds->v.rad[i], pos, ds->v.rad, ds->v.nbr, ax, ay, en);
+        }
+    } else {
+        disk_force_sum_g<G>(ds, i, valid, ax, ay, en);
+    }
+}
+
+__device__ __forceinline__ void mixed_update(DevSys *ds, int i, double2 p) {
+    if (ds->p.precision == kMixed) ds->v.pk[i] = mixed_pack(ds->p, p, ds->v.rad[i]);
+}
+
+// mixed form: offsets of every particle from the current positions
+__global__ void k_mixed_refresh(DevSys *ds) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ds->p.n) return;
+    ds->v.pk[i] = mixed_pack(ds->p, ds->v.pos[i], ds->v.rad[i]);
 }
 
 // device-side neighbour rebuild decision: checkForCellListUpdate /
@@ -150,20 +262,56 @@ __global__ void k_zero_force(DevSys *ds) {
 }
 
 // kernelCalcDiskForces (+= semantics): src/particles/disk/kernels.cu:11-57
+template <int G, bool M>
 __global__ void k_force_acc(DevSys *ds) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= ds->p.n) return;
-    if (ds->w.count[i] == 0) return;
-    const double2 *__restrict__ pos = ds->v.pos;
-    double2 pi = pos[i];
+    const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = gid / G;
     double ax, ay, en;
-    disk_force_sum(ds, i, pi, ds->v.rad[i], pos, ds->v.rad, ds->v.nbr, ax, ay, en);
+    if (G == 1) {
+        if (i >= ds->p.n) return;
+        if (ds->w.count[i] == 0) return;
+        force_sum<1, M>(ds, i, true, ax, ay, en);
+    } else {
+        force_sum<G, M>(ds, i, i < ds->p.n, ax, ay, en);
+        if (i >= ds->p.n || (gid & (G - 1)) != 0) return;
+        if (ds->w.count[i] == 0) return;
+    }
     double2 *frc = ds->v.frc;
     double2 f = frc[i];
     f.x += ax;
     f.y += ay;
     frc[i] = f;
     ds->w.pe[i] += en;
+}
+
+// kernelCalculateDampedForces: src/particles/base/kernels.cu:83-89
+__global__ void k_damp(DevSys *ds, double gamma) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ds->p.n) return;
+    double2 f = ds->v.frc[i], u = ds->v.vel[i];
+    f.x -= gamma * u.x;
+    f.y -= gamma * u.y;
+    ds->v.frc[i] = f;
+}
+
+// kernelGradDescStep: src/particles/base/kernels.cu:613-637, with the
+// displacement maxima kept as in k_drift
+__global__ void k_grad_desc(DevSys *ds, double alpha) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double v[2] = {0.0, 0.0};
+    if (i < ds->p.n) {
+        double2 *pos = ds->v.pos;
+        double2 p = pos[i], f = ds->v.frc[i];
+        p.x = p.x + alpha * f.x;
+        p.y = p.y + alpha * f.y;
+        pos[i] = p;
+        double2 a = ds->w.pos_n[i], c = ds->w.pos_c[i];
+        double dxn = p.x - a.x, dyn = p.y - a.y, dxc = p.x - c.x, dyc = p.y - c.y;
+        v[0] = dxn * dxn + dyn * dyn;
+        v[1] = dxc * dxc + dyc * dyc;
+    }
+    const int ops[2] = {1, 1};
+    if (grid_reduce<2>(v, ops, ds)) { ds->s.max_nd2 = v[0]; ds->s.max_cd2 = v[1]; }
 }
 
 // PE and KE totals (kernelCalculateTranslationalKineticEnergy + reductions,
@@ -471,6 +619,7 @@ __global__ void k_nlist_cell(DevSys *ds) {
         }
         ds->w.count[i] = cnt;
         ds->w.pos_n[i] = pi;
+        mixed_update(ds, i, pi);
     }
     finish_list_build(ds, cnt);
 }
@@ -510,6 +659,7 @@ __global__ void k_nlist_all(DevSys *ds) {
     if (i < n) {
         ds->w.count[i] = cnt;
         ds->w.pos_n[i] = pi;
+        mixed_update(ds, i, pi);
     }
     finish_list_build(ds, cnt);
 }
@@ -534,6 +684,7 @@ __global__ void k_nve_first(DevSys *ds, double dt_half, double dt) {
         p.x = p.x + u.x * dt;
         p.y = p.y + u.y * dt;
         pos[i] = p;
+        mixed_update(ds, i, p);
         double2 a = ds->w.pos_n[i], c = ds->w.pos_c[i];
         double dxn = p.x - a.x, dyn = p.y - a.y, dxc = p.x - c.x, dyc = p.y - c.y;
         v[0] = dxn * dxn + dyn * dyn;
@@ -550,19 +701,28 @@ __global__ void k_nve_first(DevSys *ds, double dt_half, double dt) {
 }
 
 // NVE::step second half (src/integrator/nve.cu:21-24): zero, forces, kick dt/2.
+template <int G, bool M>
 __global__ void k_nve_second(DevSys *ds, double dt_half) {
     if (halted(ds)) return;
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < ds->p.n) {
-        const double2 *__restrict__ pos = ds->v.pos;
-        double2 pi = pos[i];
-        double ax, ay, en;
-        disk_force_sum(ds, i, pi, ds->v.rad[i], pos, ds->v.rad, ds->v.nbr, ax, ay, en);
-        double2 f = make_double2(0.0 + ax, 0.0 + ay);
-        ds->v.frc[i] = f;
-        ds->w.pe[i] = 0.0 + en;
+    const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = gid / G;
+    double ax, ay, en;
+    force_sum<G, M>(ds, i, i < ds->p.n, ax, ay, en);
+    if (i < ds->p.n && (gid & (G - 1)) == 0) {
         double2 *vel = ds->v.vel;
         double2 u = vel[i];
+        double2 f;
+        const double g = ds->s.damping;
+        if (g != 0.0) {
+            // DampedNVE::step (src/integrator/damped_nve.cu:22-23): F = 0 - g v,
+            // then += the pair sum unless the particle has no neighbours
+            f = make_double2(0.0 - g * u.x, 0.0 - g * u.y);
+            if (ds->w.count[i] != 0) { f.x += ax; f.y += ay; }
+        } else {
+            f = make_double2(0.0 + ax, 0.0 + ay);
+        }
+        ds->v.frc[i] = f;
+        ds->w.pe[i] = 0.0 + en;
         double dtm = dt_half / ds->v.mass[i];
         u.x = u.x + f.x * dtm;
         u.y = u.y + f.y * dtm;
@@ -628,6 +788,7 @@ __global__ void k_fire_move(DevSys *ds) {
         p.x = p.x + u.x * dt;
         p.y = p.y + u.y * dt;
         pos[i] = p;
+        mixed_update(ds, i, p);
         double2 a = ds->w.pos_n[i], c = ds->w.pos_c[i];
         double dxn = p.x - a.x, dyn = p.y - a.y, dxc = p.x - c.x, dyc = p.y - c.y;
         v[0] = dxn * dxn + dyn * dyn;
@@ -648,15 +809,15 @@ __global__ void k_fire_move(DevSys *ds) {
 // next step's Fire::step decision.  mode 0 = loop iteration, 1 = setup
 // (forces only: minimizeFire's initial force call and last_avg_pe), 2 = a
 // single Fire::step (no convergence test, decision for the next step only).
+template <int G, bool M>
 __global__ void k_fire_force(DevSys *ds, int mode) {
     if (halted(ds)) return;
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = gid / G;
     double v[3] = {0.0, 0.0, 0.0};
-    if (i < ds->p.n) {
-        const double2 *__restrict__ pos = ds->v.pos;
-        double2 pi = pos[i];
-        double ax, ay, en;
-        disk_force_sum(ds, i, pi, ds->v.rad[i], pos, ds->v.rad, ds->v.nbr, ax, ay, en);
+    double ax, ay, en;
+    force_sum<G, M>(ds, i, i < ds->p.n, ax, ay, en);
+    if (i < ds->p.n && (gid & (G - 1)) == 0) {
         double2 f = make_double2(0.0 + ax, 0.0 + ay);
         ds->v.frc[i] = f;
         ds->w.pe[i] = 0.0 + en;
@@ -689,10 +850,19 @@ __global__ void k_fire_force(DevSys *ds, int mode) {
     double diff = fabs(avg / s.last_avg_pe - 1);
     s.last_avg_pe = avg;
     long long it = s.iter;
-    if (diff < s.pe_diff_target || avg < s.pe_target) {
+    // mixed form: FP32 pairs until max|F| reaches switch_fmax, FIRE keeps going
+    // uphill, or max|F| stops falling (FP32 noise floor); FP64 pairs after, and
+    // only an FP64 state may pass the PE-change and max|F| tests
+    bool fp64 = true;
+    if (M && !s.fp64_now) {
+        if (v[2] < 0.81 * s.best_f2) { s.best_f2 = v[2]; s.best_it = it; }
+        if (sqrt(v[2]) <= s.switch_fmax || s.f_nbad > 5 || it - s.best_it > 2000) s.fp64_now = 1;
+        fp64 = false;
+    }
+    if ((fp64 && diff < s.pe_diff_target) || avg < s.pe_target) {
         s.result_step = it; s.f_converged = 1; s.flags |= kDone; return;
     }
-    if (s.fmax_target > 0 && sqrt(v[2]) <= s.fmax_target) {
+    if (fp64 && s.fmax_target > 0 && sqrt(v[2]) <= s.fmax_target) {
         s.result_step = it; s.f_converged = 1; s.flags |= kDone; return;
     }
     if (it + 1 >= s.max_steps) { s.result_step = s.max_steps; s.flags |= kDone; return; }

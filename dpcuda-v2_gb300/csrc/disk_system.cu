@@ -94,6 +94,41 @@ struct dpg_system {
     int tpb = kTPB;
     int grid(int count) const { return std::max(1, (count + tpb - 1) / tpb); }
     int grid_full(int count) const { return std::max(1, (count + kTPB - 1) / kTPB); }
+    // force kernels: fg threads per particle (bit-identical sums, more warps
+    // in flight for small systems), ftpb threads per block
+    int fg = 1;
+    int ftpb = kTPB;
+    int fgrid() const { return std::max(1, (int)(((long long)n * fg + ftpb - 1) / ftpb)); }
+    // mixed form (precision DPG_MIXED): FP32 pair kernels, one thread per particle
+    bool mixed = false;
+    double switch_fmax = 1e-6;
+    void *fire_force_fn() const {
+        if (mixed) return (void *)k_fire_force<1, true>;
+        switch (fg) {
+            case 2: return (void *)k_fire_force<2, false>;
+            case 4: return (void *)k_fire_force<4, false>;
+            case 8: return (void *)k_fire_force<8, false>;
+            default: return (void *)k_fire_force<1, false>;
+        }
+    }
+    void *nve_second_fn() const {
+        if (mixed) return (void *)k_nve_second<1, true>;
+        switch (fg) {
+            case 2: return (void *)k_nve_second<2, false>;
+            case 4: return (void *)k_nve_second<4, false>;
+            case 8: return (void *)k_nve_second<8, false>;
+            default: return (void *)k_nve_second<1, false>;
+        }
+    }
+    void *force_acc_fn() const {
+        if (mixed) return (void *)k_force_acc<1, true>;
+        switch (fg) {
+            case 2: return (void *)k_force_acc<2, false>;
+            case 4: return (void *)k_force_acc<4, false>;
+            case 8: return (void *)k_force_acc<8, false>;
+            default: return (void *)k_force_acc<1, false>;
+        }
+    }
 };
 
 static int dalloc(dpg_system *s, void **p, size_t bytes) {
@@ -113,6 +148,7 @@ static void free_graphs(dpg_system *s) {
 }
 
 static int push_params(dpg_system *s) {
+    mixed_grid_update(s->h.p);
     CK(cudaMemcpyAsync(&s->d->p, &s->h.p, sizeof(DevParams), cudaMemcpyHostToDevice, s->stream));
     return DPG_OK;
 }
@@ -141,6 +177,36 @@ static int check_launch(dpg_system *s) {
         TRY(check_launch(s));                                           \
     } while (0)
 
+// launch of a kernel chosen at run time (the force kernels' group size)
+template <class... A>
+static int launch_fn(dpg_system *s, void *fn, int blocks, int threads, A... a) {
+    void *args[] = {(void *)&a...};
+    CK(cudaLaunchKernel(fn, dim3(blocks), dim3(threads), args, 0, s->stream));
+    return DPG_OK;
+}
+
+// mixed form: offsets from the current positions (after any host-side or
+// single-operation change of positions or box; the loop kernels keep them
+// current themselves)
+static int mixed_refresh(dpg_system *s) {
+    if (!s->mixed) return DPG_OK;
+    k_mixed_refresh<<<s->grid(s->n), s->tpb, 0, s->stream>>>(s->d);
+    CK(cudaGetLastError());
+    return DPG_OK;
+}
+
+static int launch_force_acc(dpg_system *s) {
+    TRY(mixed_refresh(s));
+    return launch_fn(s, s->force_acc_fn(), s->fgrid(), s->ftpb, s->d);
+}
+static int launch_fire_force(dpg_system *s, int mode) {
+    if (mode != 0) TRY(mixed_refresh(s));
+    return launch_fn(s, s->fire_force_fn(), s->fgrid(), s->ftpb, s->d, mode);
+}
+static int launch_nve_second(dpg_system *s, double dt_half) {
+    return launch_fn(s, s->nve_second_fn(), s->fgrid(), s->ftpb, s->d, dt_half);
+}
+
 // ---------------------------------------------------------------------------
 // creation / destruction
 // ---------------------------------------------------------------------------
@@ -149,7 +215,8 @@ extern "C" int dpg_create(const dpg_params *p, void *cuda_stream, dpg_handle *ou
     if (p->n_particles <= 0 || p->n_particles > (1LL << 30))
         return set_err(DPG_ERR_ARG, "dpg_create: n_particles must be in [1, 2^30]");
     if (!(p->box_x > 0) || !(p->box_y > 0)) return set_err(DPG_ERR_ARG, "dpg_create: box must be > 0");
-    if (p->precision != DPG_FP64) return set_err(DPG_ERR_ARG, "dpg_create: this entry point builds DPG_FP64 systems");
+    if (p->precision != DPG_FP64 && p->precision != DPG_MIXED)
+        return set_err(DPG_ERR_ARG, "dpg_create: precision must be DPG_FP64 or DPG_MIXED");
     dpg_system *s = new dpg_system();
     s->n = (int)p->n_particles;
     s->prm = *p;
@@ -170,6 +237,19 @@ extern "C" int dpg_create(const dpg_params *p, void *cuda_stream, dpg_handle *ou
     while (s->tpb > 32 && (long long)s->n < (long long)s->tpb * 2 * nsm) s->tpb >>= 1;
     const char *tp = getenv("DPG_TPB");
     if (tp && atoi(tp) >= 32 && atoi(tp) <= kTPB) s->tpb = atoi(tp) & ~31;
+    // group size for the force kernels: enough threads to give every SM about
+    // 6 warps, at most 8 lanes per particle (measured at N = 16384 on GB300:
+    // 52.7, 37.8, 42.2, 55.1 us per FIRE force pass for 1, 2, 4, 8 lanes)
+    s->fg = 1;
+    while (s->fg < 8 && (long long)s->n * s->fg < (long long)nsm * 192) s->fg <<= 1;
+    const char *fgs = getenv("DPG_FORCE_GROUP");
+    if (fgs) {
+        int g = atoi(fgs);
+        if (g == 1 || g == 2 || g == 4 || g == 8) s->fg = g;
+    }
+    s->ftpb = kTPB;
+    s->mixed = p->precision == DPG_MIXED;
+    if (s->mixed) s->fg = 1;
     int rc = DPG_OK;
     auto A = [&](void **pp, size_t b) { if (rc == DPG_OK) rc = dalloc(s, pp, b); };
     DevView &v = s->h.v;
@@ -179,10 +259,11 @@ extern "C" int dpg_create(const dpg_params *p, void *cuda_stream, dpg_handle *ou
     A((void **)&v.pos_t, n * 16); A((void **)&v.vel_t, n * 16); A((void **)&v.frc_t, n * 16);
     A((void **)&v.rad_t, n * 8); A((void **)&v.mass_t, n * 8); A((void **)&v.sidx_t, n * 4);
     A((void **)&v.m1, n * 16); A((void **)&v.m2, n * 16); A((void **)&v.m1_t, n * 16); A((void **)&v.m2_t, n * 16);
+    if (s->mixed) A((void **)&v.pk, n * 16);
     A((void **)&w.pos_n, n * 16); A((void **)&w.pos_c, n * 16); A((void **)&w.pe, n * 8);
     A((void **)&w.count, n * 4); A((void **)&w.cell_raw, n * 4); A((void **)&w.cell_of, n * 4);
     A((void **)&w.perm, n * 4);
-    w.max_blocks = std::max(s->grid(s->n), s->grid_full(s->n));
+    w.max_blocks = std::max(std::max(s->grid(s->n), s->grid_full(s->n)), s->fgrid());
     A((void **)&w.partials, (size_t)w.max_blocks * 8 * 8);
     A((void **)&w.s_pos, n * 16); A((void **)&w.s_vel, n * 16); A((void **)&w.s_frc, n * 16);
     A((void **)&w.s_rad, n * 8); A((void **)&w.s_mass, n * 8); A((void **)&w.s_sidx, n * 4);
@@ -196,6 +277,10 @@ extern "C" int dpg_create(const dpg_params *p, void *cuda_stream, dpg_handle *ou
     DevParams &pp = s->h.p;
     pp.n = s->n; pp.method = -1; pp.cap = 4; pp.precision = p->precision;
     pp.box[0] = p->box_x; pp.box[1] = p->box_y; pp.e_c = p->e_c; pp.n_c = p->n_c;
+    if (s->mixed) {
+        mixed_grid_init(pp);
+        mixed_grid_update(pp);
+    }
     memset(&s->h.s, 0, sizeof(DevState));
     rc = [&]() -> int {
         CK(cudaMemcpyAsync(s->d, &s->h, sizeof(DevSys), cudaMemcpyHostToDevice, s->stream));
@@ -544,7 +629,7 @@ extern "C" int dpg_setup_neighbors(dpg_handle s, const dpg_neighbor_config *cfg,
     TRY(rebuild_now(s, s->method == DPG_NEIGH_CELL ? 2 : 1));
     s->have_neighbors = true;
     // setupNeighbors ends with calculateForces (accumulating)
-    LAUNCH(k_force_acc, s->grid(s->n), s->tpb, s->d);
+    TRY(launch_force_acc(s));
     CK(cudaStreamSynchronize(s->stream));
     if (info) return dpg_neighbor_info_get(s, info);
     return DPG_OK;
@@ -637,7 +722,7 @@ extern "C" int dpg_zero_forces(dpg_handle s) {
 
 extern "C" int dpg_compute_forces(dpg_handle s) {
     TRY(need_neighbors(s));
-    LAUNCH(k_force_acc, s->grid(s->n), s->tpb, s->d);
+    TRY(launch_force_acc(s));
     return DPG_OK;
 }
 
@@ -807,7 +892,7 @@ extern "C" int dpg_adam_minimize(dpg_handle s, double alpha, double b1, double b
         LAUNCH(k_zero_force, s->grid(s->n), s->tpb, s->d);
         int rb = 0;
         TRY(dpg_check_neighbors(s, &rb));
-        LAUNCH(k_force_acc, s->grid(s->n), s->tpb, s->d);
+        TRY(launch_force_acc(s));
         TRY(dpg_adam_step(s, step, alpha, b1, b2, eps));
         TRY(observe(s));
         double avg = s->hs->pe / dof;
@@ -851,8 +936,8 @@ static int enqueue_iteration(dpg_system *s, int kind) {
     if (kind == kLoopFire) LAUNCH(k_fire_move, G, s->tpb, s->d);
     else LAUNCH(k_nve_first, G, s->tpb, s->d, 0.5 * s->chunk_dt, s->chunk_dt);
     TRY(enqueue_rebuild(s));
-    if (kind == kLoopFire) LAUNCH(k_fire_force, G, s->tpb, s->d, 0);
-    else LAUNCH(k_nve_second, G, s->tpb, s->d, 0.5 * s->chunk_dt);
+    if (kind == kLoopFire) TRY(launch_fire_force(s, 0));
+    else TRY(launch_nve_second(s, 0.5 * s->chunk_dt));
     return DPG_OK;
 }
 
@@ -928,8 +1013,8 @@ static int build_cond_graph(dpg_system *s, int kind) {
         cudaGraphNode_t prev = nullptr;
         for (auto &k : rebuild_nodes(s)) prev = add_kernel(ib, prev, k.fn, k.blocks, k.threads, a_d, &err);
         last = inode;
-        if (kind == kLoopFire) last = add_kernel(body, last, (void *)k_fire_force, G, s->tpb, a_ff, &err);
-        else last = add_kernel(body, last, (void *)k_nve_second, G, s->tpb, a_nve2, &err);
+        if (kind == kLoopFire) last = add_kernel(body, last, s->fire_force_fn(), s->fgrid(), s->ftpb, a_ff, &err);
+        else last = add_kernel(body, last, s->nve_second_fn(), s->fgrid(), s->ftpb, a_nve2, &err);
         last = add_kernel(body, last, (void *)k_loop_guard, 1, 1, a_d, &err);
     }
     if (err == cudaSuccess) err = cudaGraphInstantiate(&s->loop_exec[kind], g, 0);
@@ -948,6 +1033,7 @@ static int build_cond_graph(dpg_system *s, int kind) {
 // finish the interrupted iteration.
 static int run_loop(dpg_system *s, int kind, int *halted_overflow) {
     *halted_overflow = 0;
+    TRY(mixed_refresh(s));
     if (s->mode == kModeCond) {
         int rc = build_cond_graph(s, kind);
         if (rc != DPG_OK) {
@@ -981,8 +1067,8 @@ static int run_loop(dpg_system *s, int kind, int *halted_overflow) {
 // run the interrupted iteration's second half.
 static int finish_after_overflow(dpg_system *s, int kind) {
     TRY(resolve_overflow(s));
-    if (kind == kLoopFire) LAUNCH(k_fire_force, s->grid(s->n), s->tpb, s->d, 0);
-    else LAUNCH(k_nve_second, s->grid(s->n), s->tpb, s->d, 0.5 * s->chunk_dt);
+    if (kind == kLoopFire) TRY(launch_fire_force(s, 0));
+    else TRY(launch_nve_second(s, 0.5 * s->chunk_dt));
     return pull_state(s);
 }
 
@@ -1011,6 +1097,46 @@ extern "C" int dpg_nve_steps(dpg_handle s, double dt, int64_t n_steps) {
         return set_err(DPG_ERR_STATE, "NVE loop ended after %lld of %lld steps",
                        s->hs->nve_steps_done, (long long)n_steps);
     TRY(put_field(s, &s->d->s.flags, 0));
+    return DPG_OK;
+}
+
+extern "C" int dpg_set_mixed_switch(dpg_handle s, double switch_fmax) {
+    if (!s) return set_err(DPG_ERR_ARG, "null handle");
+    if (!s->mixed) return set_err(DPG_ERR_STATE, "not a DPG_MIXED system");
+    if (!(switch_fmax >= 0)) return set_err(DPG_ERR_ARG, "switch_fmax must be >= 0");
+    s->switch_fmax = switch_fmax;
+    return DPG_OK;
+}
+
+// ---- damped NVE and gradient descent -------------------------------------
+extern "C" int dpg_damped_forces(dpg_handle s, double damping) {
+    if (!s) return set_err(DPG_ERR_ARG, "null handle");
+    LAUNCH(k_damp, s->grid(s->n), s->tpb, s->d, damping);
+    return DPG_OK;
+}
+
+extern "C" int dpg_damped_nve_steps(dpg_handle s, double dt, double damping, int64_t n_steps) {
+    if (!s) return set_err(DPG_ERR_ARG, "null handle");
+    TRY(put_field(s, &s->d->s.damping, damping));
+    int rc = dpg_nve_steps(s, dt, n_steps);
+    int rc2 = put_field(s, &s->d->s.damping, 0.0);
+    return rc != DPG_OK ? rc : rc2;
+}
+
+extern "C" int dpg_grad_desc_step(dpg_handle s, double alpha) {
+    if (!s) return set_err(DPG_ERR_ARG, "null handle");
+    LAUNCH(k_grad_desc, s->grid(s->n), s->tpb, s->d, alpha);
+    return DPG_OK;
+}
+
+extern "C" int dpg_grad_desc_steps(dpg_handle s, double alpha, int64_t n_steps) {
+    TRY(need_neighbors(s));
+    for (int64_t t = 0; t < n_steps; t++) {
+        TRY(dpg_zero_forces(s));
+        TRY(dpg_check_neighbors(s, nullptr));
+        TRY(launch_force_acc(s));
+        TRY(dpg_grad_desc_step(s, alpha));
+    }
     return DPG_OK;
 }
 
@@ -1047,7 +1173,7 @@ extern "C" int dpg_fire_step(dpg_handle s, int *stopped) {
     LAUNCH(k_fire_move, s->grid(s->n), s->tpb, s->d);
     TRY(enqueue_rebuild(s));
     TRY(resolve_overflow(s));
-    LAUNCH(k_fire_force, s->grid(s->n), s->tpb, s->d, 2);
+    TRY(launch_fire_force(s, 2));
     TRY(pull_state(s));
     if (stopped) *stopped = s->hs->f_stopped;
     TRY(put_field(s, &s->d->s.flags, 0));
@@ -1073,13 +1199,17 @@ extern "C" int dpg_fire_minimize(dpg_handle s, const dpg_fire_params *p, dpg_fir
     st.guard_limit = p->max_steps + 4;
     st.h_loop = 0;
     st.h_rb = 0;
+    st.fp64_now = 0;  // mixed form: FP32 pairs first, FP64 refinement after the switch
+    st.switch_fmax = s->switch_fmax;
+    st.best_f2 = INFINITY;
+    st.best_it = 0;
     CK(cudaMemcpyAsync(&s->d->s, &st, sizeof(DevState), cudaMemcpyHostToDevice, s->stream));
     // minimizeFire setup: v = 0, zero, neighbour check, forces, last PE
     LAUNCH(k_zero_vel, s->grid(s->n), s->tpb, s->d);
     LAUNCH(k_decide_rebuild, 1, 1, s->d);
     TRY(enqueue_rebuild(s));
     TRY(resolve_overflow(s));
-    LAUNCH(k_fire_force, s->grid(s->n), s->tpb, s->d, 1);
+    TRY(launch_fire_force(s, 1));
     for (int guard = 0; guard < 64; guard++) {
         TRY(pull_state(s));
         if (s->hs->flags & kDone) break;
@@ -1095,6 +1225,7 @@ extern "C" int dpg_fire_minimize(dpg_handle s, const dpg_fire_params *p, dpg_fir
     // minimizeFire ends with setVelocitiesToZero
     LAUNCH(k_zero_vel, s->grid(s->n), s->tpb, s->d);
     TRY(observe(s));
+    TRY(put_field(s, &s->d->s.fp64_now, 0));  // later calls start in FP32 again
     if (r) {
         r->steps = s->hs->result_step;
         r->stopped = s->hs->f_stopped;
@@ -1129,12 +1260,13 @@ extern "C" int dpg_profile_loop(dpg_handle s, int kind, int iters, double dt, do
         LAUNCH(k_decide_rebuild, 1, 1, s->d);
         TRY(enqueue_rebuild(s));
         TRY(resolve_overflow(s));
-        LAUNCH(k_fire_force, s->grid(s->n), s->tpb, s->d, 1);
+        TRY(launch_fire_force(s, 1));
     } else {
         TRY(put_field(s, &s->d->s.flags, 0));
         TRY(put_field(s, &s->d->s.nve_steps_done, 0LL));
         TRY(put_field(s, &s->d->s.max_steps, (long long)iters + 1));
     }
+    TRY(mixed_refresh(s));
     std::vector<cudaEvent_t> ev(4 * (size_t)iters);
     for (auto &e : ev) CK(cudaEventCreate(&e));
     int rc = DPG_OK;
@@ -1146,8 +1278,7 @@ extern "C" int dpg_profile_loop(dpg_handle s, int kind, int iters, double dt, do
         cudaEventRecord(ev[4 * i + 1], s->stream);
         rc = enqueue_rebuild(s);
         cudaEventRecord(ev[4 * i + 2], s->stream);
-        if (kind == 0) k_fire_force<<<G, s->tpb, 0, s->stream>>>(s->d, 0);
-        else k_nve_second<<<G, s->tpb, 0, s->stream>>>(s->d, 0.5 * dt);
+        if (rc == DPG_OK) rc = (kind == 0) ? launch_fire_force(s, 0) : launch_nve_second(s, 0.5 * dt);
         cudaEventRecord(ev[4 * i + 3], s->stream);
     }
     cudaError_t e = cudaStreamSynchronize(s->stream);

@@ -14,6 +14,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <cmath>
+
 namespace dpg {
 
 constexpr int kTPB = 256;      // threads per block for per-particle kernels
@@ -38,6 +40,12 @@ struct DevParams {
     double cell_size;
     double nthr2, cthr2;  // rebuild thresholds (squared)
     double inv_area;
+    // mixed form (precision DPG_MIXED): a grid of mg_m[d] cells of size
+    // mg_cs[d] per axis; each particle keeps an FP32 offset from the centre
+    // of its grid cell and the cell's wrapped coordinates (pk)
+    int mg_m[2];
+    double mg_cs[2], mg_inv[2];
+    float mg_cs_f[2];
 };
 
 struct DevView {
@@ -49,6 +57,7 @@ struct DevView {
     int *sidx_t;
     double2 *m1, *m2, *m1_t, *m2_t;  // Adam moments and their swap twins
     int *nbr;                        // neighbour list, column-major [cap][n]
+    float4 *pk;                      // mixed form: {offset x, offset y, radius, cell code}
 };
 
 struct DevState {
@@ -71,6 +80,12 @@ struct DevState {
     double last_avg_pe, pe_target, pe_diff_target, fmax_target, dof;
     long long iter, max_steps, result_step;
     long long nve_steps_done;
+    double damping;           // DampedNVE coefficient (0 in plain NVE)
+    // mixed form: FP64 pair arithmetic once fp64_now is set (FIRE refinement)
+    int fp64_now;
+    int pad2;
+    double switch_fmax, best_f2;
+    long long best_it;
     // loop guard: the WHILE body ends with k_loop_guard, which stops the loop
     // when a flag is raised or after guard_limit iterations, whatever else happens
     long long guard, guard_limit;
@@ -123,6 +138,68 @@ __device__ __forceinline__ int cell_coord(double p, double cs, int ncd) {
     long long idx = __double2ll_rd(p / cs);
     long long m = idx % ncd;
     return (int)(idx >= 0 ? m : (m + ncd) % ncd);
+}
+
+// ---- mixed form: FP32 offsets from grid-cell centres -------------------------
+// grid cell counts: cells of about 2 length units, at least 3 a side (fixed at
+// creation); the cell size follows the box
+inline void mixed_grid_init(DevParams &p) {
+    for (int d = 0; d < 2; d++) {
+        double m = std::floor(p.box[d] / 2.0);
+        p.mg_m[d] = (int)(m < 3.0 ? 3.0 : (m > 65535.0 ? 65535.0 : m));
+    }
+}
+
+inline void mixed_grid_update(DevParams &p) {
+    for (int d = 0; d < 2; d++) {
+        if (p.mg_m[d] <= 0) continue;
+        p.mg_cs[d] = p.box[d] / p.mg_m[d];
+        p.mg_inv[d] = p.mg_m[d] / p.box[d];
+        p.mg_cs_f[d] = (float)p.mg_cs[d];
+    }
+}
+
+__device__ __forceinline__ int wrap_cell(long long c, int m) {
+    long long r = c % m;
+    return (int)(r < 0 ? r + m : r);
+}
+
+// offset of x from the centre of its cell of the mixed grid, radius, and the
+// cell's wrapped coordinates packed as cx | cy << 16
+__device__ __forceinline__ float4 mixed_pack(const DevParams &p, double2 x, double r) {
+    double fx = floor(x.x * p.mg_inv[0]), fy = floor(x.y * p.mg_inv[1]);
+    int wx = wrap_cell((long long)fx, p.mg_m[0]), wy = wrap_cell((long long)fy, p.mg_m[1]);
+    float4 k;
+    k.x = (float)(x.x - (fx + 0.5) * p.mg_cs[0]);
+    k.y = (float)(x.y - (fy + 0.5) * p.mg_cs[1]);
+    k.z = (float)r;
+    k.w = __int_as_float(wx | (wy << 16));
+    return k;
+}
+
+// FP32 harmonic pair force on a from b: displacement (o_a - o_b) + dc * cell
+// size, with the periodic wrap done on the integer cell difference dc
+__device__ __forceinline__ float mixed_pair(const DevParams &p, float4 a, float4 b, float e_c,
+                                            float n_c, float &fx, float &fy) {
+    int ca = __float_as_int(a.w), cb = __float_as_int(b.w);
+    int dcx = (ca & 0xffff) - (cb & 0xffff), dcy = (ca >> 16) - (cb >> 16);
+    const int mx = p.mg_m[0], my = p.mg_m[1];
+    if (dcx > mx / 2) dcx -= mx; else if (dcx < -(mx / 2)) dcx += mx;
+    if (dcy > my / 2) dcy -= my; else if (dcy < -(my / 2)) dcy += my;
+    float dx = (a.x - b.x) + (float)dcx * p.mg_cs_f[0];
+    float dy = (a.y - b.y) + (float)dcy * p.mg_cs_f[1];
+    float rs = a.z + b.z;
+    float d2 = dx * dx + dy * dy;
+    fx = 0.f;
+    fy = 0.f;
+    if (d2 >= rs * rs) return 0.f;
+    float d = sqrtf(d2);
+    float ov = 1.0f - d / rs;
+    float ovp = n_c == 2.0f ? ov : powf(ov, n_c - 1.0f);
+    float fm = e_c * ovp / (rs * d);
+    fx = fm * dx;
+    fy = fm * dy;
+    return e_c * ov * ovp / (2.0f * n_c);
 }
 
 // ---- block reductions with a deterministic order ---------------------------
@@ -191,12 +268,26 @@ __device__ bool grid_reduce(double (&v)[K], const int (&ops)[K], DevSys *ds) {
     double a[K];
 #pragma unroll
     for (int k = 0; k < K; k++) a[k] = ops[k] ? -INFINITY : 0.0;
-    for (int b = threadIdx.x; b < G; b += blockDim.x)
+    // batches of 8 independent loads per thread (the latency of one L2 round
+    // trip per batch), combined in ascending block order
+    const int bd = blockDim.x;
+    for (int b0 = threadIdx.x; b0 < G; b0 += 8 * bd) {
+        double x[8][K];
 #pragma unroll
-        for (int k = 0; k < K; k++) {
-            double x = __ldcg(&part[k * G + b]);
-            a[k] = ops[k] ? fmax(a[k], x) : a[k] + x;
-        }
+        for (int u = 0; u < 8; u++)
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                int b = b0 + u * bd;
+                x[u][k] = b < G ? __ldcg(&part[k * G + b]) : (ops[k] ? -INFINITY : 0.0);
+            }
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                if (b0 + u * bd >= G) continue;
+                a[k] = ops[k] ? fmax(a[k], x[u][k]) : a[k] + x[u][k];
+            }
+    }
     block_reduce<K>(a, ops, sm);
     if (threadIdx.x == 0) {
         ds->s.ticket = 0;

@@ -11,14 +11,15 @@
 //
 // Precision.  Each system carries prec = 0 (mixed) or 1 (FP64):
 //  - mixed: positions are FP64; for the pair loop each particle also keeps an
-//    FP32 offset from the origin of its cell (cell size < 4 units, so the
-//    offset carries ~1e-7 absolute precision) and its cell coordinates; a pair
+//    FP32 offset from the centre of its cell (|offset| < 1.3 units, so the
+//    offset carries ~6e-8 absolute precision) and its cell coordinates; a pair
 //    displacement is (o_i - o_j) + dc * cell_size in FP32 with the periodic
 //    wrap done on the integer cell coordinates, the pair force is FP32, and
 //    the per-particle sums are FP64.  One 16-byte load per neighbour.
 //  - FP64: the reference's pair arithmetic (disk_pair).
-//  Mixed systems switch to FP64 when max|F| falls below switch_fmax (or FIRE
-//  stalls), for the final refinement.
+//  Mixed systems switch to FP64 when max|F| falls below switch_fmax, or when
+//  it stops falling (the FP32 noise floor, ~1e-7 x the contact stiffness),
+//  for the final refinement.
 //
 // Control.  Per-system FIRE state, convergence tests and the pressure-band
 // jamming state machine (scripts/runArthurJamWithFire.cpp) live on the device;
@@ -31,6 +32,9 @@ namespace dpg {
 namespace {
 
 constexpr int kEB = 128;  // threads per block (slot ranges are padded to this)
+// a mixed system whose max|F| has not dropped by 10% for this many iterations
+// has reached the FP32 noise floor and switches to FP64 pair arithmetic
+constexpr long long kStallIters = 2000;
 
 enum EPhase : int { kIdle = 0, kSetup = 1, kMinimize = 2 };
 enum EAction : int { kActNone = 0, kActDecompress = 1, kActCompress = 2, kActRevertScale = 3 };
@@ -49,6 +53,9 @@ struct ESys {
     long long ngood, nbad;
     // results of the last force pass
     double pe, power, fmax2, virial, contacts, max_d2;
+    // mixed phase: lowest max|F|^2 so far and the iteration it was reached
+    double best_f2;
+    long long best_it;
     // jamming (scripts/runArthurJamWithFire.cpp:36-106)
     int jam_stage;           // 0 decompressing, 1 compressing
     int jam_status;          // 0 final state, 1 length tolerance, 2 out of steps, -1 running
@@ -86,37 +93,26 @@ struct EDev {
     int *cell_cnt, *cell_start, *cell_cur, *cell_items;
     double *part;            // [nblocks][8] block partials
     int n_flagged, max_count, overflow, active;
+    int n_pending;           // systems with a transition queued by the last force pass
     unsigned ticket;
     long long guard, guard_limit;
-    unsigned long long h_loop, h_rb;
+    unsigned long long h_loop, h_rb, h_tr;
 };
 
 __device__ __forceinline__ int code_of(int cx, int cy) { return cx | (cy << 16); }
 __device__ __forceinline__ int code_x(int c) { return c & 0xffff; }
 __device__ __forceinline__ int code_y(int c) { return c >> 16; }
 
-// Kahan-compensated sum of the system's block partials k (fixed order)
-__device__ double sys_sum(const EDev *e, const ESys &s, int k) {
-    double sum = 0.0, c = 0.0;
-    for (int b = 0; b < s.nblk; b++) {
-        double y = __ldcg(&e->part[(size_t)(s.blk0 + b) * 8 + k]) - c;
-        double t = sum + y;
-        c = (t - sum) - y;
-        sum = t;
-    }
-    return sum;
-}
-
-__device__ double sys_max(const EDev *e, const ESys &s, int k) {
-    double m = 0.0;
-    for (int b = 0; b < s.nblk; b++) m = fmax(m, __ldcg(&e->part[(size_t)(s.blk0 + b) * 8 + k]));
-    return m;
-}
-
-// Publish a block's partials; returns true (on thread 0) in the last block of
-// the system to arrive.  Every thread of the block must call it.
+// Per-system reduction by "last block of the system done": every block of the
+// system publishes its block partials; the last block to arrive reduces them
+// with all of its threads (thread t takes blocks t, t + blockDim, ... with a
+// compensated (Kahan) running sum, then a fixed-order tree over the threads),
+// so the result is deterministic and costs one L2 round trip, not one per
+// block.  Returns true on thread 0 of that block, with the totals in v
+// (ops[k]: 0 = sum, 1 = max of non-negative values).  Every thread of every
+// block must call it.
 template <int K>
-__device__ bool sys_publish(EDev *e, ESys &s, double (&v)[K], const int (&ops)[K], unsigned *ticket) {
+__device__ bool sys_reduce(EDev *e, ESys &s, double (&v)[K], const int (&ops)[K], unsigned *ticket) {
     __shared__ double sm[32 * K];
     __shared__ int last;
     block_reduce<K>(v, ops, sm);
@@ -129,8 +125,33 @@ __device__ bool sys_publish(EDev *e, ESys &s, double (&v)[K], const int (&ops)[K
         if (last) *ticket = 0;
     }
     __syncthreads();
-    if (last) __threadfence();
-    return last && threadIdx.x == 0;
+    if (!last) return false;
+    __threadfence();
+    double a[K], c[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) { a[k] = 0.0; c[k] = 0.0; }
+    for (int b = threadIdx.x; b < s.nblk; b += blockDim.x) {
+        const double *pp = &e->part[(size_t)(s.blk0 + b) * 8];
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            double x = __ldcg(&pp[k]);
+            if (ops[k]) {
+                a[k] = fmax(a[k], x);
+            } else {
+                double y = x - c[k];
+                double t = a[k] + y;
+                c[k] = (t - a[k]) - y;
+                a[k] = t;
+            }
+        }
+    }
+    block_reduce<K>(a, ops, sm);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < K; k++) v[k] = a[k];
+        return true;
+    }
+    return false;
 }
 
 __device__ __forceinline__ bool grid_last(EDev *e) {
@@ -200,15 +221,15 @@ __global__ void __launch_bounds__(kEB) e_move(EDev *e) {
         if (s.prec == 0) {  // FP32 offset from the particle's (unwrapped) cell origin
             int2 cu = e->cellu[i];
             float4 k = e->pk[i];
-            k.x = (float)(x.x - cu.x * s.cs);
-            k.y = (float)(x.y - cu.y * s.cs);
+            k.x = (float)(x.x - (cu.x + 0.5) * s.cs);
+            k.y = (float)(x.y - (cu.y + 0.5) * s.cs);
             e->pk[i] = k;
         }
     }
     const int ops[1] = {1};
-    if (sys_publish<1>(e, s, v, ops, &s.ticket_a)) {
+    if (sys_reduce<1>(e, s, v, ops, &s.ticket_a)) {
         if (live) {
-            s.max_d2 = sys_max(e, s, 0);
+            s.max_d2 = v[0];
             if (s.max_d2 > e->p.half_skin2) s.rebuild = 1;
         }
         if (s.rebuild && s.phase != kIdle) atomicAdd(&e->n_flagged, 1);
@@ -346,17 +367,17 @@ __global__ void __launch_bounds__(kEB) e_nlist(EDev *e) {
         e->pos_ref[i] = xi;
         int2 cu = e->cellu[i];
         float4 k;
-        k.x = (float)(xi.x - cu.x * s.cs);
-        k.y = (float)(xi.y - cu.y * s.cs);
+        k.x = (float)(xi.x - (cu.x + 0.5) * s.cs);
+        k.y = (float)(xi.y - (cu.y + 0.5) * s.cs);
         k.z = (float)e->rad[i];
         k.w = __int_as_float(c);
         e->pk[i] = k;
     }
     double v[1] = {(double)cnt};
     const int ops[1] = {1};
-    if (sys_publish<1>(e, s, v, ops, &s.ticket_b)) {
+    if (sys_reduce<1>(e, s, v, ops, &s.ticket_b)) {
         if (on) {
-            int mx = (int)sys_max(e, s, 0);
+            int mx = (int)v[0];
             atomicMax(&e->max_count, mx);
             if (mx > e->p.cap) atomicExch(&e->overflow, 1);
             s.rebuild = 0;
@@ -392,78 +413,17 @@ __device__ __forceinline__ void pair_f32(const float4 a, const float4 b, int ncd
     contact = 1;
 }
 
-__global__ void __launch_bounds__(kEB) e_force(EDev *e) {
-    if (e->overflow) return;  // lists truncated: the host grows them and reruns this pass
-    const int sid = e->blk_sys[blockIdx.x];
-    ESys &s = e->sys[sid];
+// Per-system epilogue of a force pass (thread 0 of the system's last block):
+// minimizeFire tests, the mixed-precision switch, the next FIRE decision and
+// the jamming state machine (scripts/runArthurJamWithFire.cpp:36-106).
+__device__ void e_force_epilogue(EDev *e, ESys &s, const double (&v)[5], bool setup) {
     const EParams &p = e->p;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool live = s.phase != kIdle;
-    const bool setup = s.phase == kSetup;
-    // partials: 0 PE, 1 power, 2 max|F|^2, 3 virial, 4 contacts
-    double v[5] = {0, 0, 0, 0, 0};
-    if (live && i < s.off + s.n) {
-        const int T = p.T;
-        int cnt = min(e->cnt[i], p.cap);
-        double ax = 0.0, ay = 0.0, en = 0.0, wv = 0.0, nc = 0.0;
-        if (s.prec == 0) {
-            const float4 a = e->pk[i];
-            const float ecf = (float)p.e_c;
-            for (int k = 0; k < cnt; k++) {
-                int j = __ldg(&e->nbr[(size_t)k * T + i]);
-                float4 b = e->pk[j];
-                float fx, fy, ef, wf;
-                int ct;
-                pair_f32(a, b, s.ncd, s.cs_f, ecf, fx, fy, ef, wf, ct);
-                ax += (double)fx;
-                ay += (double)fy;
-                en += (double)ef;
-                wv += (double)wf;
-                nc += ct;
-            }
-        } else {
-            const double2 xi = e->pos[i];
-            const double ri = e->rad[i];
-            for (int k = 0; k < cnt; k++) {
-                int j = __ldg(&e->nbr[(size_t)k * T + i]);
-                double2 xj = e->pos[j];
-                double fx, fy;
-                double ee = disk_pair(xi.x, xi.y, ri, xj.x, xj.y, e->rad[j], s.L, s.L, p.e_c, p.n_c, fx, fy);
-                ax += fx;
-                ay += fy;
-                en += ee;
-                if (fx != 0.0 || fy != 0.0) {
-                    double dx = pbc_dist(xi.x, xj.x, s.L), dy = pbc_dist(xi.y, xj.y, s.L);
-                    wv += fx * dx + fy * dy;
-                    nc += 1.0;
-                }
-            }
-        }
-        double2 f = make_double2(ax, ay);
-        e->frc[i] = f;
-        e->pe[i] = en;
-        double2 u = e->vel[i];
-        if (!setup) {
-            double dtm = (s.dt / 2.0) / e->mass[i];
-            u.x = u.x + f.x * dtm;
-            u.y = u.y + f.y * dtm;
-            e->vel[i] = u;
-        }
-        v[0] = en;
-        v[1] = f.x * u.x + f.y * u.y;
-        v[2] = f.x * f.x + f.y * f.y;
-        v[3] = wv;
-        v[4] = nc;
-    }
-    const int ops[5] = {0, 0, 1, 0, 0};
-    if (!sys_publish<5>(e, s, v, ops, &s.ticket_a)) return;
-    if (!live) return;
     // ---- per-system epilogue: minimizeFire tests and the next FIRE decision ----
-    s.pe = sys_sum(e, s, 0);
-    s.power = sys_sum(e, s, 1);
-    s.fmax2 = sys_max(e, s, 2);
-    s.virial = sys_sum(e, s, 3);
-    s.contacts = sys_sum(e, s, 4);
+    s.pe = v[0];
+    s.power = v[1];
+    s.fmax2 = v[2];
+    s.virial = v[3];
+    s.contacts = v[4];
     double avg = s.pe / (double)s.n;
     s.fire_total++;
     bool finished = false;
@@ -471,13 +431,20 @@ __global__ void __launch_bounds__(kEB) e_force(EDev *e) {
         s.last_avg_pe = avg;
         s.phase = kMinimize;
         s.iter = 0;
+        s.best_f2 = s.fmax2;
+        s.best_it = 0;
         e_fire_decide(p, s, s.power);
         return;
     }
     double fmax = sqrt(s.fmax2);
-    // mixed systems hand over to FP64 pair arithmetic for the final refinement
-    if (s.prec == 0 && (fmax <= p.switch_fmax || s.nbad > 5)) {
-        s.prec = 1;
+    // mixed systems hand over to FP64 pair arithmetic for the final refinement:
+    // at switch_fmax, when FIRE keeps going uphill, or when max|F| stalls
+    if (s.prec == 0) {
+        if (s.fmax2 < 0.81 * s.best_f2) {
+            s.best_f2 = s.fmax2;
+            s.best_it = s.iter;
+        }
+        if (fmax <= p.switch_fmax || s.nbad > 5 || s.iter - s.best_it > kStallIters) s.prec = 1;
     }
     double diff = fabs(avg / s.last_avg_pe - 1);
     s.last_avg_pe = avg;
@@ -546,6 +513,89 @@ __global__ void __launch_bounds__(kEB) e_force(EDev *e) {
     s.scale = Lnew / L_prior;
 }
 
+__global__ void __launch_bounds__(kEB) e_force(EDev *e) {
+    if (e->overflow) return;  // lists truncated: the host grows them and reruns this pass
+    const int sid = e->blk_sys[blockIdx.x];
+    ESys &s = e->sys[sid];
+    const EParams &p = e->p;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool live = s.phase != kIdle;
+    const bool setup = s.phase == kSetup;
+    // partials: 0 PE, 1 power, 2 max|F|^2, 3 virial, 4 contacts
+    double v[5] = {0, 0, 0, 0, 0};
+    if (live && i < s.off + s.n) {
+        const int T = p.T;
+        int cnt = min(e->cnt[i], p.cap);
+        double ax = 0.0, ay = 0.0, en = 0.0, wv = 0.0, nc = 0.0;
+        if (s.prec == 0) {
+            // FP32 pair terms summed in FP32 over runs of 8 neighbours, FP64 across runs
+            const float4 a = e->pk[i];
+            const float ecf = (float)p.e_c;
+            int ncount = 0;
+            for (int k0 = 0; k0 < cnt; k0 += 8) {
+                float sx = 0.f, sy = 0.f, se = 0.f, sw = 0.f;
+                const int k1 = min(cnt, k0 + 8);
+                for (int k = k0; k < k1; k++) {
+                    int j = __ldg(&e->nbr[(size_t)k * T + i]);
+                    float4 b = e->pk[j];
+                    float fx, fy, ef, wf;
+                    int ct;
+                    pair_f32(a, b, s.ncd, s.cs_f, ecf, fx, fy, ef, wf, ct);
+                    sx += fx;
+                    sy += fy;
+                    se += ef;
+                    sw += wf;
+                    ncount += ct;
+                }
+                ax += (double)sx;
+                ay += (double)sy;
+                en += (double)se;
+                wv += (double)sw;
+            }
+            nc = (double)ncount;
+        } else {
+            const double2 xi = e->pos[i];
+            const double ri = e->rad[i];
+            for (int k = 0; k < cnt; k++) {
+                int j = __ldg(&e->nbr[(size_t)k * T + i]);
+                double2 xj = e->pos[j];
+                double fx, fy;
+                double ee = disk_pair(xi.x, xi.y, ri, xj.x, xj.y, e->rad[j], s.L, s.L, p.e_c, p.n_c, fx, fy);
+                ax += fx;
+                ay += fy;
+                en += ee;
+                if (fx != 0.0 || fy != 0.0) {
+                    double dx = pbc_dist(xi.x, xj.x, s.L), dy = pbc_dist(xi.y, xj.y, s.L);
+                    wv += fx * dx + fy * dy;
+                    nc += 1.0;
+                }
+            }
+        }
+        double2 f = make_double2(ax, ay);
+        e->frc[i] = f;
+        e->pe[i] = en;
+        double2 u = e->vel[i];
+        if (!setup) {
+            double dtm = (s.dt / 2.0) / e->mass[i];
+            u.x = u.x + f.x * dtm;
+            u.y = u.y + f.y * dtm;
+            e->vel[i] = u;
+        }
+        v[0] = en;
+        v[1] = f.x * u.x + f.y * u.y;
+        v[2] = f.x * f.x + f.y * f.y;
+        v[3] = wv;
+        v[4] = nc;
+    }
+    const int ops[5] = {0, 0, 1, 0, 0};
+    if (sys_reduce<5>(e, s, v, ops, &s.ticket_a) && live) {
+        e_force_epilogue(e, s, v, setup);
+        if (s.pending != kActNone) atomicAdd(&e->n_pending, 1);
+    }
+    // the transition pass (graph IF node) runs only when some system asked for one
+    if (grid_last(e) && e->h_tr) cudaGraphSetConditional(e->h_tr, e->n_pending > 0 ? 1u : 0u);
+}
+
 // ---- transitions between minimisations (save / restore / scale, FIRE reset) ----
 __global__ void __launch_bounds__(kEB) e_transition(EDev *e) {
     if (e->overflow) return;
@@ -565,7 +615,7 @@ __global__ void __launch_bounds__(kEB) e_transition(EDev *e) {
     }
     double v[1] = {0.0};
     const int ops[1] = {0};
-    if (sys_publish<1>(e, s, v, ops, &s.ticket_b) && act != kActNone) {
+    if (sys_reduce<1>(e, s, v, ops, &s.ticket_b) && act != kActNone) {
         double L0 = act == kActRevertScale ? s.L_last : s.L;
         s.L = L0 * s.scale;
         s.cs = s.L / s.ncd;
@@ -583,6 +633,7 @@ __global__ void __launch_bounds__(kEB) e_transition(EDev *e) {
         s.iter = 0;
         s.prec = (e->p.switch_fmax > 0 && s.ncd >= 3) ? 0 : 1;
     }
+    if (grid_last(e)) e->n_pending = 0;
 }
 
 // WHILE-body guard: continue while any system is active and the budget lasts

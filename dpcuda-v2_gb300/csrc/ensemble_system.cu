@@ -36,7 +36,7 @@ struct dpg_ensemble_system {
     double *xfer = nullptr;
     size_t n_total = 0;
     cudaGraphExec_t exec = nullptr;
-    cudaGraphConditionalHandle h_loop = 0, h_rb = 0;
+    cudaGraphConditionalHandle h_loop = 0, h_rb = 0, h_tr = 0;
     bool have_state = false;
     int mode = 2;
 };
@@ -151,7 +151,7 @@ extern "C" int dpg_ensemble_create(const dpg_ensemble_params *p, const int64_t *
     h.p.cutoff2 = p->cutoff * p->cutoff;
     h.p.cutoff2_f = (float)h.p.cutoff2;
     h.p.half_skin2 = (p->skin / 2) * (p->skin / 2);
-    h.p.switch_fmax = p->precision == DPG_MIXED ? (p->switch_fmax > 0 ? p->switch_fmax : 1e-7) : 0.0;
+    h.p.switch_fmax = p->precision == DPG_MIXED ? (p->switch_fmax > 0 ? p->switch_fmax : 1e-6) : 0.0;
     std::vector<int> bs(s->nblocks);
     for (int k = 0; k < s->S; k++)
         for (int b = 0; b < s->sys[k].nblk; b++) bs[s->sys[k].blk0 + b] = k;
@@ -235,6 +235,7 @@ static int build_graph(ES *s) {
     if (err == cudaSuccess) err = cudaGraphAddNode(&wnode, g, nullptr, nullptr, 0, &wp);
     cudaGraph_t body = err == cudaSuccess ? wp.conditional.phGraph_out[0] : nullptr;
     if (err == cudaSuccess) err = cudaGraphConditionalHandleCreate(&s->h_rb, body, 0, 0);
+    if (err == cudaSuccess) err = cudaGraphConditionalHandleCreate(&s->h_tr, body, 0, 0);
     EDev *dp = s->d;
     void *a[] = {&dp};
     cudaGraphNode_t last = nullptr;
@@ -255,8 +256,18 @@ static int build_graph(ES *s) {
         prev = addk(ib, prev, (void *)e_cell_sort, (s->total_cells + 255) / 256, 256, a, &err);
         prev = addk(ib, prev, (void *)e_nlist, s->nblocks, kEB, a, &err);
         last = addk(body, inode, (void *)e_force, s->nblocks, kEB, a, &err);
-        last = addk(body, last, (void *)e_transition, s->nblocks, kEB, a, &err);
-        last = addk(body, last, (void *)e_guard, 1, 1, a, &err);
+        // IF(any system queued a transition) { e_transition }
+        cudaGraphNodeParams tp = {};
+        tp.type = cudaGraphNodeTypeConditional;
+        tp.conditional.handle = s->h_tr;
+        tp.conditional.type = cudaGraphCondTypeIf;
+        tp.conditional.size = 1;
+        cudaGraphNode_t tnode = nullptr;
+        if (err == cudaSuccess) err = cudaGraphAddNode(&tnode, body, &last, nullptr, 1, &tp);
+        if (err == cudaSuccess) {
+            addk(tp.conditional.phGraph_out[0], nullptr, (void *)e_transition, s->nblocks, kEB, a, &err);
+            last = addk(body, tnode, (void *)e_guard, 1, 1, a, &err);
+        }
     }
     if (err == cudaSuccess) err = cudaGraphInstantiate(&s->exec, g, 0);
     cudaGraphDestroy(g);
@@ -301,9 +312,11 @@ static int run(ES *s, long long guard_limit) {
         if (s->mode == 2 && build_graph(s) == DPG_OK) {
             TRY(put(s, &s->d->h_loop, (unsigned long long)s->h_loop));
             TRY(put(s, &s->d->h_rb, (unsigned long long)s->h_rb));
+            TRY(put(s, &s->d->h_tr, (unsigned long long)s->h_tr));
             CK(cudaGraphLaunch(s->exec, s->stream));
             TRY(put(s, &s->d->h_loop, 0ULL));
             TRY(put(s, &s->d->h_rb, 0ULL));
+            TRY(put(s, &s->d->h_tr, 0ULL));
             ran = true;
         }
         if (!ran) {
@@ -342,7 +355,8 @@ static int run(ES *s, long long guard_limit) {
     return set_err(DPG_ERR_STATE, "ensemble loop did not finish");
 }
 
-static int start(ES *s, const dpg_fire_params *fp, int jam, const dpg_jam_params *jp) {
+// per-system FIRE / jamming state reset and parameters upload (no launches)
+static int prepare(ES *s, const dpg_fire_params *fp, int jam, const dpg_jam_params *jp) {
     if (!s->have_state) return set_err(DPG_ERR_STATE, "set the state first");
     TRY(pull_sys(s));
     EParams &p = s->h.p;
@@ -363,15 +377,22 @@ static int start(ES *s, const dpg_fire_params *fp, int jam, const dpg_jam_params
         y.jam_stage = 0; y.jam_status = -1; y.jam_step = 0;
         y.L_low = y.L_high = y.L_last = -1; y.L_saved = -1; y.scale = 1.0; y.rebuilds = 0;
         y.ticket_a = y.ticket_b = 0;
+        y.best_f2 = INFINITY; y.best_it = 0;
     }
     CK(cudaMemcpyAsync(s->d_sys, s->sys.data(), sizeof(ESys) * s->S, cudaMemcpyHostToDevice, s->stream));
     CK(cudaMemcpyAsync(&s->d->p, &p, sizeof(EParams), cudaMemcpyHostToDevice, s->stream));
     TRY(put(s, &s->d->active, s->S));
     TRY(put(s, &s->d->n_flagged, 0));
+    TRY(put(s, &s->d->n_pending, 0));
     TRY(put(s, &s->d->overflow, 0));
     TRY(put(s, &s->d->ticket, 0u));
     // velocities start at zero (minimizeFire's setVelocitiesToZero)
     CK(cudaMemsetAsync(s->h.vel, 0, 16 * (size_t)s->T, s->stream));
+    return DPG_OK;
+}
+
+static int start(ES *s, const dpg_fire_params *fp, int jam, const dpg_jam_params *jp) {
+    TRY(prepare(s, fp, jam, jp));
     long long budget = jam ? (long long)4e9 : fp->max_steps * 2 + 16;
     TRY(run(s, budget));
     TRY(pull_sys(s));
@@ -409,5 +430,77 @@ extern "C" int dpg_ensemble_jam(dpg_ensemble s, const dpg_jam_params *p, dpg_ens
     if (!s || !p) return set_err(DPG_ERR_ARG, "null argument");
     TRY(start(s, &p->fire, 1, p));
     fill_results(s, r);
+    return DPG_OK;
+}
+
+extern "C" int dpg_ensemble_compute_forces(dpg_ensemble s, int precision, dpg_ensemble_result *r) {
+    if (!s) return set_err(DPG_ERR_ARG, "null handle");
+    if (precision != DPG_FP64 && precision != DPG_MIXED) return set_err(DPG_ERR_ARG, "bad precision");
+    const dpg_fire_params fp = {0.1, 1e-2, 0.0, 0.0, 1, 0.0};
+    for (int attempt = 0; attempt < 8; attempt++) {
+        TRY(prepare(s, &fp, 0, nullptr));
+        for (auto &y : s->sys) y.prec = (precision == DPG_MIXED && y.ncd >= 3) ? 0 : 1;
+        CK(cudaMemcpyAsync(s->d_sys, s->sys.data(), sizeof(ESys) * s->S, cudaMemcpyHostToDevice, s->stream));
+        TRY(put(s, &s->d->n_flagged, 1));
+        TRY(enqueue_rebuild(s));
+        LAUNCH(e_force, s->nblocks, kEB, s->d);
+        EDev cur;
+        TRY(pull_dev(s, &cur));
+        if (!cur.overflow) {
+            TRY(pull_sys(s));
+            fill_results(s, r);
+            return DPG_OK;
+        }
+        int ncap = pow2ceil(cur.max_count);
+        if ((size_t)ncap * s->T > ((size_t)1 << 31)) return set_err(DPG_ERR_OVERFLOW, "ensemble neighbour list too large");
+        TRY(alloc_nbr(s, ncap));
+        if (s->exec) { cudaGraphExecDestroy(s->exec); s->exec = nullptr; }
+        TRY(put(s, &s->d->nbr, s->h.nbr));
+        TRY(put(s, &s->d->p.cap, ncap));
+        TRY(put(s, &s->d->overflow, 0));
+    }
+    return set_err(DPG_ERR_OVERFLOW, "ensemble neighbour list did not settle");
+}
+
+extern "C" int dpg_ensemble_profile_loop(dpg_ensemble s, const dpg_fire_params *p, int iters,
+                                         double *avg_us, int64_t *counts) {
+    if (!s || !p || !avg_us || iters <= 0) return set_err(DPG_ERR_ARG, "null argument or iters <= 0");
+    TRY(prepare(s, p, 0, nullptr));
+    std::vector<cudaEvent_t> ev(5 * (size_t)iters);
+    for (auto &e : ev) CK(cudaEventCreate(&e));
+    int rc = DPG_OK;
+    for (int i = 0; i < iters && rc == DPG_OK; i++) {
+        cudaEventRecord(ev[5 * i + 0], s->stream);
+        LAUNCH(e_move, s->nblocks, kEB, s->d);
+        cudaEventRecord(ev[5 * i + 1], s->stream);
+        rc = enqueue_rebuild(s);
+        cudaEventRecord(ev[5 * i + 2], s->stream);
+        LAUNCH(e_force, s->nblocks, kEB, s->d);
+        cudaEventRecord(ev[5 * i + 3], s->stream);
+        LAUNCH(e_transition, s->nblocks, kEB, s->d);
+        cudaEventRecord(ev[5 * i + 4], s->stream);
+    }
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    double acc[4] = {0, 0, 0, 0};
+    if (rc == DPG_OK && e == cudaSuccess) {
+        for (int i = 0; i < iters; i++)
+            for (int k = 0; k < 4; k++) {
+                float ms = 0;
+                cudaEventElapsedTime(&ms, ev[5 * i + k], ev[5 * i + k + 1]);
+                acc[k] += ms * 1e3;
+            }
+    }
+    for (auto &x : ev) cudaEventDestroy(x);
+    if (rc != DPG_OK) return rc;
+    if (e != cudaSuccess) return set_err(DPG_ERR_CUDA, "profile: %s", cudaGetErrorString(e));
+    for (int k = 0; k < 4; k++) avg_us[k] = acc[k] / iters;
+    TRY(pull_sys(s));
+    if (counts) {
+        long long rb = 0, fire = 0;
+        for (auto &y : s->sys) { rb += y.rebuilds; fire += y.fire_total; }
+        counts[0] = iters;
+        counts[1] = rb;
+        counts[2] = fire;
+    }
     return DPG_OK;
 }

@@ -13,7 +13,7 @@ There is no CPU fallback: importing works anywhere, but creating a system
 needs the CUDA library and a GPU, and fails loudly otherwise.
 """
 from .lib import DpgError, load_library, library_path  # noqa: F401
-from .disk import (Disk, NVE, Fire, Adam, minimizeFire, minimizeAdam, jamPressure, jamPhi,  # noqa: F401
-                   NEIGH_CELL, NEIGH_VERLET, NEIGH_ALL, FP64, MIXED)
+from .disk import (Disk, NVE, DampedNVE, GradDesc, Fire, Adam, minimizeFire, minimizeAdam,  # noqa: F401
+                   jamPressure, jamPhi, NEIGH_CELL, NEIGH_VERLET, NEIGH_ALL, FP64, MIXED)
 from .bumpy import RigidBumpy  # noqa: F401
 from .ensemble import Ensemble  # noqa: F401

@@ -24,13 +24,15 @@ class RigidBumpy:
     BODY_KEYS = ("x", "y", "th", "vx", "vy", "w", "fx", "fy", "tq", "pe", "I")
 
     def __init__(self, n_bodies, n_vertices, box_size, e_c, n_c, vertex_radius,
-                 segment_length_per_vertex_diameter, rotation=True, stream=None):
+                 segment_length_per_vertex_diameter, rotation=True, stream=None, precision=0):
+        """precision 0 = DPG_FP64 (the reference arithmetic), 1 = DPG_MIXED (FP32
+        vertex pairs, FP64 torques and body sums, FP64 refinement in FIRE)."""
         self.lib = load_library()
         self.nb, self.nv = int(n_bodies), int(n_vertices)
         bx, by = (box_size, box_size) if np.isscalar(box_size) else box_size
         prm = BumpyParams(self.nb, self.nv, float(bx), float(by), float(e_c), float(n_c),
                           float(vertex_radius), float(segment_length_per_vertex_diameter),
-                          int(bool(rotation)), 0)
+                          int(bool(rotation)), int(precision))
         h = C.c_void_p()
         check(self.lib.dpg_bumpy_create(C.byref(prm), C.c_void_p(stream) if stream else None,
                                         C.byref(h)))
@@ -164,6 +166,9 @@ class RigidBumpy:
                                                C.byref(res)))
         return dict(steps=res.steps, stopped=res.stopped, converged=res.converged,
                     avg_pe=res.avg_pe, max_force=res.max_force)
+
+    def setMixedSwitch(self, switch_fmax):
+        check(self.lib.dpg_bumpy_set_mixed_switch(self.h, float(switch_fmax)))
 
     def scaleBox(self, factor):
         check(self.lib.dpg_bumpy_scale_box(self.h, float(factor)))

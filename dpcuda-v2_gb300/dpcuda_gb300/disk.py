@@ -256,6 +256,39 @@ class Disk:
     def nveSteps(self, dt, n_steps):
         check(self.lib.dpg_nve_steps(self.h, float(dt), int(n_steps)))
 
+    def setMixedSwitch(self, switch_fmax):
+        """DPG_MIXED systems: max|F| below which FIRE continues in FP64."""
+        check(self.lib.dpg_set_mixed_switch(self.h, float(switch_fmax)))
+
+    def writeState(self, directory, step=-1):
+        """State files in the reference's layout (positions.dat, radii.dat, ...)."""
+        check(self.lib.dpg_write_state(self.h, str(directory).encode(), int(step)))
+
+    def readState(self, directory):
+        """Load positions, velocities, radii, masses and box from a state directory."""
+        check(self.lib.dpg_read_state(self.h, str(directory).encode()))
+
+    @staticmethod
+    def stateCount(directory):
+        """Number of particles stored in a state directory."""
+        lib = load_library()
+        n = C.c_int64()
+        check(lib.dpg_state_count(str(directory).encode(), C.byref(n)))
+        return n.value
+
+    def calculateDampedForces(self, damping_coefficient):
+        check(self.lib.dpg_damped_forces(self.h, float(damping_coefficient)))
+
+    def dampedNveSteps(self, dt, damping_coefficient, n_steps):
+        check(self.lib.dpg_damped_nve_steps(self.h, float(dt), float(damping_coefficient),
+                                            int(n_steps)))
+
+    def updatePositionsGradDesc(self, alpha):
+        check(self.lib.dpg_grad_desc_step(self.h, float(alpha)))
+
+    def gradDescSteps(self, alpha, n_steps):
+        check(self.lib.dpg_grad_desc_steps(self.h, float(alpha), int(n_steps)))
+
 
 class NVE:
     """NVE velocity Verlet (src/integrator/nve.cu:15-25)."""
@@ -268,6 +301,32 @@ class NVE:
 
     def run(self, n_steps):
         self.particle.nveSteps(self.dt, n_steps)
+
+
+class DampedNVE:
+    """Velocity Verlet with F -= damping v (src/integrator/damped_nve.cu:15-27)."""
+
+    def __init__(self, particle: Disk, dt: float, damping_coefficient: float):
+        self.particle, self.dt, self.damping = particle, float(dt), float(damping_coefficient)
+
+    def step(self):
+        self.particle.dampedNveSteps(self.dt, self.damping, 1)
+
+    def run(self, n_steps):
+        self.particle.dampedNveSteps(self.dt, self.damping, n_steps)
+
+
+class GradDesc:
+    """Gradient descent x += alpha F (src/integrator/grad_desc.cu:11-17)."""
+
+    def __init__(self, particle: Disk, alpha: float):
+        self.particle, self.alpha = particle, float(alpha)
+
+    def step(self):
+        self.particle.gradDescSteps(self.alpha, 1)
+
+    def run(self, n_steps):
+        self.particle.gradDescSteps(self.alpha, n_steps)
 
 
 class Fire:

@@ -17,7 +17,7 @@ FP64, MIXED = 0, 1
 
 class Ensemble:
     def __init__(self, n_particles, boxes, cutoff, skin, e_c=1.0, n_c=2.0, precision=MIXED,
-                 switch_fmax=1e-7, stream=None):
+                 switch_fmax=1e-6, stream=None):
         self.lib = load_library()
         self.n = np.ascontiguousarray(n_particles, dtype=np.int64)
         self.boxes = np.ascontiguousarray(boxes, dtype=np.float64)
@@ -67,6 +67,13 @@ class Ensemble:
                             converged=r.converged))
         return out
 
+    def calculateForces(self, precision=FP64):
+        """One force pass on every system at the current positions; forces via
+        getState(), per-system energies / pressure / contacts returned."""
+        res = (EnsembleResult * self.S)()
+        check(self.lib.dpg_ensemble_compute_forces(self.h, int(precision), res))
+        return self._results(res)
+
     def minimizeFire(self, alpha_init=0.1, dt=1e-2, avg_pe_target=1e-16, avg_pe_diff_target=1e-16,
                      num_steps=100000, fmax_target=0.0):
         prm = FireParams(float(alpha_init), float(dt), float(avg_pe_target),
@@ -87,3 +94,13 @@ class Ensemble:
         res = (EnsembleResult * self.S)()
         check(self.lib.dpg_ensemble_jam(self.h, C.byref(prm), res))
         return self._results(res)
+
+    def profileLoop(self, iters, alpha_init=0.1, dt=1e-2, fmax_target=1e-13):
+        """Mean device time per iteration of each phase of the FIRE loop (us), as
+        plain launches.  Leaves the systems mid-minimisation."""
+        prm = FireParams(float(alpha_init), float(dt), 0.0, 0.0, 10**9, float(fmax_target))
+        avg = (C.c_double * 4)()
+        cnt = (C.c_int64 * 3)()
+        check(self.lib.dpg_ensemble_profile_loop(self.h, C.byref(prm), int(iters), avg, cnt))
+        return {"move_us": avg[0], "rebuild_us": avg[1], "force_us": avg[2], "transition_us": avg[3],
+                "iters": cnt[0], "rebuilds": cnt[1], "force_passes": cnt[2]}

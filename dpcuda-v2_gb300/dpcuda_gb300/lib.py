@@ -115,6 +115,13 @@ SIGNATURES = {
     "dpg_kick": [VP, D],
     "dpg_drift": [VP, D],
     "dpg_nve_steps": [VP, D, I64],
+    "dpg_write_state": [VP, C.c_char_p, I64],
+    "dpg_read_state": [VP, C.c_char_p],
+    "dpg_state_count": [C.c_char_p, I64P],
+    "dpg_damped_forces": [VP, D],
+    "dpg_damped_nve_steps": [VP, D, D, I64],
+    "dpg_grad_desc_step": [VP, D],
+    "dpg_grad_desc_steps": [VP, D, I64],
     "dpg_power_fire": [VP, DP],
     "dpg_mix": [VP, D],
     "dpg_zero_velocities": [VP],
@@ -122,6 +129,7 @@ SIGNATURES = {
     "dpg_fire_step": [VP, IP],
     "dpg_fire_get": [VP, DP, DP, I64P, I64P, IP],
     "dpg_fire_minimize": [VP, C.POINTER(FireParams), C.POINTER(FireResult)],
+    "dpg_set_mixed_switch": [VP, D],
     "dpg_adam_init": [VP],
     "dpg_adam_step": [VP, I64, D, D, D, D],
     "dpg_adam_minimize": [VP, D, D, D, D, D, D, I64, I64P],
@@ -141,6 +149,8 @@ SIGNATURES = {
     "dpg_ensemble_get_state": [VP, DP, DP, DP, DP],
     "dpg_ensemble_fire_minimize": [VP, C.POINTER(FireParams), C.POINTER(EnsembleResult)],
     "dpg_ensemble_jam": [VP, C.POINTER(JamParams), C.POINTER(EnsembleResult)],
+    "dpg_ensemble_profile_loop": [VP, C.POINTER(FireParams), I32, DP, I64P],
+    "dpg_ensemble_compute_forces": [VP, I32, C.POINTER(EnsembleResult)],
     "dpg_bumpy_create": [C.POINTER(BumpyParams), VP, C.POINTER(VP)],
     "dpg_bumpy_destroy": [VP],
     "dpg_bumpy_set_bodies": [VP, DP, DP, DP, DP, DP, DP, DP, I32P],
@@ -163,6 +173,7 @@ SIGNATURES = {
     "dpg_bumpy_fire_init": [VP, D, D],
     "dpg_bumpy_fire_step": [VP, IP],
     "dpg_bumpy_fire_minimize": [VP, C.POINTER(FireParams), D, C.POINTER(FireResult)],
+    "dpg_bumpy_set_mixed_switch": [VP, D],
     "dpg_bumpy_scale_box": [VP, D],
 }
 _RESTYPES = {"dpg_last_error": C.c_char_p}

@@ -174,6 +174,34 @@ int dpg_drift(dpg_handle h, double dt);
 /* n_steps of NVE::step (src/integrator/nve.cu:15-25), device-resident loop */
 int dpg_nve_steps(dpg_handle h, double dt, int64_t n_steps);
 
+/* ---- state files in the reference's on-disk layout ---------------------- */
+/* One text file per array in `dir` (created if missing): positions.dat,
+ * velocities.dat, forces.dat ("x<TAB>y" lines), radii.dat, masses.dat,
+ * potential_energy.dat, box_size.dat (one value per line), "%.17e", static
+ * order -- the layout of the reference's StateLog (src/io/state_log.cu:27-41,
+ * include/io/io_utils.h:81-108, include/constants.h:11); step.dat too when
+ * step >= 0 (a restart directory). */
+int dpg_write_state(dpg_handle h, const char *dir, int64_t step);
+/* Reads positions, radii, masses, box_size (required) and velocities (optional,
+ * else zero) from `dir` into the system, as Particle::loadDataFromPath
+ * (src/particles/base/particle.cu:180-215); the slot order is reset. */
+int dpg_read_state(dpg_handle h, const char *dir);
+/* number of particles in a state directory (values in radii.dat) */
+int dpg_state_count(const char *dir, int64_t *n_particles);
+
+/* ---- damped NVE and gradient descent ----------------------------------- */
+/* calculateDampedForces: F -= damping * v (src/particles/base/particle.cu:1363-1365,
+ * kernel src/particles/base/kernels.cu:83-89) */
+int dpg_damped_forces(dpg_handle h, double damping);
+/* n DampedNVE::step (src/integrator/damped_nve.cu:15-27): kick dt/2, drift,
+ * neighbour check, F = -damping v + pair forces, kick dt/2; one device loop */
+int dpg_damped_nve_steps(dpg_handle h, double dt, double damping, int64_t n_steps);
+/* updatePositionsGradDesc: x += alpha F (src/particles/base/particle.cu:267-269) */
+int dpg_grad_desc_step(dpg_handle h, double alpha);
+/* n GradDesc::step (src/integrator/grad_desc.cu:11-17): zero, neighbour check,
+ * forces, x += alpha F */
+int dpg_grad_desc_steps(dpg_handle h, double alpha, int64_t n_steps);
+
 /* ---- FIRE / Adam ------------------------------------------------------ */
 /* Particle::getPowerFire (src/particles/base/particle.cu:993-1009) */
 int dpg_power_fire(dpg_handle h, double *power);
@@ -189,6 +217,13 @@ int dpg_fire_get(dpg_handle h, double *alpha, double *dt, int64_t *n_good, int64
                  int *stopped);
 /* minimizeFire (src/routines/minimization.cu:75-112), device-resident loop */
 int dpg_fire_minimize(dpg_handle h, const dpg_fire_params *p, dpg_fire_result *r);
+/* DPG_MIXED systems (no reference counterpart): pair forces are FP32 from
+ * per-particle offsets to grid-cell centres, summed in FP64.  In
+ * dpg_fire_minimize the system switches to the FP64 pair arithmetic once
+ * max|F| <= switch_fmax (default 1e-6), FIRE goes uphill 6 times running, or
+ * max|F| stops falling for 2000 iterations; the PE-change and fmax_target
+ * stop tests only pass in FP64. */
+int dpg_set_mixed_switch(dpg_handle h, double switch_fmax);
 /* Particle::initAdamVariables (src/particles/base/particle.cu:319-322) */
 int dpg_adam_init(dpg_handle h);
 /* Particle::updatePositionsAdam (src/particles/base/particle.cu:329-333) */
@@ -332,6 +367,11 @@ int dpg_bumpy_fire_init(dpg_bumpy_handle h, double alpha_init, double dt);
 int dpg_bumpy_fire_step(dpg_bumpy_handle h, int *stopped);
 /* minimizeFire with the rigid overrides; p->fmax_target > 0 stops at
  * max|F_b| <= fmax_target and max|tau_b| <= tmax_target */
+/* DPG_MIXED bodies (no reference counterpart): FP32 vertex-pair forces, FP64
+ * vertex torques and body sums; FIRE switches to FP64 vertex pairs once
+ * max(|F|, |tau|) <= switch_fmax (default 1e-6) or stops falling, and only an
+ * FP64 state passes the stop tests */
+int dpg_bumpy_set_mixed_switch(dpg_bumpy_handle h, double switch_fmax);
 int dpg_bumpy_fire_minimize(dpg_bumpy_handle h, const dpg_fire_params *p, double tmax_target,
                             dpg_fire_result *r);
 /* scalePositionsFull (rigid_bumpy.cu:1044-1048) with the box: Particle::scaleBox */
@@ -356,7 +396,8 @@ typedef struct {
     double skin;        /* lists rebuilt when a particle moved more than skin / 2 */
     int precision;      /* DPG_FP64, or DPG_MIXED (FP32 pair forces, then FP64 refinement) */
     int reserved;
-    double switch_fmax; /* DPG_MIXED: FP32 pair forces until max|F| <= switch_fmax */
+    double switch_fmax; /* DPG_MIXED: FP32 pair forces until max|F| <= switch_fmax (0: 1e-6)
+                           or until max|F| stops falling; FP64 pair forces after */
 } dpg_ensemble_params;
 
 typedef struct {
@@ -378,6 +419,13 @@ int dpg_ensemble_set_state(dpg_ensemble e, const double *x, const double *y, con
 int dpg_ensemble_get_state(dpg_ensemble e, double *x, double *y, double *fx, double *fy);
 /* minimizeFire on every system (p->fmax_target > 0 adds the max|F_i| stop) */
 int dpg_ensemble_fire_minimize(dpg_ensemble e, const dpg_fire_params *p, dpg_ensemble_result *per_system);
+/* One force pass on every system at its current positions (cell and neighbour
+ * lists rebuilt first): forces readable with dpg_ensemble_get_state, and
+ * per-system avg_pe, max_force, pressure and contacts in per_system (may be
+ * NULL).  precision DPG_FP64 uses the reference pair arithmetic, DPG_MIXED
+ * the FP32 pair forces (systems with fewer than 3 cells a side use FP64).
+ * Disk::calculateForces (src/particles/disk/disk.cu:218-221) for a batch. */
+int dpg_ensemble_compute_forces(dpg_ensemble e, int precision, dpg_ensemble_result *per_system);
 /* pressure-band jamming of every system (the dpg_jam_pressure control flow) */
 int dpg_ensemble_jam(dpg_ensemble e, const dpg_jam_params *p, dpg_ensemble_result *per_system);
 
@@ -391,6 +439,15 @@ int dpg_ensemble_jam(dpg_ensemble e, const dpg_jam_params *p, dpg_ensemble_resul
  * reference counterpart: this is the measurement hook bench.py uses for the
  * per-kernel roofline. */
 int dpg_profile_loop(dpg_handle h, int kind, int iters, double dt, double *avg_us, int64_t *counts);
+/* The ensemble's FIRE loop from a fresh start (the dpg_ensemble_fire_minimize
+ * parameters), `iters` iterations as plain stream launches with events around
+ * each phase: avg_us[4] = mean device time per iteration of move, cell/list
+ * rebuild kernels, forces (+ per-system reductions and FIRE decisions),
+ * transition; counts[3] = {iterations, list rebuilds summed over systems,
+ * force passes summed over systems}.  Leaves the systems mid-minimisation
+ * (set the state again before a solve).  No reference counterpart. */
+int dpg_ensemble_profile_loop(dpg_ensemble e, const dpg_fire_params *p, int iters, double *avg_us,
+                              int64_t *counts);
 
 #ifdef __cplusplus
 }

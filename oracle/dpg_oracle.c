@@ -660,6 +660,54 @@ void orc_nve_steps(orc_sys *s, double dt, int64_t n_steps) {
     }
 }
 
+/* kernelCalculateDampedForces: src/particles/base/kernels.cu:83-89 */
+void orc_damped_forces(orc_sys *s, double gamma) {
+    const int64_t n = s->n;
+#pragma omp parallel for schedule(static) if (n >= PAR_MIN)
+    for (int64_t i = 0; i < n; i++) {
+        s->fx[i] -= gamma * s->vx[i];
+        s->fy[i] -= gamma * s->vy[i];
+    }
+}
+
+/* DampedNVE::step: src/integrator/damped_nve.cu:15-27 */
+void orc_damped_nve_steps(orc_sys *s, double dt, double gamma, int64_t n_steps) {
+    for (int64_t t = 0; t < n_steps; t++) {
+        orc_update_velocities(s, 0.5 * dt);
+        orc_update_positions(s, dt);
+        orc_check_for_neighbor_update(s);
+        orc_zero_force_and_pe(s);
+        orc_damped_forces(s, gamma);
+        orc_calculate_forces(s);
+        orc_update_velocities(s, 0.5 * dt);
+    }
+}
+
+/* kernelGradDescStep: src/particles/base/kernels.cu:613-637 */
+void orc_update_positions_grad_desc(orc_sys *s, double alpha) {
+    const int64_t n = s->n;
+#pragma omp parallel for schedule(static) if (n >= PAR_MIN)
+    for (int64_t i = 0; i < n; i++) {
+        double px = s->x[i] + alpha * s->fx[i];
+        double py = s->y[i] + alpha * s->fy[i];
+        s->x[i] = px; s->y[i] = py;
+        double dxn = px - s->lnx[i], dyn = py - s->lny[i];
+        s->nd2[i] = dxn * dxn + dyn * dyn;
+        double dxc = px - s->lcx[i], dyc = py - s->lcy[i];
+        s->cd2[i] = dxc * dxc + dyc * dyc;
+    }
+}
+
+/* GradDesc::step: src/integrator/grad_desc.cu:11-17 */
+void orc_grad_desc_steps(orc_sys *s, double alpha, int64_t n_steps) {
+    for (int64_t t = 0; t < n_steps; t++) {
+        orc_zero_force_and_pe(s);
+        orc_check_for_neighbor_update(s);
+        orc_calculate_forces(s);
+        orc_update_positions_grad_desc(s, alpha);
+    }
+}
+
 /* ======================================================================
  *  FIRE: src/integrator/fire.cu:3-46, include/integrator/fire.h:15-35
  * ====================================================================== */

@@ -74,6 +74,10 @@ double orc_total_ke(orc_sys *s); /* computes per-particle KE first */
 double orc_max_force(orc_sys *s);
 double orc_force_balance(orc_sys *s);
 void orc_nve_steps(orc_sys *s, double dt, int64_t n_steps);
+void orc_damped_forces(orc_sys *s, double gamma);                    /* F -= gamma v */
+void orc_damped_nve_steps(orc_sys *s, double dt, double gamma, int64_t n_steps);
+void orc_update_positions_grad_desc(orc_sys *s, double alpha);       /* x += alpha F */
+void orc_grad_desc_steps(orc_sys *s, double alpha, int64_t n_steps);
 
 /* ---- FIRE -------------------------------------------------------------- */
 void orc_fire_init(orc_sys *s, double alpha_init, double dt);

@@ -71,6 +71,8 @@ _SIGS = {
     "total_ke": (D, [P]),
     "max_force": (D, [P]),
     "nve_steps": (None, [P, D, I64]),
+    "damped_nve_steps": (None, [P, D, D, I64]),
+    "grad_desc_steps": (None, [P, D, I64]),
     "fire_init": (None, [P, D, D]),
     "fire_step": (C.c_int, [P]),
     "fire_state": (None, [P, DP, DP, LP, LP, C.POINTER(C.c_int)]),
@@ -265,6 +267,12 @@ class DiskOracle:
 
     def nve_steps(self, dt, n):
         self._f("nve_steps")(self.h, float(dt), int(n))
+
+    def damped_nve_steps(self, dt, gamma, n):
+        self._f("damped_nve_steps")(self.h, float(dt), float(gamma), int(n))
+
+    def grad_desc_steps(self, alpha, n):
+        self._f("grad_desc_steps")(self.h, float(alpha), int(n))
 
     def fire_init(self, alpha_init=0.1, dt=1e-2):
         self._f("fire_init")(self.h, float(alpha_init), float(dt))

@@ -467,6 +467,37 @@ void ref_nve_steps(ref_sys *s, double dt, int64_t n_steps) {
     }
 }
 
+/* DampedNVE::step (src/integrator/damped_nve.cu:15-27) over the reference kernels */
+void ref_damped_nve_steps(ref_sys *s, double dt, double gamma, int64_t n_steps) {
+    for (int64_t t = 0; t < n_steps; t++) {
+        ref_update_velocities(s, 0.5 * dt);
+        ref_update_positions(s, dt);
+        ref_check_for_neighbor_update(s);
+        ref_zero_force_and_pe(s);
+        sync(s);
+        launch(s->n, [&] {
+            kernelCalculateDampedForces(s->fx.data(), s->fy.data(), s->vx.data(), s->vy.data(), gamma);
+        });
+        ref_calculate_forces(s);
+        ref_update_velocities(s, 0.5 * dt);
+    }
+}
+
+/* GradDesc::step (src/integrator/grad_desc.cu:11-17) over the reference kernels */
+void ref_grad_desc_steps(ref_sys *s, double alpha, int64_t n_steps) {
+    for (int64_t t = 0; t < n_steps; t++) {
+        ref_zero_force_and_pe(s);
+        ref_check_for_neighbor_update(s);
+        ref_calculate_forces(s);
+        sync(s);
+        launch(s->n, [&] {
+            kernelGradDescStep(s->x.data(), s->y.data(), s->fx.data(), s->fy.data(), s->lnx.data(),
+                               s->lny.data(), s->nd2.data(), s->lcx.data(), s->lcy.data(),
+                               s->cd2.data(), alpha);
+        });
+    }
+}
+
 void ref_fire_init(ref_sys *s, double alpha_init, double dt) {
     s->f_alpha = alpha_init; s->f_alpha0 = alpha_init; s->f_dt = dt;
     s->f_dtmax = 10.0 * dt; s->f_dtmin = 0.001 * dt;

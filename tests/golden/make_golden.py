@@ -134,6 +134,22 @@ def make_fire_min():
     np.savez_compressed(HERE / "disk_n2048_fire_min.npz", **d)
 
 
+def make_damped_gd():
+    """DampedNVE (src/integrator/damped_nve.cu) and GradDesc (src/integrator/grad_desc.cu)."""
+    d = {}
+    n, phi, seed = 512, 0.84, 9
+    o, st, vx, vy, meth = system(n, phi, seed, vel_T=1e-3)
+    d.update(x0=st["x"], y0=st["y"], r=st["r"], m=st["m"], box=st["box"], vx0=vx, vy0=vy,
+             method=meth)
+    o.damped_nve_steps(1e-2, 0.5, 300)
+    snapshot(o, "damped300", d)
+    d["damped300_rebuilds"] = np.array(o.num_rebuilds())
+    o.grad_desc_steps(1e-2, 200)
+    snapshot(o, "gd200", d)
+    d["gd200_rebuilds"] = np.array(o.num_rebuilds())
+    np.savez_compressed(HERE / "disk_n512_damped_gd.npz", **d)
+
+
 def make_rng():
     d = {}
     for seed in (1, 7, 12345):
@@ -185,10 +201,15 @@ def make_bumpy(nb, phi, seed, name):
 if __name__ == "__main__":
     if build_reference() is None:
         sys.exit("reference tree not available; cannot regenerate fixtures")
+    if len(sys.argv) > 1:  # regenerate only the named fixtures, e.g. make_damped_gd
+        for name in sys.argv[1:]:
+            globals()[name]()
+        sys.exit(0)
     make_rng()
     make_small()
     make_cfg1()
     make_fire_min()
+    make_damped_gd()
     make_bumpy(64, 0.80, 3, "bumpy_n64_verlet.npz")
     make_bumpy(256, 0.80, 5, "bumpy_n256_cell.npz")
     print("fixtures written to", HERE)

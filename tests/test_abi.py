@@ -49,3 +49,15 @@ def test_error_path_without_gpu_is_loud():
     from dpcuda_gb300 import Disk, DpgError
     with pytest.raises(DpgError):
         Disk(16, 10.0)
+
+
+def test_state_count_reads_the_reference_layout(tmp_path):
+    """dpg_state_count is host-only: count the values of radii.dat written in the
+    reference's StateLog format ("%.17e", one per line)."""
+    import numpy as np
+    from dpcuda_gb300 import Disk, DpgError
+    r = np.linspace(0.5, 0.7, 37)
+    (tmp_path / "radii.dat").write_text("".join(f"{v:.17e}\n" for v in r))
+    assert Disk.stateCount(tmp_path) == 37
+    with pytest.raises(DpgError):
+        Disk.stateCount(tmp_path / "missing")

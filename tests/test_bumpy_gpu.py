@@ -121,3 +121,39 @@ def test_bumpy_nve_energy_drift(dpg):
     o1 = b.observables()
     e1 = o1["pe"] + o1["ke"]
     assert abs(e1 - e0) / abs(e0) < 1e-3
+
+
+# ---- the mixed form: FP32 vertex pairs, FP64 torques and body sums ----------
+def make_mixed(dpg, d):
+    nb = len(d["r"])
+    b = dpg.RigidBumpy(nb, int(d["nvb"].sum()), float(d["box"]), float(d["e_c"]), 2.0,
+                       float(d["rv"]), float(d["seg"]), True, precision=1)
+    b.setBodies(d["x0"], d["y0"], d["th0"], d["r"], d["nvb"])
+    b.setVertexPositions(d["px0"], d["py0"])
+    b.setMass(1.0)
+    return b
+
+
+def test_mixed_body_forces_match_fp64(dpg):
+    d = dict(np.load(G / "bumpy_n256_cell.npz"))
+    a, m = make(dpg, d), make_mixed(dpg, d)
+    a.setupNeighbors("cell", 1.5, 0.2, 8.0, 0.5)
+    m.setupNeighbors("cell", 1.5, 0.2, 8.0, 0.5)
+    ba, bm = a.getBodies(), m.getBodies()
+    scale = max(np.abs(ba["fx"]).max(), np.abs(ba["fy"]).max())
+    for k in ("fx", "fy"):
+        np.testing.assert_allclose(bm[k], ba[k], rtol=0, atol=1e-5 * scale, err_msg=k)
+    np.testing.assert_allclose(bm["tq"], ba["tq"], rtol=0, atol=1e-5 * np.abs(ba["tq"]).max())
+
+
+def test_mixed_bumpy_fire_refines_to_fp64_residual(dpg):
+    from oracle.oracle import bumpy_packing
+    st = bumpy_packing(128, 0.82, 9)
+    b = dpg.RigidBumpy(128, st["nv"], st["box"], st["e_c"], 2.0, st["rv"], st["seg"], True,
+                       precision=1)
+    b.setBodies(st["x"], st["y"], st["th"], st["r"], st["nvb"])
+    b.setMass(1.0)
+    b.setupNeighbors("cell", 1.5, 0.2, 8.0, 0.5)
+    r = b.minimizeFire(0.1, 1e-2, 0.0, 0.0, 400000, fmax_target=1e-12, tmax_target=1e-12)
+    obs = b.observables()
+    assert r["converged"] == 1 and obs["max_force"] <= 1e-12 and obs["max_torque"] <= 1e-12

@@ -105,6 +105,35 @@ def test_single_ops_match_fused_nve(dpg):
         np.testing.assert_array_equal(a[k], b[k])
 
 
+def test_damped_nve_and_gradient_descent_bitexact(dpg):
+    """DampedNVE::step and GradDesc::step against the reference kernels'
+    trajectories, with neighbour rebuilds on the way."""
+    d = load("disk_n512_damped_gd.npz")
+    s = make(dpg, d)
+    s.dampedNveSteps(1e-2, 0.5, 300)
+    assert_state(s, d, "damped300")
+    info = s.neighborInfo()
+    assert (info["n_rebuilds"], info["n_cell_rebuilds"]) == tuple(int(v) for v in d["damped300_rebuilds"])
+    s.gradDescSteps(1e-2, 200)
+    assert_state(s, d, "gd200")
+    info = s.neighborInfo()
+    assert (info["n_rebuilds"], info["n_cell_rebuilds"]) == tuple(int(v) for v in d["gd200_rebuilds"])
+    # the per-method form of DampedNVE::step gives the same trajectory
+    a, b = make(dpg, d), make(dpg, d)
+    for _ in range(40):
+        a.updateVelocities(0.5e-2)
+        a.updatePositions(1e-2)
+        a.checkForNeighborUpdate()
+        a.zeroForceAndPotentialEnergy()
+        a.calculateDampedForces(0.5)
+        a.calculateForces()
+        a.updateVelocities(0.5e-2)
+    b.dampedNveSteps(1e-2, 0.5, 40)
+    sa, sb = a.getState(), b.getState()
+    for k in KEYS:
+        np.testing.assert_array_equal(sa[k], sb[k])
+
+
 def test_fire_steps_bitexact(dpg):
     d = load("disk_n1024_cell.npz")
     s = make(dpg, d)
@@ -155,8 +184,10 @@ def test_fire_minimize_matches_reference(dpg):
     assert r["stopped"] == int(d["stopped"])
     assert abs(r["steps"] - int(d["steps"])) <= max(50, int(d["steps"]) // 100)
     np.testing.assert_allclose(r["avg_pe"], float(d["avg_pe"]), rtol=1e-10)
+    # the PE-change test stops FIRE while particles still move by ~1e-7 per
+    # step, so stopping a few steps apart leaves positions ~1e-7 apart
     a = s.getState()
-    np.testing.assert_allclose(a["x"], d["x"], rtol=0, atol=1e-8)
+    np.testing.assert_allclose(a["x"], d["x"], rtol=0, atol=2e-6)
     # pressure: the stop points differ by a few steps; 1e-8 relative
     np.testing.assert_allclose(s.getPressure(), float(d["pressure"]), rtol=1e-8)
 
@@ -297,3 +328,92 @@ def test_large_n_properties(dpg):
     s.nveSteps(1e-2, 50)
     b = s.getState()
     assert np.all(np.isfinite(b["x"]))
+
+
+def test_state_files_round_trip_in_reference_layout(dpg, tmp_path):
+    """dpg_write_state writes the reference's StateLog layout ("%.17e", x<TAB>y,
+    static order); dpg_read_state loads it back bit for bit."""
+    d = load("disk_n1024_cell.npz")
+    s = make(dpg, d)
+    s.nveSteps(1e-2, 50)
+    s.writeState(tmp_path / "restart", step=50)
+    st = s.getState()
+    lines = (tmp_path / "restart" / "positions.dat").read_text().splitlines()
+    assert lines[3] == f"{st['x'][3]:.17e}\t{st['y'][3]:.17e}"
+    assert (tmp_path / "restart" / "step.dat").read_text() == "50"
+    assert dpg.Disk.stateCount(tmp_path / "restart") == len(d["r"])
+    t = dpg.Disk(len(d["r"]), 1.0)
+    t.readState(tmp_path / "restart")
+    np.testing.assert_array_equal(t.getBoxSize(), s.getBoxSize())
+    got = t.getState()
+    for k in ("x", "y", "vx", "vy"):
+        np.testing.assert_array_equal(got[k], st[k])
+    # the loaded state continues like the original
+    t.setupNeighbors("cell", CUT_MULT, 0.2, 8.0, 0.5)
+    s2 = dpg.Disk(len(d["r"]), float(d["box"]))
+    s2.setState(st["x"], st["y"], st["vx"], st["vy"], d["r"], d["m"])
+    s2.setupNeighbors("cell", CUT_MULT, 0.2, 8.0, 0.5)
+    t.nveSteps(1e-2, 20)
+    s2.nveSteps(1e-2, 20)
+    a, b = t.getState(), s2.getState()
+    for k in KEYS:
+        np.testing.assert_array_equal(a[k], b[k])
+
+
+# ---- the mixed form (DPG_MIXED): FP32 pair forces, FP64 sums and integration ----
+def make_mixed(dpg, d, method="cell"):
+    n = len(d["r"])
+    s = dpg.Disk(n, float(d["box"]), precision=dpg.MIXED)
+    s.setState(d["x0"], d["y0"], d.get("vx0"), d.get("vy0"), d["r"], d["m"])
+    s.setupNeighbors(method, CUT_MULT, 0.2, 8.0, 0.5)
+    return s
+
+
+def test_mixed_forces_match_fp64(dpg):
+    """FP32 pair forces from cell-centre offsets agree with the FP64 forces to
+    1e-5 of the largest force (FP32 rounding of O(1) offsets and radii)."""
+    d = load("disk_n1024_cell.npz")
+    a, b = make(dpg, d), make_mixed(dpg, d)
+    for s in (a, b):
+        s.zeroForceAndPotentialEnergy()
+        s.calculateForces()
+    fa, fb = a.getState(), b.getState()
+    scale = max(np.abs(fa["fx"]).max(), np.abs(fa["fy"]).max())
+    for k in ("fx", "fy"):
+        np.testing.assert_allclose(fb[k], fa[k], rtol=0, atol=1e-5 * scale)
+    np.testing.assert_allclose(b.totalPotentialEnergy(), a.totalPotentialEnergy(), rtol=1e-5)
+
+
+def test_mixed_nve_tracks_fp64_and_conserves_energy(dpg):
+    d = load("disk_n1024_cell.npz")
+    a, b = make(dpg, d), make_mixed(dpg, d)
+    e0 = b.totalPotentialEnergy() + b.totalKineticEnergy()
+    a.nveSteps(1e-2, 100)
+    b.nveSteps(1e-2, 100)
+    sa, sb = a.getState(), b.getState()
+    np.testing.assert_allclose(sb["x"], sa["x"], rtol=0, atol=1e-6)
+    np.testing.assert_allclose(sb["y"], sa["y"], rtol=0, atol=1e-6)
+    b.nveSteps(1e-2, 2000)
+    e1 = b.totalPotentialEnergy() + b.totalKineticEnergy()
+    assert abs(e1 - e0) / abs(e0) < 1e-3
+
+
+def test_mixed_fire_refines_to_fp64_residual(dpg):
+    """Mixed FIRE switches to FP64 pair arithmetic and reaches max|F| <= 1e-12;
+    from the same partly relaxed start it ends at the FP64 path's energy."""
+    from oracle.oracle import disk_packing
+    st = disk_packing(2048, 0.86, 31)
+    s = dpg.Disk(2048, st["box"])
+    s.setState(st["x"], st["y"], None, None, st["r"], st["m"])
+    s.setupNeighbors("cell", CUT_MULT, 0.2, 8.0, 0.5)
+    dpg.minimizeFire(s, 0.1, 1e-2, 0.0, 0.0, 1_000_000, fmax_target=1e-5)
+    g = s.getState()
+    r64 = dpg.minimizeFire(s, 0.1, 1e-2, 0.0, 0.0, 1_000_000, fmax_target=1e-12)
+    pe64 = s.totalPotentialEnergy()
+    m = dpg.Disk(2048, st["box"], precision=dpg.MIXED)
+    m.setState(g["x"], g["y"], None, None, st["r"], st["m"])
+    m.setupNeighbors("cell", CUT_MULT, 0.2, 8.0, 0.5)
+    r = dpg.minimizeFire(m, 0.1, 1e-2, 0.0, 0.0, 1_000_000, fmax_target=1e-12)
+    assert r64["max_force"] <= 1e-12
+    assert r["converged"] and r["max_force"] <= 1e-12
+    np.testing.assert_allclose(m.totalPotentialEnergy(), pe64, rtol=1e-10)

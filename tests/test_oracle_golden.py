@@ -132,3 +132,16 @@ def test_oracle_matches_reference_kernels_on_scaling_and_revert():
     for k in ca:
         np.testing.assert_array_equal(ca[k], cb[k])
     assert a.box() == b.box()
+
+
+def test_damped_nve_and_gradient_descent():
+    """DampedNVE::step and GradDesc::step (src/integrator/damped_nve.cu:15-27,
+    src/integrator/grad_desc.cu:11-17), with neighbour rebuilds along the way."""
+    d = load("disk_n512_damped_gd.npz")
+    o = make(d)
+    o.damped_nve_steps(1e-2, 0.5, 300)
+    assert_state(o, d, "damped300")
+    assert list(o.num_rebuilds()) == list(d["damped300_rebuilds"])
+    o.grad_desc_steps(1e-2, 200)
+    assert_state(o, d, "gd200")
+    assert list(o.num_rebuilds()) == list(d["gd200_rebuilds"])
