@@ -26,6 +26,7 @@ UNITS = [
     ("disk_system.cu", ["--fmad=false"]),
     ("bumpy_system.cu", ["--fmad=false"]),
     ("ensemble_system.cu", ["--fmad=false"]),
+    ("noalloc.cu", ["--fmad=false"]),
     ("jam.cpp", []),
     ("state_io.cpp", []),
 ]

@@ -143,6 +143,7 @@ SIGNATURES = {
     "dpg_save_state": [VP],
     "dpg_restore_state": [VP],
     "dpg_profile_loop": [VP, I32, I32, D, DP, I64P],
+    "dpg_disk_forces_noalloc": [VP, VP, VP, I64, D, D, D, D, D, VP, VP, VP, VP],
     "dpg_ensemble_create": [C.POINTER(EnsembleParams), I64P, DP, VP, C.POINTER(VP)],
     "dpg_ensemble_destroy": [VP],
     "dpg_ensemble_set_state": [VP, DP, DP, DP, DP],
