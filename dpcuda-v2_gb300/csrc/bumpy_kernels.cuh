@@ -33,6 +33,7 @@ struct BumpyExt {
     int *o2n;                // old -> new body slot during a re-sort
     int *vnbr, *vcount;      // vertex neighbour list, column-major [capv][nv]
     float4 *vpk;             // mixed form: packed FP32 vertex offsets (see mixed_pack)
+    int mixed;               // 1: FP32 vertex pairs (the body DevParams stay FP64)
     long long vlist_built;   // n_rebuilds value at the last vertex-list build
     double tmax2, power_rot;
     // snapshot of the rotational state (setLastState)
@@ -103,7 +104,7 @@ __device__ __forceinline__ void body_move(BumpySys *bs, int b, int lane, double 
         double rxr = rx * ca - ry * sa, ryr = rx * sa + ry * ca;
         double2 nq = make_double2(nx + rxr, ny + ryr);
         x.vpos[f + k] = nq;
-        if (d.p.precision == kMixed) x.vpk[f + k] = mixed_pack(d.p, nq, x.rv);
+        if (x.mixed) x.vpk[f + k] = mixed_pack(d.p, nq, x.rv);
     }
 }
 
@@ -127,7 +128,7 @@ __device__ __forceinline__ void body_forces(const BumpySys *__restrict__ bs, int
     const double bx = d.p.box[0], by = d.p.box[1], e_c = d.p.e_c, n_c = d.p.n_c, rv = x.rv;
     const double2 c = d.v.pos[b];
     const int f = x.start[b], nvb = x.nvb[b];
-    const bool mixed = d.p.precision == kMixed && !d.s.fp64_now;
+    const bool mixed = x.mixed && !d.s.fp64_now;
     bfx = 0.0; bfy = 0.0; btq = 0.0; bpe = 0.0;
     for (int base = 0; base < nvb; base += 32) {
         int k = base + lane;
@@ -301,7 +302,7 @@ __global__ void kb_vlist(BumpySys *bs) {
             }
             x.vcount[v] = cnt;
             mxc = max(mxc, cnt);
-            if (d.p.precision == kMixed) x.vpk[v] = mixed_pack(d.p, q, x.rv);
+            if (x.mixed) x.vpk[v] = mixed_pack(d.p, q, x.rv);
         }
     }
     double val[1] = {(double)mxc};
@@ -549,7 +550,7 @@ __global__ void kb_fire_force(BumpySys *bs, int mode, double tmax_target) {
     long long it = s.iter;
     // mixed form: FP32 vertex pairs until the switch (as k_fire_force), then FP64
     bool fp64 = true;
-    if (ds->p.precision == kMixed && !s.fp64_now) {
+    if (bs->x.mixed && !s.fp64_now) {
         double g2 = fmax(v[2], v[3]);
         if (g2 < 0.81 * s.best_f2) { s.best_f2 = g2; s.best_it = it; }
         if (sqrt(g2) <= s.switch_fmax || s.f_nbad > 5 || it - s.best_it > 2000) s.fp64_now = 1;

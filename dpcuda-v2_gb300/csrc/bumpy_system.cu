@@ -163,7 +163,9 @@ extern "C" int dpg_bumpy_create(const dpg_bumpy_params *p, void *cuda_stream, dp
     }
     if (rc != DPG_OK) { dpg_bumpy_destroy(s); return rc; }
     DevParams &pp = s->h.b.p;
-    pp.n = s->nb; pp.method = -1; pp.cap = 4; pp.precision = p->precision;
+    // the body kernels shared with disks run in FP64; the mixed form lives in
+    // the vertex kernels (BumpyExt.mixed, vpk) on the same mixed grid
+    pp.n = s->nb; pp.method = -1; pp.cap = 4; pp.precision = DPG_FP64;
     pp.box[0] = p->box_x; pp.box[1] = p->box_y; pp.e_c = p->e_c; pp.n_c = p->n_c;
     if (p->precision == DPG_MIXED) {
         mixed_grid_init(pp);
@@ -171,6 +173,7 @@ extern "C" int dpg_bumpy_create(const dpg_bumpy_params *p, void *cuda_stream, dp
     }
     memset(&s->h.b.s, 0, sizeof(DevState));
     x.nv = s->nv; x.capv = 4; x.rotation = p->rotation ? 1 : 0; x.rv = p->vertex_radius;
+    x.mixed = p->precision == DPG_MIXED ? 1 : 0;
     x.vlist_built = 0;
     s->h_rad.assign(nb, 0.0);
     cudaError_t e = cudaMemcpyAsync(s->d, &s->h, sizeof(BumpySys), cudaMemcpyHostToDevice, s->stream);

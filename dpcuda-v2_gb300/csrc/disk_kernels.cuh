@@ -166,8 +166,10 @@ __device__ __forceinline__ void force_sum(const DevSys *__restrict__ ds, int i, 
     }
 }
 
+// mixed disk systems only (rigid-body systems keep their vertex offsets in
+// BumpyExt and leave the body DevParams at FP64)
 __device__ __forceinline__ void mixed_update(DevSys *ds, int i, double2 p) {
-    if (ds->p.precision == kMixed) ds->v.pk[i] = mixed_pack(ds->p, p, ds->v.rad[i]);
+    if (ds->p.precision == kMixed && ds->v.pk) ds->v.pk[i] = mixed_pack(ds->p, p, ds->v.rad[i]);
 }
 
 // mixed form: offsets of every particle from the current positions
