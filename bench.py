@@ -355,6 +355,7 @@ def run_ours(args):
 
     # ---- large-N force kernel (N = 2^20 NVE, plain FP64) -----------------------
     large = large_n_roofline(dpg, dev, sptr, peak)
+    others = other_configs(dpg, sptr)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -382,7 +383,7 @@ def run_ours(args):
                           "wall_s_timed": t_wall,
                           "plain_fp64": plain,
                           "mixed_batched_over_plain_fp64": value / plain["value"],
-                          "roofline_large": large}}
+                          "roofline_large": large, "other_workloads": others}}
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
@@ -422,6 +423,55 @@ def plain_fp64_leg(dpg, sptr, sts, timed):
     out["unit"] = "FIRE solves/s"
     out["dtype"] = "f64"
     out["force_group"] = "threads per particle chosen by the library (8 at N=16384)"
+    return out
+
+
+def other_configs(dpg, sptr):
+    """Throughput of the other workloads, FP64 drop-in vs mixed form, each timed
+    with CUDA events around one device-resident loop call:
+    - NVE of 1024 bidisperse disks at phi 0.80 (T 1e-4, dt 1e-2, 10^4 steps);
+    - NVE of 4096 rigid bumpy bodies (20 / 28 vertices, phi 0.80, dt 5e-3,
+      T 1e-4, 10^3 steps)."""
+    import torch
+    from dpcuda_gb300.init import bumpy_packing, disk_packing
+    stream = torch.cuda.ExternalStream(sptr)
+    out = {}
+
+    def time_call(fn):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / 1e3
+
+    rng = np.random.default_rng(1)
+    st = disk_packing(1024, 0.80, 1)
+    vx, vy = rng.normal(0, 1e-2, 1024), rng.normal(0, 1e-2, 1024)
+    vx -= vx.mean()
+    vy -= vy.mean()
+    for form, prec in (("fp64", dpg.FP64), ("mixed", dpg.MIXED)):
+        s = dpg.Disk(1024, st["box"], stream=sptr, precision=prec)
+        s.setState(st["x"], st["y"], vx, vy, st["r"], st["m"])
+        s.setupNeighbors("cell", CUT_MULT, 0.2, 8.0, 0.5)
+        s.nveSteps(1e-2, 100)
+        sec = time_call(lambda: s.nveSteps(1e-2, 10000))
+        out[f"nve_1024_{form}_particle_steps_per_s"] = 1024 * 10000 / sec
+        s.close()
+    b = bumpy_packing(4096, 0.80, 3)
+    bv = rng.normal(0, 1e-2, (2, 4096))
+    bv -= bv.mean(axis=1, keepdims=True)
+    for form, prec in (("fp64", 0), ("mixed", 1)):
+        r = dpg.RigidBumpy(4096, b["nv"], b["box"], b["e_c"], 2.0, b["rv"], b["seg"], True,
+                           stream=sptr, precision=prec)
+        r.setBodies(b["x"], b["y"], b["th"], b["r"], b["nvb"], bv[0], bv[1])
+        r.setMass(1.0)
+        r.setupNeighbors("cell", 1.5, 0.2, 8.0, 0.5)
+        r.nveSteps(5e-3, 20)
+        sec = time_call(lambda: r.nveSteps(5e-3, 1000))
+        out[f"bumpy_nve_4096_{form}_body_steps_per_s"] = 4096 * 1000 / sec
+        r.close()
     return out
 
 

@@ -553,7 +553,9 @@ __global__ void kb_fire_force(BumpySys *bs, int mode, double tmax_target) {
     if (bs->x.mixed && !s.fp64_now) {
         double g2 = fmax(v[2], v[3]);
         if (g2 < 0.81 * s.best_f2) { s.best_f2 = g2; s.best_it = it; }
-        if (sqrt(g2) <= s.switch_fmax || s.f_nbad > 5 || it - s.best_it > 2000) s.fp64_now = 1;
+        const double gm = sqrt(g2);
+        if (gm <= s.switch_fmax || s.f_nbad > 5 || (gm < 100.0 * s.switch_fmax && it - s.best_it > 2000))
+            s.fp64_now = 1;
         fp64 = false;
     }
     if ((fp64 && diff < s.pe_diff_target) || avg < s.pe_target) {

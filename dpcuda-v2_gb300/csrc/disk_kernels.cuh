@@ -853,12 +853,15 @@ __global__ void k_fire_force(DevSys *ds, int mode) {
     s.last_avg_pe = avg;
     long long it = s.iter;
     // mixed form: FP32 pairs until max|F| reaches switch_fmax, FIRE keeps going
-    // uphill, or max|F| stops falling (FP32 noise floor); FP64 pairs after, and
-    // only an FP64 state may pass the PE-change and max|F| tests
+    // uphill, or max|F| stops falling within 100x of switch_fmax (FP32 noise
+    // floor); FP64 pairs after, and only an FP64 state may pass the PE-change
+    // and max|F| tests
     bool fp64 = true;
     if (M && !s.fp64_now) {
         if (v[2] < 0.81 * s.best_f2) { s.best_f2 = v[2]; s.best_it = it; }
-        if (sqrt(v[2]) <= s.switch_fmax || s.f_nbad > 5 || it - s.best_it > 2000) s.fp64_now = 1;
+        const double fm = sqrt(v[2]);
+        if (fm <= s.switch_fmax || s.f_nbad > 5 || (fm < 100.0 * s.switch_fmax && it - s.best_it > 2000))
+            s.fp64_now = 1;
         fp64 = false;
     }
     if ((fp64 && diff < s.pe_diff_target) || avg < s.pe_target) {

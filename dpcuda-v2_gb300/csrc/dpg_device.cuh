@@ -221,23 +221,30 @@ __device__ __forceinline__ void warp_max(double (&v)[K]) {
 }
 
 // Reduce K values over the block (ops[k]: 0 = sum, 1 = max).  Thread 0 gets the result.
-template <int K>
-__device__ __forceinline__ void block_reduce(double (&v)[K], const int (&ops)[K], double *sm) {
+template <int K, typename T>
+__device__ __forceinline__ void block_reduce(T (&v)[K], const int (&ops)[K], T *sm) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    double s[K], m[K];
+    // warp tree (shfl_down), then warp results in order; ops are compile-time
+    // constants at every call site, so only the needed operation is emitted
 #pragma unroll
-    for (int k = 0; k < K; k++) { s[k] = v[k]; m[k] = v[k]; }
-    warp_sum(s);
-    warp_max(m);
+    for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            T o = __shfl_down_sync(0xffffffffu, v[k], off);
+            v[k] = ops[k] ? (v[k] > o ? v[k] : o) : v[k] + o;
+        }
     if (lane == 0)
 #pragma unroll
-        for (int k = 0; k < K; k++) sm[wid * K + k] = ops[k] ? m[k] : s[k];
+        for (int k = 0; k < K; k++) sm[wid * K + k] = v[k];
     __syncthreads();
     if (threadIdx.x == 0) {
 #pragma unroll
         for (int k = 0; k < K; k++) {
-            double a = sm[k];
-            for (int w = 1; w < nw; w++) a = ops[k] ? fmax(a, sm[w * K + k]) : a + sm[w * K + k];
+            T a = sm[k];
+            for (int w = 1; w < nw; w++) {
+                T b = sm[w * K + k];
+                a = ops[k] ? (a > b ? a : b) : a + b;
+            }
             v[k] = a;
         }
     }

@@ -32,8 +32,10 @@ namespace dpg {
 namespace {
 
 constexpr int kEB = 128;  // threads per block (slot ranges are padded to this)
-// a mixed system whose max|F| has not dropped by 10% for this many iterations
-// has reached the FP32 noise floor and switches to FP64 pair arithmetic
+// a mixed system within 100x of switch_fmax whose max|F| has not dropped by
+// 10% for this many iterations has reached the FP32 noise floor and switches
+// to FP64 pair arithmetic (far above it, FIRE's max|F| may plateau for
+// thousands of iterations while the packing rearranges)
 constexpr long long kStallIters = 2000;
 
 enum EPhase : int { kIdle = 0, kSetup = 1, kMinimize = 2 };
@@ -43,12 +45,14 @@ struct ESys {
     // geometry
     int off, n, blk0, nblk;
     int ncd, cell_off;       // cell grid (ncd x ncd) and its first global cell
-    double L, cs;
+    int item_off;            // first slot of its cell items (systems packed in order)
+    double L, cs, inv_cs;
     float cs_f;
     // loop
     int phase, rebuild, prec, done;
+    int vel_f32;             // velocities live in vel32 (set at the FP32 -> FP64 switch)
     int uphill, stopped, converged, pending;
-    long long iter, fire_total, rebuilds;
+    long long iter, fire_total, rebuilds, fp64_total;
     double dt, alpha, last_avg_pe;
     long long ngood, nbad;
     // results of the last force pass
@@ -86,9 +90,12 @@ struct EDev {
     int *slot_sys;           // slot -> system (-1 padding)
     double2 *pos, *vel, *frc, *pos_ref, *pos_save;
     double *rad, *mass, *pe, *vir;
-    float4 *pk;              // {offset x, offset y, radius, cell code}
+    float2 *vel32, *frc32;   // FP32 phase: velocities and forces
+    float *invm;             // 1 / mass
+    float4 *pk;              // {offset x, offset y, radius, cell code}, offsets from ctr
+    float2 *oref;            // offsets at the last list build (FP32 displacement test)
+    double2 *ctr;            // centre of the particle's (unwrapped) cell at the last build
     int *cellc;              // wrapped cell code (cx | cy << 16) of each slot
-    int2 *cellu;             // unwrapped cell indices (offsets are taken from these)
     int *nbr, *cnt;          // neighbour list [cap][T], counts
     int *cell_cnt, *cell_start, *cell_cur, *cell_items;
     double *part;            // [nblocks][8] block partials
@@ -108,17 +115,21 @@ __device__ __forceinline__ int code_y(int c) { return c >> 16; }
 // with all of its threads (thread t takes blocks t, t + blockDim, ... with a
 // compensated (Kahan) running sum, then a fixed-order tree over the threads),
 // so the result is deterministic and costs one L2 round trip, not one per
-// block.  Returns true on thread 0 of that block, with the totals in v
-// (ops[k]: 0 = sum, 1 = max of non-negative values).  Every thread of every
-// block must call it.
-template <int K>
-__device__ bool sys_reduce(EDev *e, ESys &s, double (&v)[K], const int (&ops)[K], unsigned *ticket) {
-    __shared__ double sm[32 * K];
+// block.  Block partials are reduced in T (FP32 in the FP32 phase, whose
+// per-particle values are FP32 anyway), the per-system totals in FP64.
+// Returns true on thread 0 of that block, with the totals in out (ops[k]:
+// 0 = sum, 1 = max of non-negative values).  Every thread of every block must
+// call it.
+template <int K, typename T>
+__device__ bool sys_reduce_t(EDev *e, ESys &s, T (&v)[K], const int (&ops)[K], unsigned *ticket,
+                             double (&out)[K]) {
+    __shared__ T sm[32 * K];
+    __shared__ double smd[32 * K];
     __shared__ int last;
-    block_reduce<K>(v, ops, sm);
+    block_reduce<K, T>(v, ops, sm);
     if (threadIdx.x == 0) {
 #pragma unroll
-        for (int k = 0; k < K; k++) e->part[(size_t)blockIdx.x * 8 + k] = v[k];
+        for (int k = 0; k < K; k++) e->part[(size_t)blockIdx.x * 8 + k] = (double)v[k];
         __threadfence();
         unsigned t = atomicAdd(ticket, 1u);
         last = (t == (unsigned)s.nblk - 1);
@@ -145,13 +156,19 @@ __device__ bool sys_reduce(EDev *e, ESys &s, double (&v)[K], const int (&ops)[K]
             }
         }
     }
-    block_reduce<K>(a, ops, sm);
+    block_reduce<K, double>(a, ops, smd);
     if (threadIdx.x == 0) {
 #pragma unroll
-        for (int k = 0; k < K; k++) v[k] = a[k];
+        for (int k = 0; k < K; k++) out[k] = a[k];
         return true;
     }
     return false;
+}
+
+// FP64 values in and out (v holds the totals on the returning thread)
+template <int K>
+__device__ bool sys_reduce(EDev *e, ESys &s, double (&v)[K], const int (&ops)[K], unsigned *ticket) {
+    return sys_reduce_t<K, double>(e, s, v, ops, ticket, v);
 }
 
 __device__ __forceinline__ bool grid_last(EDev *e) {
@@ -191,46 +208,128 @@ __device__ void e_fire_decide(const EParams &p, ESys &s, double power) {
     }
 }
 
+// ---- FP64 reciprocal and reciprocal square root for the refinement stage ----
+// Newton-Raphson iteration on an FP32 estimate: y <- y (1.5 - 0.5 x y^2) for
+// x^-1/2 and y <- y (2 - x y) for x^-1; each step doubles the number of
+// correct bits, so two steps from the 2^-23 FP32 seed reach FP64 precision.
+// Valid for x in the FP32 normal range (contact distances and radius sums).
+__device__ __forceinline__ double rsqrt_newton(double x) {
+    double y = (double)rsqrtf((float)x);
+    y = y * (1.5 - 0.5 * x * y * y);
+    y = y * (1.5 - 0.5 * x * y * y);
+    return y;
+}
+
+__device__ __forceinline__ double rcp_newton(double x) {
+    double y = (double)(1.0f / (float)x);
+    y = y * (2.0 - x * y);
+    y = y * (2.0 - x * y);
+    return y;
+}
+
+// FIRE mix (per-particle norms, src/particles/base/kernels.cu:91-112) with
+// |v| / |F| from the Newton reciprocal square root; the FP64 square root is
+// kept only for |v|^2 below the FP32 normal range
+__device__ __forceinline__ double2 fire_mix_newton(double2 v, double2 f, double alpha) {
+    const double fn2 = f.x * f.x + f.y * f.y, vn2 = v.x * v.x + v.y * v.y;
+    double mix = 0.0;
+    if (fn2 > 1e-32) {  // |F| > 1e-16
+        const double vn = vn2 > 1e-36 ? vn2 * rsqrt_newton(vn2) : sqrt(vn2);
+        mix = vn * rsqrt_newton(fn2) * alpha;
+    } else {
+        v = make_double2(0.0, 0.0);
+    }
+    return make_double2(v.x * (1 - alpha) + f.x * mix, v.y * (1 - alpha) + f.y * mix);
+}
+
 // ---- move -------------------------------------------------------------------
+// FIRE mix in FP32 (per-particle norms, src/particles/base/kernels.cu:91-112)
+__device__ __forceinline__ float2 fire_mix_f(float2 v, float2 f, float alpha) {
+    float fn = sqrtf(f.x * f.x + f.y * f.y), vn = sqrtf(v.x * v.x + v.y * v.y);
+    float mix = 0.f;
+    if (fn > 1e-16f) {
+        mix = vn / fn * alpha;
+    } else {
+        v = make_float2(0.f, 0.f);
+    }
+    return make_float2(v.x * (1.f - alpha) + f.x * mix, v.y * (1.f - alpha) + f.y * mix);
+}
+
+// FIRE move.  FP32 phase: velocities, forces, the kick and the mix in FP32;
+// FP64 only for the position sums and the offsets from the cell centre.
+// FP64 phase: the reference arithmetic.
 __global__ void __launch_bounds__(kEB) e_move(EDev *e) {
     const int sid = e->blk_sys[blockIdx.x];
     ESys &s = e->sys[sid];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool live = s.phase == kMinimize;
+    const bool f32 = s.prec == 0;
     double v[1] = {0.0};
+    float vf[1] = {0.f};
     if (live && i < s.off + s.n) {
-        const double dt = s.dt, alpha = s.alpha;
-        double2 u = e->vel[i], f = e->frc[i], x = e->pos[i];
-        if (s.uphill) {
-            double back = -dt / 2.0;
-            x.x = x.x + u.x * back;
-            x.y = x.y + u.y * back;
-            u = make_double2(0.0, 0.0);
-        }
-        double dtm = (dt / 2.0) / e->mass[i];
-        u.x = u.x + f.x * dtm;
-        u.y = u.y + f.y * dtm;
-        u = fire_mix(u, f, alpha);
-        x.x = x.x + u.x * dt;
-        x.y = x.y + u.y * dt;
-        e->vel[i] = u;
-        e->pos[i] = x;
-        double2 r = e->pos_ref[i];
-        double ddx = x.x - r.x, ddy = x.y - r.y;
-        v[0] = ddx * ddx + ddy * ddy;
-        if (s.prec == 0) {  // FP32 offset from the particle's (unwrapped) cell origin
-            int2 cu = e->cellu[i];
-            float4 k = e->pk[i];
-            k.x = (float)(x.x - (cu.x + 0.5) * s.cs);
-            k.y = (float)(x.y - (cu.y + 0.5) * s.cs);
-            e->pk[i] = k;
+        double2 x = e->pos[i];
+        const double2 c = e->ctr[i];
+        if (s.prec == 0) {
+            const float dt = (float)s.dt, alpha = (float)s.alpha;
+            float2 u = e->vel32[i];
+            const float2 f = e->frc32[i];
+            if (s.uphill) {
+                const float back = -0.5f * dt;
+                x.x += (double)(u.x * back);
+                x.y += (double)(u.y * back);
+                u = make_float2(0.f, 0.f);
+            }
+            const float h = 0.5f * dt * e->invm[i];
+            u.x += f.x * h;
+            u.y += f.y * h;
+            u = fire_mix_f(u, f, alpha);
+            e->vel32[i] = u;
+            x.x += (double)(u.x * dt);
+            x.y += (double)(u.y * dt);
+            e->pos[i] = x;
+            const float2 o = make_float2((float)(x.x - c.x), (float)(x.y - c.y));
+            *reinterpret_cast<float2 *>(&e->pk[i]) = o;
+            const float2 r = e->oref[i];
+            const float ddx = o.x - r.x, ddy = o.y - r.y;
+            vf[0] = ddx * ddx + ddy * ddy;
+        } else {
+            const double dt = s.dt, alpha = s.alpha;
+            double2 u, f = e->frc[i];
+            if (s.vel_f32) {
+                const float2 w = e->vel32[i];
+                u = make_double2(w.x, w.y);
+            } else {
+                u = e->vel[i];
+            }
+            if (s.uphill) {
+                double back = -dt / 2.0;
+                x.x = x.x + u.x * back;
+                x.y = x.y + u.y * back;
+                u = make_double2(0.0, 0.0);
+            }
+            double dtm = (0.5 * dt) * rcp_newton(e->mass[i]);
+            u.x = u.x + f.x * dtm;
+            u.y = u.y + f.y * dtm;
+            u = fire_mix_newton(u, f, alpha);
+            x.x = x.x + u.x * dt;
+            x.y = x.y + u.y * dt;
+            e->vel[i] = u;
+            e->pos[i] = x;
+            *reinterpret_cast<float2 *>(&e->pk[i]) = make_float2((float)(x.x - c.x), (float)(x.y - c.y));
+            double2 r = e->pos_ref[i];
+            double ddx = x.x - r.x, ddy = x.y - r.y;
+            v[0] = ddx * ddx + ddy * ddy;
         }
     }
     const int ops[1] = {1};
-    if (sys_reduce<1>(e, s, v, ops, &s.ticket_a)) {
+    double tot[1];
+    const bool last = f32 ? sys_reduce_t<1, float>(e, s, vf, ops, &s.ticket_a, tot)
+                          : sys_reduce_t<1, double>(e, s, v, ops, &s.ticket_a, tot);
+    if (last) {
         if (live) {
-            s.max_d2 = v[0];
+            s.max_d2 = tot[0];
             if (s.max_d2 > e->p.half_skin2) s.rebuild = 1;
+            if (s.prec == 1) s.vel_f32 = 0;  // every block has read vel32 by now
         }
         if (s.rebuild && s.phase != kIdle) atomicAdd(&e->n_flagged, 1);
     }
@@ -254,22 +353,30 @@ __global__ void __launch_bounds__(kEB) e_cell_count(EDev *e) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (!flagged(s) || i >= s.off + s.n) return;
     double2 x = e->pos[i];
-    long long ux = __double2ll_rd(x.x / s.cs), uy = __double2ll_rd(x.y / s.cs);
-    int cx = wrap_int(ux, s.ncd), cy = wrap_int(uy, s.ncd);
-    e->cellc[i] = code_of(cx, cy);
-    e->cellu[i] = make_int2((int)ux, (int)uy);
+    double fx = floor(x.x * s.inv_cs), fy = floor(x.y * s.inv_cs);
+    int cx = wrap_int((long long)fx, s.ncd), cy = wrap_int((long long)fy, s.ncd);
+    int code = code_of(cx, cy);
+    e->cellc[i] = code;
+    double2 c = make_double2((fx + 0.5) * s.cs, (fy + 0.5) * s.cs);
+    e->ctr[i] = c;
+    e->pk[i] = make_float4((float)(x.x - c.x), (float)(x.y - c.y), (float)e->rad[i], __int_as_float(code));
     atomicAdd(&e->cell_cnt[s.cell_off + cx + cy * s.ncd], 1);
 }
 
-__global__ void __launch_bounds__(kScanTPB) e_cell_scan(EDev *e) {
-    __shared__ int wsum[kScanTPB / 32];
+// exclusive scan of one system's cell counts per block (blockIdx.x = system);
+// a system's items start at its item_off, so systems need no carry between them
+constexpr int kEScanTPB = 256;
+__global__ void __launch_bounds__(kEScanTPB) e_cell_scan(EDev *e) {
+    __shared__ int wsum[kEScanTPB / 32];
     __shared__ int carry_s;
-    const int nc = e->p.total_cells;
+    const ESys &s = e->sys[blockIdx.x];
+    if (!flagged(s)) return;
+    const int nc = s.ncd * s.ncd, c0 = s.cell_off;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    int carry = 0;
-    for (int base = 0; base < nc; base += kScanTPB) {
+    int carry = s.item_off;
+    for (int base = 0; base < nc; base += kEScanTPB) {
         int idx = base + threadIdx.x;
-        int a = idx < nc ? e->cell_cnt[idx] : 0;
+        int a = idx < nc ? e->cell_cnt[c0 + idx] : 0;
         int incl = a;
 #pragma unroll
         for (int off = 1; off < 32; off <<= 1) {
@@ -279,21 +386,22 @@ __global__ void __launch_bounds__(kScanTPB) e_cell_scan(EDev *e) {
         if (lane == 31) wsum[wid] = incl;
         __syncthreads();
         if (wid == 0) {
-            int w = wsum[lane], wi = w;
+            int w = lane < kEScanTPB / 32 ? wsum[lane] : 0, wi = w;
 #pragma unroll
             for (int off = 1; off < 32; off <<= 1) {
                 int y = __shfl_up_sync(0xffffffffu, wi, off);
                 if (lane >= off) wi += y;
             }
-            wsum[lane] = wi - w;
+            if (lane < kEScanTPB / 32) wsum[lane] = wi - w;
             if (lane == 31) carry_s = wi;
         }
         __syncthreads();
-        if (idx < nc) e->cell_start[idx] = carry + wsum[wid] + incl - a;
+        if (idx < nc) e->cell_start[c0 + idx] = carry + wsum[wid] + incl - a;
         carry += carry_s;
         __syncthreads();
     }
-    if (threadIdx.x == 0) e->cell_start[nc] = carry;
+    // end of the last cell = start of the next system's items (sentinel)
+    if (threadIdx.x == 0) e->cell_start[c0 + nc] = s.item_off + s.n;
 }
 
 __global__ void __launch_bounds__(kEB) e_cell_fill(EDev *e) {
@@ -336,16 +444,22 @@ __global__ void __launch_bounds__(kEB) e_nlist(EDev *e) {
         int c = e->cellc[i];
         int cx = code_x(c), cy = code_y(c);
         if (ncd >= 3 && s.cs * s.cs >= c2) {
+            // FP32 distances from the cell-centre offsets, with a 1e-4 relative
+            // margin on the cutoff: the list may hold a few extra pairs, never
+            // miss one (offsets carry ~1e-7 absolute rounding)
+            const float4 a = e->pk[i];
+            const float c2f = e->p.cutoff2_f * 1.0001f, cs = s.cs_f;
             for (int oy = -1; oy <= 1; oy++) {
                 int yy = pmod(cy + oy, ncd);
                 for (int ox = -1; ox <= 1; ox++) {
                     int g = s.cell_off + pmod(cx + ox, ncd) + yy * ncd;
+                    const float sx = (float)ox * cs, sy = (float)oy * cs;
                     for (int k = e->cell_start[g]; k < e->cell_start[g + 1]; k++) {
                         int j = e->cell_items[k];
                         if (j == i) continue;
-                        double2 xj = e->pos[j];
-                        double dx = pbc_dist(xi.x, xj.x, L), dy = pbc_dist(xi.y, xj.y, L);
-                        if (dx * dx + dy * dy < c2) {
+                        float4 b = e->pk[j];
+                        float dx = (a.x - b.x) - sx, dy = (a.y - b.y) - sy;
+                        if (dx * dx + dy * dy < c2f) {
                             if (cnt < cap) e->nbr[(size_t)cnt * T + i] = j;
                             cnt++;
                         }
@@ -365,13 +479,8 @@ __global__ void __launch_bounds__(kEB) e_nlist(EDev *e) {
         }
         e->cnt[i] = cnt;
         e->pos_ref[i] = xi;
-        int2 cu = e->cellu[i];
-        float4 k;
-        k.x = (float)(xi.x - (cu.x + 0.5) * s.cs);
-        k.y = (float)(xi.y - (cu.y + 0.5) * s.cs);
-        k.z = (float)e->rad[i];
-        k.w = __int_as_float(c);
-        e->pk[i] = k;
+        const float4 k = e->pk[i];
+        e->oref[i] = make_float2(k.x, k.y);
     }
     double v[1] = {(double)cnt};
     const int ops[1] = {1};
@@ -391,8 +500,8 @@ __global__ void __launch_bounds__(kEB) e_nlist(EDev *e) {
 // FP32 pair force from offsets: displacement (o_i - o_j) + dc * cs with the
 // periodic wrap applied to the integer cell difference.
 __device__ __forceinline__ void pair_f32(const float4 a, const float4 b, int ncd, float cs,
-                                        float e_c, float &fx, float &fy, float &en, float &w,
-                                        int &contact) {
+                                        float e_c, float n_c, float &fx, float &fy, float &en,
+                                        float &w, int &contact) {
     int ca = __float_as_int(a.w), cb = __float_as_int(b.w);
     int dcx = code_x(ca) - code_x(cb), dcy = code_y(ca) - code_y(cb);
     if (dcx > ncd / 2) dcx -= ncd; else if (dcx < -(ncd / 2)) dcx += ncd;
@@ -405,10 +514,11 @@ __device__ __forceinline__ void pair_f32(const float4 a, const float4 b, int ncd
     if (d2 >= rs * rs) return;
     float d = sqrtf(d2);
     float ov = 1.0f - d / rs;
-    float fm = e_c * ov / (rs * d);
+    float ovp = n_c == 2.0f ? ov : powf(ov, n_c - 1.0f);
+    float fm = e_c * ovp / (rs * d);
     fx = fm * dx;
     fy = fm * dy;
-    en = 0.25f * e_c * ov * ov;
+    en = e_c * ov * ovp / (2.0f * n_c);
     w = fx * dx + fy * dy;
     contact = 1;
 }
@@ -426,6 +536,7 @@ __device__ void e_force_epilogue(EDev *e, ESys &s, const double (&v)[5], bool se
     s.contacts = v[4];
     double avg = s.pe / (double)s.n;
     s.fire_total++;
+    if (s.prec == 1) s.fp64_total++;
     bool finished = false;
     if (setup) {
         s.last_avg_pe = avg;
@@ -444,7 +555,11 @@ __device__ void e_force_epilogue(EDev *e, ESys &s, const double (&v)[5], bool se
             s.best_f2 = s.fmax2;
             s.best_it = s.iter;
         }
-        if (fmax <= p.switch_fmax || s.nbad > 5 || s.iter - s.best_it > kStallIters) s.prec = 1;
+        const bool stalled = fmax < 100.0 * p.switch_fmax && s.iter - s.best_it > kStallIters;
+        if (fmax <= p.switch_fmax || s.nbad > 5 || stalled) {
+            s.prec = 1;
+            s.vel_f32 = 1;  // the next move takes the FP32 velocities over
+        }
     }
     double diff = fabs(avg / s.last_avg_pe - 1);
     s.last_avg_pe = avg;
@@ -522,15 +637,17 @@ __global__ void __launch_bounds__(kEB) e_force(EDev *e) {
     const bool live = s.phase != kIdle;
     const bool setup = s.phase == kSetup;
     // partials: 0 PE, 1 power, 2 max|F|^2, 3 virial, 4 contacts
+    const bool f32 = s.prec == 0;
     double v[5] = {0, 0, 0, 0, 0};
+    float vf[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
     if (live && i < s.off + s.n) {
         const int T = p.T;
         int cnt = min(e->cnt[i], p.cap);
         double ax = 0.0, ay = 0.0, en = 0.0, wv = 0.0, nc = 0.0;
+        const float4 a = e->pk[i];
         if (s.prec == 0) {
             // FP32 pair terms summed in FP32 over runs of 8 neighbours, FP64 across runs
-            const float4 a = e->pk[i];
-            const float ecf = (float)p.e_c;
+            const float ecf = (float)p.e_c, ncf = (float)p.n_c;
             int ncount = 0;
             for (int k0 = 0; k0 < cnt; k0 += 8) {
                 float sx = 0.f, sy = 0.f, se = 0.f, sw = 0.f;
@@ -540,7 +657,7 @@ __global__ void __launch_bounds__(kEB) e_force(EDev *e) {
                     float4 b = e->pk[j];
                     float fx, fy, ef, wf;
                     int ct;
-                    pair_f32(a, b, s.ncd, s.cs_f, ecf, fx, fy, ef, wf, ct);
+                    pair_f32(a, b, s.ncd, s.cs_f, ecf, ncf, fx, fy, ef, wf, ct);
                     sx += fx;
                     sy += fy;
                     se += ef;
@@ -552,44 +669,80 @@ __global__ void __launch_bounds__(kEB) e_force(EDev *e) {
                 en += (double)se;
                 wv += (double)sw;
             }
-            nc = (double)ncount;
+            const float2 fv = make_float2((float)ax, (float)ay);
+            e->frc[i] = make_double2(ax, ay);
+            e->frc32[i] = fv;
+            float2 u = e->vel32[i];
+            if (!setup) {
+                const float h = 0.5f * (float)s.dt * e->invm[i];
+                u.x += fv.x * h;
+                u.y += fv.y * h;
+                e->vel32[i] = u;
+            }
+            vf[0] = (float)en;
+            vf[1] = fv.x * u.x + fv.y * u.y;
+            vf[2] = fv.x * fv.x + fv.y * fv.y;
+            vf[3] = (float)wv;
+            vf[4] = (float)ncount;
         } else {
+            // FP64 pair arithmetic for pairs that the FP32 offsets cannot rule
+            // out (a 1e-4 relative margin on the contact distance)
             const double2 xi = e->pos[i];
             const double ri = e->rad[i];
             for (int k = 0; k < cnt; k++) {
                 int j = __ldg(&e->nbr[(size_t)k * T + i]);
+                if (s.ncd >= 3) {
+                    const float4 b = e->pk[j];
+                    int ca = __float_as_int(a.w), cb = __float_as_int(b.w);
+                    int dcx = code_x(ca) - code_x(cb), dcy = code_y(ca) - code_y(cb);
+                    if (dcx > s.ncd / 2) dcx -= s.ncd; else if (dcx < -(s.ncd / 2)) dcx += s.ncd;
+                    if (dcy > s.ncd / 2) dcy -= s.ncd; else if (dcy < -(s.ncd / 2)) dcy += s.ncd;
+                    const float dxf = (a.x - b.x) + (float)dcx * s.cs_f;
+                    const float dyf = (a.y - b.y) + (float)dcy * s.cs_f;
+                    const float rsf = a.z + b.z;
+                    if (dxf * dxf + dyf * dyf >= rsf * rsf * 1.0001f) continue;
+                }
                 double2 xj = e->pos[j];
-                double fx, fy;
-                double ee = disk_pair(xi.x, xi.y, ri, xj.x, xj.y, e->rad[j], s.L, s.L, p.e_c, p.n_c, fx, fy);
+                double dx = pbc_dist(xi.x, xj.x, s.L), dy = pbc_dist(xi.y, xj.y, s.L);
+                double rs = ri + e->rad[j];
+                double d2 = dx * dx + dy * dy;
+                if (d2 >= rs * rs) continue;
+                // 1/d and 1/rs by Newton-Raphson from FP32 estimates: two steps
+                // take the 2^-23 seed to FP64 precision (quadratic convergence)
+                const double id = rsqrt_newton(d2), irs = rcp_newton(rs);
+                double d = d2 * id;
+                double ov = 1.0 - d * irs;
+                double ovp = p.n_c == 2.0 ? ov : pow(ov, p.n_c - 1);
+                double fm = p.e_c * ovp * irs * id;
+                double fx = fm * dx, fy = fm * dy;
                 ax += fx;
                 ay += fy;
-                en += ee;
-                if (fx != 0.0 || fy != 0.0) {
-                    double dx = pbc_dist(xi.x, xj.x, s.L), dy = pbc_dist(xi.y, xj.y, s.L);
-                    wv += fx * dx + fy * dy;
-                    nc += 1.0;
-                }
+                en += p.e_c * ov * ovp / (2.0 * p.n_c);
+                wv += fx * dx + fy * dy;
+                nc += 1.0;
             }
+            double2 f = make_double2(ax, ay);
+            e->frc[i] = f;
+            double2 u = e->vel[i];
+            if (!setup) {
+                double dtm = (0.5 * s.dt) * rcp_newton(e->mass[i]);
+                u.x = u.x + f.x * dtm;
+                u.y = u.y + f.y * dtm;
+                e->vel[i] = u;
+            }
+            v[0] = en;
+            v[1] = f.x * u.x + f.y * u.y;
+            v[2] = f.x * f.x + f.y * f.y;
+            v[3] = wv;
+            v[4] = nc;
         }
-        double2 f = make_double2(ax, ay);
-        e->frc[i] = f;
-        e->pe[i] = en;
-        double2 u = e->vel[i];
-        if (!setup) {
-            double dtm = (s.dt / 2.0) / e->mass[i];
-            u.x = u.x + f.x * dtm;
-            u.y = u.y + f.y * dtm;
-            e->vel[i] = u;
-        }
-        v[0] = en;
-        v[1] = f.x * u.x + f.y * u.y;
-        v[2] = f.x * f.x + f.y * f.y;
-        v[3] = wv;
-        v[4] = nc;
     }
     const int ops[5] = {0, 0, 1, 0, 0};
-    if (sys_reduce<5>(e, s, v, ops, &s.ticket_a) && live) {
-        e_force_epilogue(e, s, v, setup);
+    double tot[5];
+    const bool last = f32 ? sys_reduce_t<5, float>(e, s, vf, ops, &s.ticket_a, tot)
+                          : sys_reduce_t<5, double>(e, s, v, ops, &s.ticket_a, tot);
+    if (last && live) {
+        e_force_epilogue(e, s, tot, setup);
         if (s.pending != kActNone) atomicAdd(&e->n_pending, 1);
     }
     // the transition pass (graph IF node) runs only when some system asked for one
@@ -612,6 +765,7 @@ __global__ void __launch_bounds__(kEB) e_transition(EDev *e) {
         x.y *= s.scale;
         e->pos[i] = x;
         e->vel[i] = make_double2(0.0, 0.0);
+        e->vel32[i] = make_float2(0.f, 0.f);
     }
     double v[1] = {0.0};
     const int ops[1] = {0};
@@ -619,6 +773,7 @@ __global__ void __launch_bounds__(kEB) e_transition(EDev *e) {
         double L0 = act == kActRevertScale ? s.L_last : s.L;
         s.L = L0 * s.scale;
         s.cs = s.L / s.ncd;
+        s.inv_cs = s.ncd / s.L;
         s.cs_f = (float)s.cs;
         s.pending = kActNone;
         s.phase = kSetup;
@@ -632,6 +787,7 @@ __global__ void __launch_bounds__(kEB) e_transition(EDev *e) {
         s.converged = 0;
         s.iter = 0;
         s.prec = (e->p.switch_fmax > 0 && s.ncd >= 3) ? 0 : 1;
+        s.vel_f32 = 0;
     }
     if (grid_last(e)) e->n_pending = 0;
 }
@@ -658,8 +814,11 @@ __global__ void e_put(EDev *e, const double *x, const double *y, const double *r
     e->pos[i] = make_double2(x[k], y[k]);
     e->rad[i] = r[k];
     e->mass[i] = m[k];
+    e->invm[i] = (float)(1.0 / m[k]);
     e->vel[i] = make_double2(0.0, 0.0);
     e->frc[i] = make_double2(0.0, 0.0);
+    e->vel32[i] = make_float2(0.f, 0.f);
+    e->frc32[i] = make_float2(0.f, 0.f);
 }
 
 __global__ void e_get(EDev *e, double *x, double *y, double *fx, double *fy, const int *src_index) {

@@ -95,7 +95,7 @@ extern "C" int dpg_ensemble_create(const dpg_ensemble_params *p, const int64_t *
     if (m && (!strcmp(m, "stream") || !strcmp(m, "graph"))) s->mode = 0;
     // layout: each system padded to whole blocks; its own cell grid
     s->sys.assign(s->S, ESys{});
-    int slot = 0, blk = 0, cell = 0;
+    int slot = 0, blk = 0, cell = 0, item = 0;
     size_t in = 0;
     for (int k = 0; k < s->S; k++) {
         if (n_particles[k] <= 0 || !(box[k] > 0)) { delete s; return set_err(DPG_ERR_ARG, "system %d: bad size or box", k); }
@@ -108,7 +108,9 @@ extern "C" int dpg_ensemble_create(const dpg_ensemble_params *p, const int64_t *
         // cells at least 10% larger than the cutoff, so compression keeps them valid
         y.ncd = std::max(1, (int)std::floor(y.L / (p->cutoff * 1.1)));
         y.cell_off = cell;
+        y.item_off = item;
         y.cs = y.L / y.ncd;
+        y.inv_cs = y.ncd / y.L;
         y.cs_f = (float)y.cs;
         y.jam_status = -1;
         y.L_low = y.L_high = y.L_last = -1;
@@ -117,6 +119,7 @@ extern "C" int dpg_ensemble_create(const dpg_ensemble_params *p, const int64_t *
         slot += y.nblk * kEB;
         blk += y.nblk;
         cell += y.ncd * y.ncd;
+        item += y.n;
         s->n.push_back(y.n);
     }
     s->T = slot;
@@ -134,7 +137,9 @@ extern "C" int dpg_ensemble_create(const dpg_ensemble_params *p, const int64_t *
     A((void **)&h.pos, 16 * T); A((void **)&h.vel, 16 * T); A((void **)&h.frc, 16 * T);
     A((void **)&h.pos_ref, 16 * T); A((void **)&h.pos_save, 16 * T);
     A((void **)&h.rad, 8 * T); A((void **)&h.mass, 8 * T); A((void **)&h.pe, 8 * T);
-    A((void **)&h.pk, 16 * T); A((void **)&h.cellc, 4 * T); A((void **)&h.cellu, 8 * T);
+    A((void **)&h.pk, 16 * T); A((void **)&h.cellc, 4 * T);
+    A((void **)&h.vel32, 8 * T); A((void **)&h.frc32, 8 * T); A((void **)&h.invm, 4 * T);
+    A((void **)&h.oref, 8 * T); A((void **)&h.ctr, 16 * T);
     A((void **)&h.cnt, 4 * T);
     A((void **)&h.cell_cnt, 4 * ((size_t)s->total_cells + 1));
     A((void **)&h.cell_start, 4 * ((size_t)s->total_cells + 1));
@@ -206,7 +211,7 @@ static cudaGraphNode_t addk(cudaGraph_t g, cudaGraphNode_t dep, void *fn, int bl
 
 static int enqueue_rebuild(ES *s) {
     LAUNCH(e_cell_count, s->nblocks, kEB, s->d);
-    LAUNCH(e_cell_scan, 1, kScanTPB, s->d);
+    LAUNCH(e_cell_scan, s->S, kEScanTPB, s->d);
     LAUNCH(e_cell_fill, s->nblocks, kEB, s->d);
     LAUNCH(e_cell_sort, (s->total_cells + 255) / 256, 256, s->d);
     LAUNCH(e_nlist, s->nblocks, kEB, s->d);
@@ -251,7 +256,7 @@ static int build_graph(ES *s) {
         cudaGraph_t ib = ip.conditional.phGraph_out[0];
         cudaGraphNode_t prev = nullptr;
         prev = addk(ib, prev, (void *)e_cell_count, s->nblocks, kEB, a, &err);
-        prev = addk(ib, prev, (void *)e_cell_scan, 1, kScanTPB, a, &err);
+        prev = addk(ib, prev, (void *)e_cell_scan, s->S, kEScanTPB, a, &err);
         prev = addk(ib, prev, (void *)e_cell_fill, s->nblocks, kEB, a, &err);
         prev = addk(ib, prev, (void *)e_cell_sort, (s->total_cells + 255) / 256, 256, a, &err);
         prev = addk(ib, prev, (void *)e_nlist, s->nblocks, kEB, a, &err);
@@ -377,7 +382,7 @@ static int prepare(ES *s, const dpg_fire_params *fp, int jam, const dpg_jam_para
         y.jam_stage = 0; y.jam_status = -1; y.jam_step = 0;
         y.L_low = y.L_high = y.L_last = -1; y.L_saved = -1; y.scale = 1.0; y.rebuilds = 0;
         y.ticket_a = y.ticket_b = 0;
-        y.best_f2 = INFINITY; y.best_it = 0;
+        y.best_f2 = INFINITY; y.best_it = 0; y.vel_f32 = 0; y.fp64_total = 0;
     }
     CK(cudaMemcpyAsync(s->d_sys, s->sys.data(), sizeof(ESys) * s->S, cudaMemcpyHostToDevice, s->stream));
     CK(cudaMemcpyAsync(&s->d->p, &p, sizeof(EParams), cudaMemcpyHostToDevice, s->stream));
@@ -388,6 +393,7 @@ static int prepare(ES *s, const dpg_fire_params *fp, int jam, const dpg_jam_para
     TRY(put(s, &s->d->ticket, 0u));
     // velocities start at zero (minimizeFire's setVelocitiesToZero)
     CK(cudaMemsetAsync(s->h.vel, 0, 16 * (size_t)s->T, s->stream));
+    CK(cudaMemsetAsync(s->h.vel32, 0, 8 * (size_t)s->T, s->stream));
     return DPG_OK;
 }
 
@@ -412,6 +418,7 @@ static void fill_results(ES *s, dpg_ensemble_result *r) {
         o.fire_steps = y.fire_total;
         o.minimizations = y.minimizations;
         o.rebuilds = y.rebuilds;
+        o.fp64_steps = y.fp64_total;
         o.status = y.jam_status;
         o.converged = y.converged;
         o.packing_fraction = 0.0;  // filled by the caller, who knows the radii

@@ -25,7 +25,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", str(REP
 UNITS = [
     ("disk_system.cu", ["--fmad=false"]),
     ("bumpy_system.cu", ["--fmad=false"]),
-    ("ensemble_system.cu", ["--fmad=false"]),
+    ("ensemble_system.cu", []),
     ("noalloc.cu", ["--fmad=false"]),
     ("jam.cpp", []),
     ("state_io.cpp", []),

@@ -64,7 +64,7 @@ class Ensemble:
                             box_length=r.box_length, contacts=r.contacts,
                             packing_fraction=area / r.box_length ** 2, fire_steps=r.fire_steps,
                             minimizations=r.minimizations, rebuilds=r.rebuilds, status=r.status,
-                            converged=r.converged))
+                            converged=r.converged, fp64_steps=r.fp64_steps))
         return out
 
     def calculateForces(self, precision=FP64):

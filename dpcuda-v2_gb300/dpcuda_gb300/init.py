@@ -55,3 +55,39 @@ def disk_packing(n: int, phi: float, seed: int, size_ratio: float = 1.4,
     x = random_uniform(n, 0.0, box, 0, seed)
     y = random_uniform(n, 0.0, box, n, seed)
     return dict(x=x, y=y, r=r, m=np.ones(n), box=box)
+
+
+def bumpy_vertex_radius(min_diameter: float, n_vertices_small: int, seg: float) -> float:
+    """Vertex radius of the reference's rigid bumpy bodies
+    (src/particles/rigid_bumpy/rigid_bumpy.cu:570-610): adjacent vertices of
+    the smallest body, on a circle of diameter min_diameter, sit seg vertex
+    diameters apart."""
+    ang = 2.0 * np.pi / n_vertices_small
+    return min_diameter / (1.0 + seg / np.sin(ang / 2.0)) / 2.0
+
+
+def bumpy_packing(n_bodies: int, phi: float, seed: int, n_small: int = 20, seg: float = 0.9,
+                  size_ratio: float = 1.4, count_ratio: float = 0.5) -> dict:
+    """Bidisperse rigid bumpy bodies (RigidBumpy::initializeFromConfig,
+    src/particles/rigid_bumpy/rigid_bumpy.cu:138-230): body radii 0.5 and
+    size_ratio / 2, n_small vertices on the small bodies and
+    floor(n_small * size_ratio) on the large ones, one vertex radius from
+    bumpy_vertex_radius, vertex energy scale (2 r_v / d_min)^2, box at packing
+    fraction phi of the body discs, positions and angles from random_uniform
+    (angles share the positions' x stream, as the reference's offsets do)."""
+    n = int(n_bodies)
+    n_large = int(n * count_ratio)
+    r = np.full(n, 0.5)
+    r[:n_large] = size_ratio / 2.0
+    a = 0.0
+    for v in r.tolist():
+        a += v * v
+    box = (a * np.pi / phi) ** 0.5
+    x = random_uniform(n, 0.0, box, 0, seed)
+    y = random_uniform(n, 0.0, box, n, seed)
+    th = random_uniform(n, 0.0, 2 * np.pi, 0, seed)
+    n_lg = int(n_small * size_ratio)
+    nvb = np.where(r == size_ratio / 2.0, n_lg, n_small).astype(np.int64)
+    rv = bumpy_vertex_radius(1.0, n_small, seg)
+    e_c = (2.0 * rv / 1.0) ** 2
+    return dict(x=x, y=y, th=th, r=r, nvb=nvb, nv=int(nvb.sum()), box=box, rv=rv, e_c=e_c, seg=seg)

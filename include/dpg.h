@@ -221,8 +221,8 @@ int dpg_fire_minimize(dpg_handle h, const dpg_fire_params *p, dpg_fire_result *r
  * per-particle offsets to grid-cell centres, summed in FP64.  In
  * dpg_fire_minimize the system switches to the FP64 pair arithmetic once
  * max|F| <= switch_fmax (default 1e-6), FIRE goes uphill 6 times running, or
- * max|F| stops falling for 2000 iterations; the PE-change and fmax_target
- * stop tests only pass in FP64. */
+ * max|F|, once below 100 switch_fmax, stops falling for 2000 iterations; the
+ * PE-change and fmax_target stop tests only pass in FP64. */
 int dpg_set_mixed_switch(dpg_handle h, double switch_fmax);
 /* Particle::initAdamVariables (src/particles/base/particle.cu:319-322) */
 int dpg_adam_init(dpg_handle h);
@@ -397,7 +397,8 @@ typedef struct {
     int precision;      /* DPG_FP64, or DPG_MIXED (FP32 pair forces, then FP64 refinement) */
     int reserved;
     double switch_fmax; /* DPG_MIXED: FP32 pair forces until max|F| <= switch_fmax (0: 1e-6)
-                           or until max|F| stops falling; FP64 pair forces after */
+                           or until max|F| stops falling within 100 switch_fmax;
+                           FP64 pair forces after */
 } dpg_ensemble_params;
 
 typedef struct {
@@ -407,6 +408,7 @@ typedef struct {
     int64_t rebuilds;
     int status;             /* jamming: 0 final state, 1 length tolerance, 2 out of steps */
     int converged;
+    int64_t fp64_steps;     /* force passes with FP64 pair arithmetic (mixed: the refinement) */
 } dpg_ensemble_result;
 
 /* n_particles[s], box[s] (square boxes) */

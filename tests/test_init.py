@@ -32,3 +32,12 @@ def test_disk_packing_matches_oracle():
     assert a["box"] == b["box"]
     for k in ("x", "y", "r", "m"):
         np.testing.assert_array_equal(a[k], b[k])
+
+
+def test_bumpy_packing_matches_oracle():
+    from oracle.oracle import bumpy_packing as oracle_bumpy
+    from dpcuda_gb300.init import bumpy_packing
+    a, b = bumpy_packing(256, 0.80, 5), oracle_bumpy(256, 0.80, 5)
+    assert a["box"] == b["box"] and a["rv"] == b["rv"] and a["e_c"] == b["e_c"]
+    for k in ("x", "y", "th", "r", "nvb"):
+        np.testing.assert_array_equal(a[k], b[k])
