@@ -50,10 +50,12 @@ CUT_MULT = 1.7 / 1.4        # r_c = d_max + skin 0.3
 MAX_STEPS = 1_000_000
 FIRE_ALPHA0, FIRE_DT0 = 0.1, 1e-2
 L2_FLUSH_BYTES = 512 << 20
-BATCH = 8                   # systems per step of the batched form
+BATCH = 16                  # systems per step of the batched form
 CUTOFF, SKIN = 1.7, 0.3     # neighbour cutoff d_max + skin, and the skin
 SWITCH_FMAX = 1e-6          # mixed systems switch to FP64 pair forces below this max|F|
 PLAIN_SOLVES = 2            # timed solves of the plain FP64 path (after one untimed)
+WARMUP_ITERS = 2000         # FIRE iterations of a warm-up solve
+E2E_STEPS = 2               # batches timed end to end through host buffers
 PROFILE_ITERS = 300
 
 
@@ -84,6 +86,8 @@ def workload_config():
             "form": f"mixed precision (FP32 pairs, FP64 accumulation, FP64 pair refinement "
                     f"below max|F| = {SWITCH_FMAX:g}), {BATCH} systems per step",
             "l2": "flushed between steps (512 MiB write)",
+            "warmup_kind": f"bounded solves of {WARMUP_ITERS} FIRE iterations over the timed batches",
+            "e2e_steps": f"first {E2E_STEPS} timed batches",
             "seeds": f"step k on rank r: 100000*r + {BATCH}*k + 1 .. + {BATCH}"}
 
 
@@ -266,10 +270,11 @@ def run_ours(args):
         e1.synchronize()
         return out, e0.elapsed_time(e1)
 
-    # ---- inputs of every step, resident in HBM before the timed region -------
-    n_step = args.warmup + args.steps
+    # ---- inputs of every timed step, resident in HBM before the timed region --
+    # (step k >= warmup uses the seeds of step k, so the reference arm, which
+    # solves the first start of each timed step, sees the same starts)
     batches = []
-    for k in range(n_step):
+    for k in range(args.warmup, args.warmup + args.steps):
         sts = [packing(sd) for sd in step_seeds(rank, k)]
         e = dpg.Ensemble([N_PART] * BATCH, [st["box"] for st in sts], CUTOFF, SKIN,
                          precision=dpg.MIXED, switch_fmax=SWITCH_FMAX, stream=sptr)
@@ -277,13 +282,16 @@ def run_ours(args):
         batches.append((e, sts))
     torch.cuda.synchronize()
 
-    def solve_batch(e):
-        return e.minimizeFire(FIRE_ALPHA0, FIRE_DT0, 0.0, 0.0, MAX_STEPS, fmax_target=FMAX)
+    def solve_batch(e, max_steps=MAX_STEPS):
+        return e.minimizeFire(FIRE_ALPHA0, FIRE_DT0, 0.0, 0.0, max_steps, fmax_target=FMAX)
 
-    for k in range(args.warmup):
-        solve_batch(batches[k][0])
-        batches[k][0].setState(*[np.concatenate([st[c] for st in batches[k][1]])
-                                 for c in ("x", "y", "r", "m")])
+    # warm-up: W bounded solves (WARMUP_ITERS FIRE iterations each), cycling over
+    # the timed batches so that every batch has built its CUDA graph, then the
+    # initial states are put back
+    for k in range(max(args.warmup, len(batches))):
+        solve_batch(batches[k % len(batches)][0], WARMUP_ITERS)
+    for e, sts in batches:
+        e.setState(*[np.concatenate([st[c] for st in sts]) for c in ("x", "y", "r", "m")])
     torch.cuda.synchronize()
 
     # ---- headline: mixed precision, BATCH systems per step --------------------
@@ -293,8 +301,7 @@ def run_ours(args):
     torch.cuda.synchronize()
     sampler.start()
     t_wall0 = time.perf_counter()
-    for k in range(args.warmup, n_step):
-        e, _ = batches[k]
+    for e, _ in batches:
         res, ms = timed(lambda: solve_batch(e))
         ev_ms.append(ms)
         results.append(res)
@@ -315,8 +322,8 @@ def run_ours(args):
     e2e_ms = []
     h2d = BATCH * N_PART * 8 * 4   # x, y, radii, masses
     d2h = BATCH * N_PART * 8 * 4   # x, y, fx, fy
-    for k in range(args.warmup, n_step):
-        e, sts = batches[k]
+    n_e2e = min(len(batches), E2E_STEPS)
+    for e, sts in batches[:n_e2e]:
         host = [np.concatenate([st[c] for st in sts]) for c in ("x", "y", "r", "m")]
         l2_flush()
         torch.cuda.synchronize()
@@ -326,10 +333,10 @@ def run_ours(args):
         out = e.getState()
         _ = float(np.abs(out["fx"]).max())
         e2e_ms.append(1e3 * (time.perf_counter() - t0))
-    e2e_value = world * args.steps * BATCH / (max_over_ranks(float(np.sum(e2e_ms))) / 1e3)
+    e2e_value = world * n_e2e * BATCH / (max_over_ranks(float(np.sum(e2e_ms))) / 1e3)
 
     # ---- the plain FP64 drop-in on the same systems (one per call) -----------
-    plain = plain_fp64_leg(dpg, sptr, batches[args.warmup][1][:PLAIN_SOLVES + 1], timed)
+    plain = plain_fp64_leg(dpg, sptr, batches[0][1][:PLAIN_SOLVES + 1], timed)
     # error of the mixed form against the FP64 path on the same starts
     pe_mixed = [r["avg_pe"] for r in results[0][1:PLAIN_SOLVES + 1]]
     plain["mixed_vs_fp64_avg_pe_rel"] = [abs(a - b) / abs(b) for a, b in
@@ -607,6 +614,7 @@ def ncu_case(which):
 
 
 def main():
+    global BATCH
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
@@ -615,11 +623,13 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--ncu-case", choices=["fire", "nve_large", "ensemble"], default=None,
                     help="run a small fixed workload for ncu captures and exit")
+    ap.add_argument("--batch", type=int, default=BATCH, help="systems per step of the batched form")
     ap.add_argument("--jam-ensemble", action="store_true",
                     help="run the batched jamming workload instead of the default line")
     ap.add_argument("--jam-systems", type=int, default=256)
     ap.add_argument("--jam-max-compressions", type=int, default=2000)
     args = ap.parse_args()
+    BATCH = args.batch
     if args.jam_ensemble:
         jam_ensemble(args)
         return

@@ -9,7 +9,8 @@
 // system has its own cell grid, rebuilt into per-cell item lists whenever that
 // system's neighbour list is rebuilt.
 //
-// Precision.  Each system carries prec = 0 (mixed) or 1 (FP64):
+// Precision.  Each system carries prec = 0 (FP32 pairs), 2 (double-word FP32
+// pairs, the refinement) or 1 (FP64):
 //  - mixed: positions are FP64; for the pair loop each particle also keeps an
 //    FP32 offset from the centre of its cell (|offset| < 1.3 units, so the
 //    offset carries ~6e-8 absolute precision) and its cell coordinates; a pair
@@ -47,12 +48,12 @@ struct ESys {
     int ncd, cell_off;       // cell grid (ncd x ncd) and its first global cell
     int item_off;            // first slot of its cell items (systems packed in order)
     double L, cs, inv_cs;
-    float cs_f;
+    float cs_f, cs_lo;       // cs as a double word: cs_f + cs_lo
     // loop
     int phase, rebuild, prec, done;
     int vel_f32;             // velocities live in vel32 (set at the FP32 -> FP64 switch)
     int uphill, stopped, converged, pending;
-    long long iter, fire_total, rebuilds, fp64_total;
+    long long iter, fire_total, rebuilds, fp64_total, dw_total;
     double dt, alpha, last_avg_pe;
     long long ngood, nbad;
     // results of the last force pass
@@ -76,6 +77,8 @@ struct EParams {
     float cutoff2_f;
     // FIRE
     double alpha0, dt0, pe_target, pe_diff_target, fmax_target, switch_fmax;
+    int dw_ok;               // double-word refinement available (harmonic contacts, n_c = 2)
+    float ec_hi, ec_lo;      // e_c as a double word
     long long max_steps;
     // jamming
     int jam;                 // 0: plain minimisation, 1: jamming protocol
@@ -93,6 +96,7 @@ struct EDev {
     float2 *vel32, *frc32;   // FP32 phase: velocities and forces
     float *invm;             // 1 / mass
     float4 *pk;              // {offset x, offset y, radius, cell code}, offsets from ctr
+    float4 *pkl;             // low words of the offsets and radius (double-word refinement)
     float2 *oref;            // offsets at the last list build (FP32 displacement test)
     double2 *ctr;            // centre of the particle's (unwrapped) cell at the last build
     int *cellc;              // wrapped cell code (cx | cy << 16) of each slot
@@ -208,6 +212,68 @@ __device__ void e_fire_decide(const EParams &p, ESys &s, double power) {
     }
 }
 
+// ---- double-FP32 ("double-word") arithmetic for the refinement stage ----------
+// A value is hi + lo with |lo| <= ulp(hi) / 2 (~48 significant bits), computed
+// on the FP32 pipe, which GB300 runs ~64x faster than FP64.  Building blocks:
+// Knuth's TwoSum and Fast2Sum, the FMA-based TwoProduct, and the double-word
+// sum / product / quotient / square root of Joldes, Muller and Popescu, "Tight
+// and rigorous error bounds for basic building blocks of double-word
+// arithmetic" (ACM TOMS 44(2), 2017), relative errors of a few 2^-48.
+struct dw {
+    float hi, lo;
+};
+
+__device__ __forceinline__ dw two_sum(float a, float b) {
+    float s = __fadd_rn(a, b), bb = __fsub_rn(s, a);
+    float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return {s, e};
+}
+__device__ __forceinline__ dw fast_two_sum(float a, float b) {  // |a| >= |b|
+    float s = __fadd_rn(a, b);
+    return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ dw dw_add(dw x, dw y) {
+    dw s = two_sum(x.hi, y.hi), t = two_sum(x.lo, y.lo);
+    float c = __fadd_rn(s.lo, t.hi);
+    dw v = fast_two_sum(s.hi, c);
+    float w = __fadd_rn(t.lo, v.lo);
+    return fast_two_sum(v.hi, w);
+}
+__device__ __forceinline__ dw dw_neg(dw x) { return {-x.hi, -x.lo}; }
+__device__ __forceinline__ dw dw_mul(dw x, dw y) {
+    float ch = __fmul_rn(x.hi, y.hi);
+    float cl = __fmaf_rn(x.hi, y.hi, -ch);
+    float tl = __fmul_rn(x.hi, y.lo);
+    cl = __fadd_rn(cl, __fmaf_rn(x.lo, y.hi, tl));
+    return fast_two_sum(ch, cl);
+}
+__device__ __forceinline__ dw dw_mul_f(dw x, float y) {
+    float ch = __fmul_rn(x.hi, y);
+    float cl = __fmaf_rn(x.hi, y, -ch);
+    cl = __fmaf_rn(x.lo, y, cl);
+    return fast_two_sum(ch, cl);
+}
+__device__ __forceinline__ dw dw_div(dw x, dw y) {
+    float q = __fdiv_rn(x.hi, y.hi);
+    dw r = dw_add(x, dw_neg(dw_mul_f(y, q)));  // remainder x - q y
+    float q2 = __fdiv_rn(r.hi, y.hi);
+    return fast_two_sum(q, q2);
+}
+__device__ __forceinline__ dw dw_sqrt(dw x) {
+    float s = __fsqrt_rn(x.hi);
+    float p = __fmul_rn(s, s), pe = __fmaf_rn(s, s, -p);
+    float r = __fadd_rn(__fsub_rn(__fsub_rn(x.hi, p), pe), x.lo);
+    return fast_two_sum(s, __fdiv_rn(r, __fmul_rn(2.0f, s)));
+}
+__device__ __forceinline__ bool dw_ge(dw a, dw b) { return a.hi > b.hi || (a.hi == b.hi && a.lo >= b.lo); }
+__device__ __forceinline__ double dw_to_double(dw a) { return (double)a.hi + (double)a.lo; }
+
+// split an FP64 value into a double word
+__device__ __forceinline__ dw dw_from_double(double v) {
+    float h = (float)v;
+    return {h, (float)(v - (double)h)};
+}
+
 // ---- FP64 reciprocal and reciprocal square root for the refinement stage ----
 // Newton-Raphson iteration on an FP32 estimate: y <- y (1.5 - 0.5 x y^2) for
 // x^-1/2 and y <- y (2 - x y) for x^-1; each step doubles the number of
@@ -263,13 +329,13 @@ __global__ void __launch_bounds__(kEB) e_move(EDev *e) {
     ESys &s = e->sys[sid];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool live = s.phase == kMinimize;
-    const bool f32 = s.prec == 0;
+    const bool f32 = s.prec != 1;
     double v[1] = {0.0};
     float vf[1] = {0.f};
     if (live && i < s.off + s.n) {
         double2 x = e->pos[i];
         const double2 c = e->ctr[i];
-        if (s.prec == 0) {
+        if (s.prec != 1) {
             const float dt = (float)s.dt, alpha = (float)s.alpha;
             float2 u = e->vel32[i];
             const float2 f = e->frc32[i];
@@ -287,8 +353,12 @@ __global__ void __launch_bounds__(kEB) e_move(EDev *e) {
             x.x += (double)(u.x * dt);
             x.y += (double)(u.y * dt);
             e->pos[i] = x;
-            const float2 o = make_float2((float)(x.x - c.x), (float)(x.y - c.y));
+            const double ox = x.x - c.x, oy = x.y - c.y;
+            const float2 o = make_float2((float)ox, (float)oy);
             *reinterpret_cast<float2 *>(&e->pk[i]) = o;
+            if (s.prec == 2)  // low words for the double-word pair arithmetic
+                *reinterpret_cast<float2 *>(&e->pkl[i]) =
+                    make_float2((float)(ox - (double)o.x), (float)(oy - (double)o.y));
             const float2 r = e->oref[i];
             const float ddx = o.x - r.x, ddy = o.y - r.y;
             vf[0] = ddx * ddx + ddy * ddy;
@@ -359,7 +429,10 @@ __global__ void __launch_bounds__(kEB) e_cell_count(EDev *e) {
     e->cellc[i] = code;
     double2 c = make_double2((fx + 0.5) * s.cs, (fy + 0.5) * s.cs);
     e->ctr[i] = c;
-    e->pk[i] = make_float4((float)(x.x - c.x), (float)(x.y - c.y), (float)e->rad[i], __int_as_float(code));
+    const double ox = x.x - c.x, oy = x.y - c.y, r = e->rad[i];
+    const float hx = (float)ox, hy = (float)oy, hr = (float)r;
+    e->pk[i] = make_float4(hx, hy, hr, __int_as_float(code));
+    e->pkl[i] = make_float4((float)(ox - (double)hx), (float)(oy - (double)hy), (float)(r - (double)hr), 0.f);
     atomicAdd(&e->cell_cnt[s.cell_off + cx + cy * s.ncd], 1);
 }
 
@@ -537,6 +610,7 @@ __device__ void e_force_epilogue(EDev *e, ESys &s, const double (&v)[5], bool se
     double avg = s.pe / (double)s.n;
     s.fire_total++;
     if (s.prec == 1) s.fp64_total++;
+    else if (s.prec == 2) s.dw_total++;
     bool finished = false;
     if (setup) {
         s.last_avg_pe = avg;
@@ -548,17 +622,27 @@ __device__ void e_force_epilogue(EDev *e, ESys &s, const double (&v)[5], bool se
         return;
     }
     double fmax = sqrt(s.fmax2);
-    // mixed systems hand over to FP64 pair arithmetic for the final refinement:
-    // at switch_fmax, when FIRE keeps going uphill, or when max|F| stalls
-    if (s.prec == 0) {
+    const int pass_prec = s.prec;  // the arithmetic of this force pass
+    // mixed systems hand over to the refinement at switch_fmax, when FIRE
+    // keeps going uphill, or when max|F| stalls near the threshold: first to
+    // double-word FP32 pairs, then, at the target, to FP64, which verifies the
+    // residual (only an FP64 state passes the stop tests)
+    if (s.prec != 1) {
         if (s.fmax2 < 0.81 * s.best_f2) {
             s.best_f2 = s.fmax2;
             s.best_it = s.iter;
         }
-        const bool stalled = fmax < 100.0 * p.switch_fmax && s.iter - s.best_it > kStallIters;
-        if (fmax <= p.switch_fmax || s.nbad > 5 || stalled) {
-            s.prec = 1;
-            s.vel_f32 = 1;  // the next move takes the FP32 velocities over
+        const double exit_f = s.prec == 0 ? p.switch_fmax : (p.fmax_target > 0 ? p.fmax_target : 1e-10);
+        const bool stalled = fmax < 100.0 * exit_f && s.iter - s.best_it > kStallIters;
+        if (fmax <= exit_f || s.nbad > 5 || stalled) {
+            if (s.prec == 0 && p.dw_ok) {
+                s.prec = 2;
+                s.best_f2 = s.fmax2;
+                s.best_it = s.iter;
+            } else {
+                s.prec = 1;
+                s.vel_f32 = 1;  // the next move takes the FP32 velocities over
+            }
         }
     }
     double diff = fabs(avg / s.last_avg_pe - 1);
@@ -567,8 +651,8 @@ __device__ void e_force_epilogue(EDev *e, ESys &s, const double (&v)[5], bool se
     const bool decompressing = p.jam && s.jam_stage == 0;
     const double pe_t = decompressing ? 1e-16 : p.pe_target;
     const double pe_dt = decompressing ? 0.0 : p.pe_diff_target;
-    if (avg < pe_t || (s.prec == 1 && diff < pe_dt)) finished = true;
-    else if (p.fmax_target > 0 && fmax <= p.fmax_target && s.prec == 1) finished = true;
+    if (avg < pe_t || (pass_prec == 1 && diff < pe_dt)) finished = true;
+    else if (p.fmax_target > 0 && fmax <= p.fmax_target && pass_prec == 1) finished = true;
     else if (it + 1 >= p.max_steps) finished = true;
     else {
         s.iter = it + 1;
@@ -636,7 +720,9 @@ __global__ void __launch_bounds__(kEB) e_force(EDev *e) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool live = s.phase != kIdle;
     const bool setup = s.phase == kSetup;
-    // partials: 0 PE, 1 power, 2 max|F|^2, 3 virial, 4 contacts
+    // partials: 0 PE, 1 power, 2 max|F|^2, 3 virial, 4 contacts (FP32 block
+    // sums in the FP32 phase; FP64 in the refinement, whose energies are exact
+    // to ~1e-14 and are the ones reported)
     const bool f32 = s.prec == 0;
     double v[5] = {0, 0, 0, 0, 0};
     float vf[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
@@ -645,29 +731,75 @@ __global__ void __launch_bounds__(kEB) e_force(EDev *e) {
         int cnt = min(e->cnt[i], p.cap);
         double ax = 0.0, ay = 0.0, en = 0.0, wv = 0.0, nc = 0.0;
         const float4 a = e->pk[i];
-        if (s.prec == 0) {
-            // FP32 pair terms summed in FP32 over runs of 8 neighbours, FP64 across runs
-            const float ecf = (float)p.e_c, ncf = (float)p.n_c;
+        if (s.prec != 1) {
             int ncount = 0;
-            for (int k0 = 0; k0 < cnt; k0 += 8) {
-                float sx = 0.f, sy = 0.f, se = 0.f, sw = 0.f;
-                const int k1 = min(cnt, k0 + 8);
-                for (int k = k0; k < k1; k++) {
-                    int j = __ldg(&e->nbr[(size_t)k * T + i]);
-                    float4 b = e->pk[j];
-                    float fx, fy, ef, wf;
-                    int ct;
-                    pair_f32(a, b, s.ncd, s.cs_f, ecf, ncf, fx, fy, ef, wf, ct);
-                    sx += fx;
-                    sy += fy;
-                    se += ef;
-                    sw += wf;
-                    ncount += ct;
+            if (s.prec == 0) {
+                // FP32 pair terms summed in FP32 over runs of 8 neighbours, FP64 across runs;
+                // the 8 indices and offsets of a run are loaded before any is used
+                const float ecf = (float)p.e_c, ncf = (float)p.n_c;
+                for (int k0 = 0; k0 < cnt; k0 += 8) {
+                    float sx = 0.f, sy = 0.f, se = 0.f, sw = 0.f;
+                    int jj[8];
+                    float4 bb[8];
+#pragma unroll
+                    for (int u = 0; u < 8; u++) jj[u] = k0 + u < cnt ? __ldg(&e->nbr[(size_t)(k0 + u) * T + i]) : i;
+#pragma unroll
+                    for (int u = 0; u < 8; u++) bb[u] = e->pk[jj[u]];
+#pragma unroll
+                    for (int u = 0; u < 8; u++) {
+                        if (k0 + u >= cnt) break;
+                        float fx, fy, ef, wf;
+                        int ct;
+                        pair_f32(a, bb[u], s.ncd, s.cs_f, ecf, ncf, fx, fy, ef, wf, ct);
+                        sx += fx;
+                        sy += fy;
+                        se += ef;
+                        sw += wf;
+                        ncount += ct;
+                    }
+                    ax += (double)sx;
+                    ay += (double)sy;
+                    en += (double)se;
+                    wv += (double)sw;
                 }
-                ax += (double)sx;
-                ay += (double)sy;
-                en += (double)se;
-                wv += (double)sw;
+            } else {
+                // double-word FP32 pairs for the contacts the FP32 offsets cannot rule out
+                const float4 al = e->pkl[i];
+                const dw xi = {a.x, al.x}, yi = {a.y, al.y}, ri = {a.z, al.z};
+                const dw csd = {s.cs_f, s.cs_lo}, ec = {p.ec_hi, p.ec_lo};
+                dw sx = {0.f, 0.f}, sy = {0.f, 0.f}, se = {0.f, 0.f};
+                float sw = 0.f;
+                const int ca = __float_as_int(a.w);
+                for (int k = 0; k < cnt; k++) {
+                    int j = __ldg(&e->nbr[(size_t)k * T + i]);
+                    const float4 b = e->pk[j];
+                    const int cb = __float_as_int(b.w);
+                    int dcx = code_x(ca) - code_x(cb), dcy = code_y(ca) - code_y(cb);
+                    if (dcx > s.ncd / 2) dcx -= s.ncd; else if (dcx < -(s.ncd / 2)) dcx += s.ncd;
+                    if (dcy > s.ncd / 2) dcy -= s.ncd; else if (dcy < -(s.ncd / 2)) dcy += s.ncd;
+                    const float dxf = (a.x - b.x) + (float)dcx * s.cs_f;
+                    const float dyf = (a.y - b.y) + (float)dcy * s.cs_f;
+                    const float rsf = a.z + b.z;
+                    if (dxf * dxf + dyf * dyf >= rsf * rsf * 1.0001f) continue;
+                    const float4 bl = e->pkl[j];
+                    dw dx = dw_add(dw_add(xi, dw_neg(dw{b.x, bl.x})), dw_mul_f(csd, (float)dcx));
+                    dw dy = dw_add(dw_add(yi, dw_neg(dw{b.y, bl.y})), dw_mul_f(csd, (float)dcy));
+                    dw rs = dw_add(ri, dw{b.z, bl.z});
+                    dw d2 = dw_add(dw_mul(dx, dx), dw_mul(dy, dy));
+                    if (dw_ge(d2, dw_mul(rs, rs))) continue;
+                    dw d = dw_sqrt(d2);
+                    dw ov = dw_add(dw{1.f, 0.f}, dw_neg(dw_div(d, rs)));
+                    dw fm = dw_div(dw_mul(ec, ov), dw_mul(rs, d));
+                    sx = dw_add(sx, dw_mul(fm, dx));
+                    sy = dw_add(sy, dw_mul(fm, dy));
+                    se = dw_add(se, dw_mul_f(dw_mul(ec, dw_mul(ov, ov)), 0.25f));
+                    sw += fm.hi * (dx.hi * dx.hi + dy.hi * dy.hi);
+                    ncount++;
+                }
+                ax = dw_to_double(sx);
+                ay = dw_to_double(sy);
+                en = dw_to_double(se);
+                wv = (double)sw;
             }
             const float2 fv = make_float2((float)ax, (float)ay);
             e->frc[i] = make_double2(ax, ay);
@@ -679,11 +811,19 @@ __global__ void __launch_bounds__(kEB) e_force(EDev *e) {
                 u.y += fv.y * h;
                 e->vel32[i] = u;
             }
-            vf[0] = (float)en;
-            vf[1] = fv.x * u.x + fv.y * u.y;
-            vf[2] = fv.x * fv.x + fv.y * fv.y;
-            vf[3] = (float)wv;
-            vf[4] = (float)ncount;
+            if (f32) {
+                vf[0] = (float)en;
+                vf[1] = fv.x * u.x + fv.y * u.y;
+                vf[2] = fv.x * fv.x + fv.y * fv.y;
+                vf[3] = (float)wv;
+                vf[4] = (float)ncount;
+            } else {
+                v[0] = en;
+                v[1] = ax * (double)u.x + ay * (double)u.y;
+                v[2] = ax * ax + ay * ay;
+                v[3] = wv;
+                v[4] = (double)ncount;
+            }
         } else {
             // FP64 pair arithmetic for pairs that the FP32 offsets cannot rule
             // out (a 1e-4 relative margin on the contact distance)
@@ -775,6 +915,7 @@ __global__ void __launch_bounds__(kEB) e_transition(EDev *e) {
         s.cs = s.L / s.ncd;
         s.inv_cs = s.ncd / s.L;
         s.cs_f = (float)s.cs;
+        s.cs_lo = (float)(s.cs - (double)s.cs_f);
         s.pending = kActNone;
         s.phase = kSetup;
         s.rebuild = 1;

@@ -112,6 +112,7 @@ extern "C" int dpg_ensemble_create(const dpg_ensemble_params *p, const int64_t *
         y.cs = y.L / y.ncd;
         y.inv_cs = y.ncd / y.L;
         y.cs_f = (float)y.cs;
+        y.cs_lo = (float)(y.cs - (double)y.cs_f);
         y.jam_status = -1;
         y.L_low = y.L_high = y.L_last = -1;
         for (int i = 0; i < y.nblk * kEB; i++) s->src_index.push_back(i < y.n ? (int)(in + i) : -1);
@@ -139,7 +140,7 @@ extern "C" int dpg_ensemble_create(const dpg_ensemble_params *p, const int64_t *
     A((void **)&h.rad, 8 * T); A((void **)&h.mass, 8 * T); A((void **)&h.pe, 8 * T);
     A((void **)&h.pk, 16 * T); A((void **)&h.cellc, 4 * T);
     A((void **)&h.vel32, 8 * T); A((void **)&h.frc32, 8 * T); A((void **)&h.invm, 4 * T);
-    A((void **)&h.oref, 8 * T); A((void **)&h.ctr, 16 * T);
+    A((void **)&h.oref, 8 * T); A((void **)&h.ctr, 16 * T); A((void **)&h.pkl, 16 * T);
     A((void **)&h.cnt, 4 * T);
     A((void **)&h.cell_cnt, 4 * ((size_t)s->total_cells + 1));
     A((void **)&h.cell_start, 4 * ((size_t)s->total_cells + 1));
@@ -157,6 +158,9 @@ extern "C" int dpg_ensemble_create(const dpg_ensemble_params *p, const int64_t *
     h.p.cutoff2_f = (float)h.p.cutoff2;
     h.p.half_skin2 = (p->skin / 2) * (p->skin / 2);
     h.p.switch_fmax = p->precision == DPG_MIXED ? (p->switch_fmax > 0 ? p->switch_fmax : 1e-6) : 0.0;
+    h.p.dw_ok = p->n_c == 2.0 ? 1 : 0;
+    h.p.ec_hi = (float)p->e_c;
+    h.p.ec_lo = (float)(p->e_c - (double)h.p.ec_hi);
     std::vector<int> bs(s->nblocks);
     for (int k = 0; k < s->S; k++)
         for (int b = 0; b < s->sys[k].nblk; b++) bs[s->sys[k].blk0 + b] = k;
@@ -382,7 +386,7 @@ static int prepare(ES *s, const dpg_fire_params *fp, int jam, const dpg_jam_para
         y.jam_stage = 0; y.jam_status = -1; y.jam_step = 0;
         y.L_low = y.L_high = y.L_last = -1; y.L_saved = -1; y.scale = 1.0; y.rebuilds = 0;
         y.ticket_a = y.ticket_b = 0;
-        y.best_f2 = INFINITY; y.best_it = 0; y.vel_f32 = 0; y.fp64_total = 0;
+        y.best_f2 = INFINITY; y.best_it = 0; y.vel_f32 = 0; y.fp64_total = 0; y.dw_total = 0;
     }
     CK(cudaMemcpyAsync(s->d_sys, s->sys.data(), sizeof(ESys) * s->S, cudaMemcpyHostToDevice, s->stream));
     CK(cudaMemcpyAsync(&s->d->p, &p, sizeof(EParams), cudaMemcpyHostToDevice, s->stream));
@@ -419,6 +423,7 @@ static void fill_results(ES *s, dpg_ensemble_result *r) {
         o.minimizations = y.minimizations;
         o.rebuilds = y.rebuilds;
         o.fp64_steps = y.fp64_total;
+        o.dw_steps = y.dw_total;
         o.status = y.jam_status;
         o.converged = y.converged;
         o.packing_fraction = 0.0;  // filled by the caller, who knows the radii
@@ -442,11 +447,15 @@ extern "C" int dpg_ensemble_jam(dpg_ensemble s, const dpg_jam_params *p, dpg_ens
 
 extern "C" int dpg_ensemble_compute_forces(dpg_ensemble s, int precision, dpg_ensemble_result *r) {
     if (!s) return set_err(DPG_ERR_ARG, "null handle");
-    if (precision != DPG_FP64 && precision != DPG_MIXED) return set_err(DPG_ERR_ARG, "bad precision");
+    if (precision != DPG_FP64 && precision != DPG_MIXED && precision != DPG_DWORD)
+        return set_err(DPG_ERR_ARG, "bad precision");
+    if (precision == DPG_DWORD && s->h.p.dw_ok == 0)
+        return set_err(DPG_ERR_ARG, "double-word pairs need harmonic contacts (n_c = 2)");
     const dpg_fire_params fp = {0.1, 1e-2, 0.0, 0.0, 1, 0.0};
     for (int attempt = 0; attempt < 8; attempt++) {
         TRY(prepare(s, &fp, 0, nullptr));
-        for (auto &y : s->sys) y.prec = (precision == DPG_MIXED && y.ncd >= 3) ? 0 : 1;
+        for (auto &y : s->sys)
+            y.prec = y.ncd < 3 ? 1 : (precision == DPG_MIXED ? 0 : (precision == DPG_DWORD ? 2 : 1));
         CK(cudaMemcpyAsync(s->d_sys, s->sys.data(), sizeof(ESys) * s->S, cudaMemcpyHostToDevice, s->stream));
         TRY(put(s, &s->d->n_flagged, 1));
         TRY(enqueue_rebuild(s));

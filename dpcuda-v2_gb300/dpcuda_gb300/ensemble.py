@@ -12,7 +12,7 @@ from .disk import _METHODS
 from .lib import (DP, EnsembleParams, EnsembleResult, FireParams, I64P, JamParams, NeighborConfig,
                   check, load_library)
 
-FP64, MIXED = 0, 1
+FP64, MIXED, DWORD = 0, 1, 2
 
 
 class Ensemble:
@@ -64,7 +64,8 @@ class Ensemble:
                             box_length=r.box_length, contacts=r.contacts,
                             packing_fraction=area / r.box_length ** 2, fire_steps=r.fire_steps,
                             minimizations=r.minimizations, rebuilds=r.rebuilds, status=r.status,
-                            converged=r.converged, fp64_steps=r.fp64_steps))
+                            converged=r.converged, fp64_steps=r.fp64_steps,
+                            dw_steps=r.dw_steps))
         return out
 
     def calculateForces(self, precision=FP64):

@@ -84,7 +84,8 @@ class EnsembleParams(C.Structure):
 class EnsembleResult(C.Structure):
     _fields_ = [("avg_pe", D), ("max_force", D), ("pressure", D), ("packing_fraction", D),
                 ("box_length", D), ("contacts", D), ("fire_steps", I64), ("minimizations", I64),
-                ("rebuilds", I64), ("status", I32), ("converged", I32), ("fp64_steps", I64)]
+                ("rebuilds", I64), ("status", I32), ("converged", I32), ("fp64_steps", I64),
+                ("dw_steps", I64)]
 
 
 # name -> argtypes (all return int status unless listed in _RESTYPES)

@@ -51,6 +51,8 @@ extern "C" {
 /* precision forms */
 #define DPG_FP64 0  /* plain all-FP64 drop-in */
 #define DPG_MIXED 1 /* FP64 cell origin + FP32 offsets, FP32 pair maths, FP64 accumulation */
+#define DPG_DWORD 2 /* dpg_ensemble_compute_forces only: the double-word FP32 pair
+                       arithmetic of the mixed form's refinement stage */
 
 typedef struct dpg_system *dpg_handle;
 
@@ -408,7 +410,8 @@ typedef struct {
     int64_t rebuilds;
     int status;             /* jamming: 0 final state, 1 length tolerance, 2 out of steps */
     int converged;
-    int64_t fp64_steps;     /* force passes with FP64 pair arithmetic (mixed: the refinement) */
+    int64_t fp64_steps;     /* force passes with FP64 pair arithmetic (mixed: the final check) */
+    int64_t dw_steps;       /* force passes with double-word FP32 pairs (mixed: the refinement) */
 } dpg_ensemble_result;
 
 /* n_particles[s], box[s] (square boxes) */
@@ -425,7 +428,8 @@ int dpg_ensemble_fire_minimize(dpg_ensemble e, const dpg_fire_params *p, dpg_ens
  * lists rebuilt first): forces readable with dpg_ensemble_get_state, and
  * per-system avg_pe, max_force, pressure and contacts in per_system (may be
  * NULL).  precision DPG_FP64 uses the reference pair arithmetic, DPG_MIXED
- * the FP32 pair forces (systems with fewer than 3 cells a side use FP64).
+ * the FP32 pair forces, DPG_DWORD the double-word FP32 pairs of the
+ * refinement (systems with fewer than 3 cells a side use FP64).
  * Disk::calculateForces (src/particles/disk/disk.cu:218-221) for a batch. */
 int dpg_ensemble_compute_forces(dpg_ensemble e, int precision, dpg_ensemble_result *per_system);
 /* pressure-band jamming of every system (the dpg_jam_pressure control flow) */

@@ -61,6 +61,9 @@ def test_ensemble_forces_match_plain_path(dpg):
     g64 = e.getState()
     res32 = e.calculateForces(dpg.MIXED)
     g32 = e.getState()
+    from dpcuda_gb300.ensemble import DWORD
+    resdw = e.calculateForces(DWORD)
+    gdw = e.getState()
     for k, st in enumerate(sts):
         s = single(dpg, st)
         s.zeroForceAndPotentialEnergy()
@@ -72,9 +75,13 @@ def test_ensemble_forces_match_plain_path(dpg):
                                        err_msg=f"FP64 {c} n={sizes[k]}")
             np.testing.assert_allclose(split(e, g32[c])[k], want[c], rtol=0, atol=1e-5 * scale,
                                        err_msg=f"mixed {c} n={sizes[k]}")
+            # double-word FP32 (~48 bits): the refinement's forces
+            np.testing.assert_allclose(split(e, gdw[c])[k], want[c], rtol=0, atol=1e-12 * scale,
+                                       err_msg=f"double-word {c} n={sizes[k]}")
         pe = s.totalPotentialEnergy() / sizes[k]
         np.testing.assert_allclose(res64[k]["avg_pe"], pe, rtol=1e-12)
         np.testing.assert_allclose(res32[k]["avg_pe"], pe, rtol=1e-5)
+        np.testing.assert_allclose(resdw[k]["avg_pe"], pe, rtol=1e-11)
         np.testing.assert_allclose(res64[k]["pressure"], s.getPressure(), rtol=1e-12)
         assert res64[k]["contacts"] == s.getContactCount()
         s.close()
