@@ -585,6 +585,17 @@ def ncu_case(which):
     iterations of the batched mixed form on 8 x 16384 disks."""
     os.environ["DPG_LOOP_MODE"] = "stream"
     import dpcuda_gb300 as dpg
+    if which == "ensemble_forces":
+        # one force pass per arithmetic (FP32, double-word, FP64) on 8 x 16384 disks
+        from dpcuda_gb300.ensemble import DWORD
+        sts = [packing(sd) for sd in step_seeds(0, 0)[:8]]
+        e = dpg.Ensemble([N_PART] * 8, [st["box"] for st in sts], CUTOFF, SKIN,
+                         precision=dpg.MIXED, switch_fmax=SWITCH_FMAX)
+        e.setState(*[np.concatenate([st[c] for st in sts]) for c in ("x", "y", "r", "m")])
+        for prec in (dpg.MIXED, DWORD, dpg.FP64, dpg.MIXED, DWORD, dpg.FP64):
+            e.calculateForces(prec)
+        print(json.dumps({"ncu_case": which, "passes": 6}))
+        return
     if which == "ensemble":
         sts = [packing(sd) for sd in step_seeds(0, 0)]
         e = dpg.Ensemble([N_PART] * BATCH, [st["box"] for st in sts], CUTOFF, SKIN,
@@ -621,7 +632,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--ncu-case", choices=["fire", "nve_large", "ensemble"], default=None,
+    ap.add_argument("--ncu-case", choices=["fire", "nve_large", "ensemble", "ensemble_forces"],
+                    default=None,
                     help="run a small fixed workload for ncu captures and exit")
     ap.add_argument("--batch", type=int, default=BATCH, help="systems per step of the batched form")
     ap.add_argument("--jam-ensemble", action="store_true",
