@@ -55,7 +55,6 @@ CUTOFF, SKIN = 1.7, 0.3     # neighbour cutoff d_max + skin, and the skin
 SWITCH_FMAX = 1e-6          # mixed systems switch to FP64 pair forces below this max|F|
 PLAIN_SOLVES = 2            # timed solves of the plain FP64 path (after one untimed)
 WARMUP_ITERS = 2000         # FIRE iterations of a warm-up solve
-E2E_STEPS = 2               # batches timed end to end through host buffers
 PROFILE_ITERS = 300
 
 
@@ -87,7 +86,7 @@ def workload_config():
                     f"below max|F| = {SWITCH_FMAX:g}), {BATCH} systems per step",
             "l2": "flushed between steps (512 MiB write)",
             "warmup_kind": f"bounded solves of {WARMUP_ITERS} FIRE iterations over the timed batches",
-            "e2e_steps": f"first {E2E_STEPS} timed batches",
+            "e2e_steps": "the same batches as the timed steps, solved again from host arrays",
             "seeds": f"step k on rank r: 100000*r + {BATCH}*k + 1 .. + {BATCH}"}
 
 
@@ -322,8 +321,8 @@ def run_ours(args):
     e2e_ms = []
     h2d = BATCH * N_PART * 8 * 4   # x, y, radii, masses
     d2h = BATCH * N_PART * 8 * 4   # x, y, fx, fy
-    n_e2e = min(len(batches), E2E_STEPS)
-    for e, sts in batches[:n_e2e]:
+    n_e2e = len(batches)
+    for e, sts in batches:
         host = [np.concatenate([st[c] for st in sts]) for c in ("x", "y", "r", "m")]
         l2_flush()
         torch.cuda.synchronize()
@@ -357,8 +356,9 @@ def run_ours(args):
                 "frac": achieved / peak, "traffic": None, "kernel": "e_force",
                 "peak_source": peak_src, "bytes_per_launch": bytes_force,
                 "launch_us": prof["force_us"], "profile_us_per_iter": prof,
-                "note": "8 x 16384 disks, FP32 pair phase; working set (25 MB) is L2-resident, "
-                        "so the kernel is latency/L2-bound, not HBM-bound"}
+                "note": f"{BATCH} x 16384 disks, first {PROFILE_ITERS} FIRE iterations (FP32 pair "
+                        f"phase); the working set ({BATCH * 16384 * 200 / 1e6:.0f} MB) is L2-resident, "
+                        "so the kernel is bound by latency and the FP64 pipe, not by HBM"}
 
     # ---- large-N force kernel (N = 2^20 NVE, plain FP64) -----------------------
     large = large_n_roofline(dpg, dev, sptr, peak)
