@@ -322,13 +322,14 @@ def run_ours(args):
     h2d = BATCH * N_PART * 8 * 4   # x, y, radii, masses
     d2h = BATCH * N_PART * 8 * 4   # x, y, fx, fy
     n_e2e = len(batches)
+    e2e_results = []
     for e, sts in batches:
         host = [np.concatenate([st[c] for st in sts]) for c in ("x", "y", "r", "m")]
         l2_flush()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         e.setState(*host)
-        solve_batch(e)
+        e2e_results.append(solve_batch(e))
         out = e.getState()
         _ = float(np.abs(out["fx"]).max())
         e2e_ms.append(1e3 * (time.perf_counter() - t0))
@@ -336,10 +337,32 @@ def run_ours(args):
 
     # ---- the plain FP64 drop-in on the same systems (one per call) -----------
     plain = plain_fp64_leg(dpg, sptr, batches[0][1][:PLAIN_SOLVES + 1], timed)
-    # error of the mixed form against the FP64 path on the same starts
-    pe_mixed = [r["avg_pe"] for r in results[0][1:PLAIN_SOLVES + 1]]
-    plain["mixed_vs_fp64_avg_pe_rel"] = [abs(a - b) / abs(b) for a, b in
-                                         zip(pe_mixed, plain["avg_pe"])]
+
+    # ---- error of the mixed form: its minima re-evaluated by the FP64 path ----
+    # (the FP64 path is bit-identical to the reference arithmetic; the two forms
+    # reach different minima from the same start, so the check is done at the
+    # mixed form's own final positions)
+    e, sts = batches[0]
+    fin = e.getState()
+    checks, off = [], 0
+    for k, st in enumerate(sts[:4]):
+        xs, ys = fin["x"][off:off + N_PART], fin["y"][off:off + N_PART]
+        off += N_PART
+        d = dpg.Disk(N_PART, st["box"], stream=sptr)
+        d.setState(xs, ys, None, None, st["r"], st["m"])
+        d.setupNeighbors("cell", CUT_MULT, 0.2, 8.0, 0.5)
+        d.zeroForceAndPotentialEnergy()
+        d.calculateForces()
+        g = d.getState()
+        f64 = float(np.sqrt(g["fx"] ** 2 + g["fy"] ** 2).max())
+        pe64 = d.totalPotentialEnergy() / N_PART
+        r = e2e_results[0][k]  # the last solve of this batch
+        checks.append({"max_force_fp64": f64, "max_force_reported": r["max_force"],
+                       "avg_pe_fp64": pe64, "avg_pe_reported": r["avg_pe"],
+                       "avg_pe_rel_diff": abs(r["avg_pe"] - pe64) / pe64})
+        d.close()
+    mixed_check = {"systems": len(checks), "max_force_fp64_max": max(c["max_force_fp64"] for c in checks),
+                   "avg_pe_rel_diff_max": max(c["avg_pe_rel_diff"] for c in checks), "detail": checks}
 
     # ---- roofline of the dominant kernel of the headline form ----------------
     peak, peak_src = measured_peak_hbm()
@@ -389,6 +412,7 @@ def run_ours(args):
                           "max_force": float(max(r["max_force"] for r in flat)),
                           "wall_s_timed": t_wall,
                           "plain_fp64": plain,
+                          "mixed_minima_checked_in_fp64": mixed_check,
                           "mixed_batched_over_plain_fp64": value / plain["value"],
                           "roofline_large": large, "other_workloads": others}}
         print(json.dumps(line), flush=True)
