@@ -770,31 +770,51 @@ __global__ void __launch_bounds__(kEB) e_force(EDev *e) {
                 dw sx = {0.f, 0.f}, sy = {0.f, 0.f}, se = {0.f, 0.f};
                 float sw = 0.f;
                 const int ca = __float_as_int(a.w);
-                for (int k = 0; k < cnt; k++) {
-                    int j = __ldg(&e->nbr[(size_t)k * T + i]);
-                    const float4 b = e->pk[j];
-                    const int cb = __float_as_int(b.w);
-                    int dcx = code_x(ca) - code_x(cb), dcy = code_y(ca) - code_y(cb);
-                    if (dcx > s.ncd / 2) dcx -= s.ncd; else if (dcx < -(s.ncd / 2)) dcx += s.ncd;
-                    if (dcy > s.ncd / 2) dcy -= s.ncd; else if (dcy < -(s.ncd / 2)) dcy += s.ncd;
-                    const float dxf = (a.x - b.x) + (float)dcx * s.cs_f;
-                    const float dyf = (a.y - b.y) + (float)dcy * s.cs_f;
-                    const float rsf = a.z + b.z;
-                    if (dxf * dxf + dyf * dyf >= rsf * rsf * 1.0001f) continue;
-                    const float4 bl = e->pkl[j];
-                    dw dx = dw_add(dw_add(xi, dw_neg(dw{b.x, bl.x})), dw_mul_f(csd, (float)dcx));
-                    dw dy = dw_add(dw_add(yi, dw_neg(dw{b.y, bl.y})), dw_mul_f(csd, (float)dcy));
-                    dw rs = dw_add(ri, dw{b.z, bl.z});
-                    dw d2 = dw_add(dw_mul(dx, dx), dw_mul(dy, dy));
-                    if (dw_ge(d2, dw_mul(rs, rs))) continue;
-                    dw d = dw_sqrt(d2);
-                    dw ov = dw_add(dw{1.f, 0.f}, dw_neg(dw_div(d, rs)));
-                    dw fm = dw_div(dw_mul(ec, ov), dw_mul(rs, d));
-                    sx = dw_add(sx, dw_mul(fm, dx));
-                    sy = dw_add(sy, dw_mul(fm, dy));
-                    se = dw_add(se, dw_mul_f(dw_mul(ec, dw_mul(ov, ov)), 0.25f));
-                    sw += fm.hi * (dx.hi * dx.hi + dy.hi * dy.hi);
-                    ncount++;
+                // runs of 4 neighbours: indices, then packed offsets, then the
+                // low words of the candidates, each batch of loads issued together
+                for (int k0 = 0; k0 < cnt; k0 += 4) {
+                    int jj[4];
+                    float4 bb[4], bl[4];
+                    int dcx[4], dcy[4];
+                    unsigned cand = 0u;
+#pragma unroll
+                    for (int u = 0; u < 4; u++) jj[u] = k0 + u < cnt ? __ldg(&e->nbr[(size_t)(k0 + u) * T + i]) : i;
+#pragma unroll
+                    for (int u = 0; u < 4; u++) bb[u] = e->pk[jj[u]];
+#pragma unroll
+                    for (int u = 0; u < 4; u++) {
+                        const int cb = __float_as_int(bb[u].w);
+                        int cx = code_x(ca) - code_x(cb), cy = code_y(ca) - code_y(cb);
+                        if (cx > s.ncd / 2) cx -= s.ncd; else if (cx < -(s.ncd / 2)) cx += s.ncd;
+                        if (cy > s.ncd / 2) cy -= s.ncd; else if (cy < -(s.ncd / 2)) cy += s.ncd;
+                        dcx[u] = cx;
+                        dcy[u] = cy;
+                        const float dxf = (a.x - bb[u].x) + (float)cx * s.cs_f;
+                        const float dyf = (a.y - bb[u].y) + (float)cy * s.cs_f;
+                        const float rsf = a.z + bb[u].z;
+                        if (k0 + u < cnt && dxf * dxf + dyf * dyf < rsf * rsf * 1.0001f) cand |= 1u << u;
+                    }
+#pragma unroll
+                    for (int u = 0; u < 4; u++)
+                        if (cand & (1u << u)) bl[u] = e->pkl[jj[u]];
+#pragma unroll
+                    for (int u = 0; u < 4; u++) {
+                        if (!(cand & (1u << u))) continue;
+                        const float4 b = bb[u];
+                        dw dx = dw_add(dw_add(xi, dw_neg(dw{b.x, bl[u].x})), dw_mul_f(csd, (float)dcx[u]));
+                        dw dy = dw_add(dw_add(yi, dw_neg(dw{b.y, bl[u].y})), dw_mul_f(csd, (float)dcy[u]));
+                        dw rs = dw_add(ri, dw{b.z, bl[u].z});
+                        dw d2 = dw_add(dw_mul(dx, dx), dw_mul(dy, dy));
+                        if (dw_ge(d2, dw_mul(rs, rs))) continue;
+                        dw d = dw_sqrt(d2);
+                        dw ov = dw_add(dw{1.f, 0.f}, dw_neg(dw_div(d, rs)));
+                        dw fm = dw_div(dw_mul(ec, ov), dw_mul(rs, d));
+                        sx = dw_add(sx, dw_mul(fm, dx));
+                        sy = dw_add(sy, dw_mul(fm, dy));
+                        se = dw_add(se, dw_mul_f(dw_mul(ec, dw_mul(ov, ov)), 0.25f));
+                        sw += fm.hi * (dx.hi * dx.hi + dy.hi * dy.hi);
+                        ncount++;
+                    }
                 }
                 ax = dw_to_double(sx);
                 ay = dw_to_double(sy);
