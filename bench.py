@@ -55,6 +55,7 @@ CUTOFF, SKIN = 1.7, 0.3     # neighbour cutoff d_max + skin, and the skin
 SWITCH_FMAX = 1e-6          # mixed systems switch to FP64 pair forces below this max|F|
 PLAIN_SOLVES = 2            # timed solves of the plain FP64 path (after one untimed)
 WARMUP_ITERS = 2000         # FIRE iterations of a warm-up solve
+E_FORCE_DRAM_PER_SYSTEM = 10.37e6 / 8  # ncu DRAM bytes per e_force launch per 16384-disk system
 PROFILE_ITERS = 300
 
 
@@ -376,7 +377,10 @@ def run_ours(args):
     bytes_force = BATCH * N_PART * (84 + 4 * k_mean)
     achieved = bytes_force / (prof["force_us"] * 1e-6) / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": None, "kernel": "e_force",
+                "frac": achieved / peak, "traffic": E_FORCE_DRAM_PER_SYSTEM * BATCH,
+                "traffic_source": "ncu dram__bytes_read+write of one FP32-phase e_force launch on "
+                                  "8 x 16384 disks (10.37 MB), scaled to the batch by systems",
+                "kernel": "e_force",
                 "peak_source": peak_src, "bytes_per_launch": bytes_force,
                 "launch_us": prof["force_us"], "profile_us_per_iter": prof,
                 "note": f"{BATCH} x 16384 disks, first {PROFILE_ITERS} FIRE iterations (FP32 pair "
