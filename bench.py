@@ -592,6 +592,8 @@ def jam_ensemble(args):
                      "status": [r["status"] for r in res],
                      "fire_steps_max": int(max(r["fire_steps"] for r in res)),
                      "minimizations_max": int(max(r["minimizations"] for r in res))}
+        print(json.dumps({"jam_form": form, "s": dt, "systems_per_s": S / dt,
+                          "in_band": out[form]["in_band"]}), file=sys.stderr, flush=True)
         e.close()
     d = np.abs(np.array(out["mixed"]["phi"]) - np.array(out["fp64"]["phi"]))
     line = {"metric": "batched jamming: systems jammed/s, mixed vs FP64", "unit": "systems/s",
