@@ -61,3 +61,22 @@ def test_state_count_reads_the_reference_layout(tmp_path):
     assert Disk.stateCount(tmp_path) == 37
     with pytest.raises(DpgError):
         Disk.stateCount(tmp_path / "missing")
+
+
+def test_bad_arguments_rejected_before_any_device_work():
+    """dpg_create / dpg_ensemble_create check their arguments first, so bad
+    sizes, boxes and precisions fail with DPG_ERR_ARG even without a GPU."""
+    import ctypes as C
+    from dpcuda_gb300.lib import EnsembleParams, Params, load_library
+    DPG_ERR_ARG = 1  # include/dpg.h
+    lib = load_library()
+    h = C.c_void_p()
+    for prm in (Params(0, 10.0, 10.0, 1.0, 2.0, 0, 0), Params(16, -1.0, 10.0, 1.0, 2.0, 0, 0),
+                Params(16, 10.0, 10.0, 1.0, 2.0, 7, 0)):
+        assert lib.dpg_create(C.byref(prm), None, C.byref(h)) == DPG_ERR_ARG
+    n = (C.c_int64 * 1)(16)
+    box = (C.c_double * 1)(10.0)
+    for ep in (EnsembleParams(0, 1.0, 2.0, 1.7, 0.3, 0, 0, 0.0),
+               EnsembleParams(1, 1.0, 2.0, -1.0, 0.3, 0, 0, 0.0),
+               EnsembleParams(1, 1.0, 2.0, 1.7, 0.3, 5, 0, 0.0)):
+        assert lib.dpg_ensemble_create(C.byref(ep), n, box, None, C.byref(h)) == DPG_ERR_ARG
