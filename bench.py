@@ -575,8 +575,9 @@ def jam_ensemble(args):
     sizes = np.floor(np.exp(rng.uniform(np.log(64), np.log(4096), S))).astype(int)
     sts = [disk_packing(int(n), 0.80, 7000 + k) for k, n in enumerate(sizes)]
     cat = [np.concatenate([st[c] for st in sts]) for c in ("x", "y", "r", "m")]
-    band = (1e-7 - 1e-9, 1e-7 + 1e-9)
+    band = (args.jam_pressure * 0.99, args.jam_pressure * 1.01)
     fire = (0.1, 1e-2, 1e-16, 1e-16, 100000, 0.0)
+    print(json.dumps({"jam_sizes": [int(n) for n in sizes]}), file=sys.stderr, flush=True)
     out = {}
     for form, prec in (("mixed", dpg.MIXED), ("fp64", dpg.FP64)):
         e = dpg.Ensemble(sizes, [st["box"] for st in sts], CUTOFF, SKIN, precision=prec,
@@ -599,7 +600,7 @@ def jam_ensemble(args):
     line = {"metric": "batched jamming: systems jammed/s, mixed vs FP64", "unit": "systems/s",
             "value": out["mixed"]["systems_per_s"], "n_gpus": 1, "higher_is_better": True,
             "config": {"workload": f"{S} systems, N log-uniform [64, 4096], phi0 0.80, "
-                                   "P = 1e-7 +- 1e-9, FIRE 1e-16/1e-16/1e5",
+                                   f"P = {args.jam_pressure:g} +- 1%, FIRE 1e-16/1e-16/1e5",
                        "sizes_sum": int(sizes.sum())},
             "fp64_systems_per_s": out["fp64"]["systems_per_s"],
             "dphi_J": {"median": float(np.median(d)), "max": float(d.max()),
@@ -670,6 +671,8 @@ def main():
                     help="run the batched jamming workload instead of the default line")
     ap.add_argument("--jam-systems", type=int, default=256)
     ap.add_argument("--jam-max-compressions", type=int, default=2000)
+    ap.add_argument("--jam-pressure", type=float, default=1e-7,
+                    help="target pressure of the batched jamming leg (band +-1%%)")
     args = ap.parse_args()
     BATCH = args.batch
     if args.jam_ensemble:
