@@ -286,6 +286,46 @@ __global__ void k_force_acc(DevSys *ds) {
     ds->w.pe[i] += en;
 }
 
+// calcWallInteraction (include/particles/base/kernels.cuh:185-235): hard walls
+// at 0 and L on both axes, terms in the reference's order (left, right,
+// bottom, top); returns the energy, force in (fx, fy) summed from 0
+__device__ __forceinline__ double wall_force(const DevParams &p, double2 x, double rad,
+                                             double &fx, double &fy) {
+    const double dist[4] = {x.x, p.box[0] - x.x, x.y, p.box[1] - x.y};
+    const bool near[4] = {x.x < rad, x.x > p.box[0] - rad, x.y < rad, x.y > p.box[1] - rad};
+    double en = 0.0;
+    fx = 0.0;
+    fy = 0.0;
+#pragma unroll
+    for (int w = 0; w < 4; w++) {
+        if (!near[w]) continue;
+        const double ov = rad - dist[w];
+        if (!(ov > 0)) continue;
+        const double q = ov / rad;
+        const double ovp = p.n_c - 1 == 1.0 ? q : pow(q, p.n_c - 1);
+        const double f = p.e_c * ovp / rad;
+        if (w == 0) fx += f;
+        else if (w == 1) fx -= f;
+        else if (w == 2) fy += f;
+        else fy -= f;
+        en += p.e_c * ov * ovp / (p.n_c * rad);
+    }
+    return en;
+}
+
+// kernelCalcDiskWallForces (+= semantics): src/particles/disk/kernels.cu:59-71
+__global__ void k_wall_force(DevSys *ds) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ds->p.n) return;
+    double fx, fy;
+    double en = wall_force(ds->p, ds->v.pos[i], ds->v.rad[i], fx, fy);
+    double2 f = ds->v.frc[i];
+    f.x += fx;
+    f.y += fy;
+    ds->v.frc[i] = f;
+    ds->w.pe[i] += en;
+}
+
 // kernelCalculateDampedForces: src/particles/base/kernels.cu:83-89
 __global__ void k_damp(DevSys *ds, double gamma) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -715,7 +755,16 @@ __global__ void k_nve_second(DevSys *ds, double dt_half) {
         double2 u = vel[i];
         double2 f;
         const double g = ds->s.damping;
-        if (g != 0.0) {
+        double pe0 = 0.0;
+        if (ds->s.walls) {
+            // NVE::wall_step (src/integrator/nve.cu:33-35): zero, wall forces,
+            // then += the pair sum unless the particle has no neighbours
+            double wx, wy;
+            const double ew = wall_force(ds->p, ds->v.pos[i], ds->v.rad[i], wx, wy);
+            f = make_double2(0.0 + wx, 0.0 + wy);
+            pe0 = 0.0 + ew;
+            if (ds->w.count[i] != 0) { f.x += ax; f.y += ay; pe0 += en; }
+        } else if (g != 0.0) {
             // DampedNVE::step (src/integrator/damped_nve.cu:22-23): F = 0 - g v,
             // then += the pair sum unless the particle has no neighbours
             f = make_double2(0.0 - g * u.x, 0.0 - g * u.y);
@@ -724,7 +773,7 @@ __global__ void k_nve_second(DevSys *ds, double dt_half) {
             f = make_double2(0.0 + ax, 0.0 + ay);
         }
         ds->v.frc[i] = f;
-        ds->w.pe[i] = 0.0 + en;
+        ds->w.pe[i] = ds->s.walls ? pe0 : 0.0 + en;
         double dtm = dt_half / ds->v.mass[i];
         u.x = u.x + f.x * dtm;
         u.y = u.y + f.y * dtm;

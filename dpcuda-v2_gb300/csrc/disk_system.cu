@@ -1123,6 +1123,20 @@ extern "C" int dpg_damped_nve_steps(dpg_handle s, double dt, double damping, int
     return rc != DPG_OK ? rc : rc2;
 }
 
+extern "C" int dpg_wall_forces(dpg_handle s) {
+    if (!s) return set_err(DPG_ERR_ARG, "null handle");
+    LAUNCH(k_wall_force, s->grid(s->n), s->tpb, s->d);
+    return DPG_OK;
+}
+
+extern "C" int dpg_nve_wall_steps(dpg_handle s, double dt, int64_t n_steps) {
+    if (!s) return set_err(DPG_ERR_ARG, "null handle");
+    TRY(put_field(s, &s->d->s.walls, 1));
+    int rc = dpg_nve_steps(s, dt, n_steps);
+    int rc2 = put_field(s, &s->d->s.walls, 0);
+    return rc != DPG_OK ? rc : rc2;
+}
+
 extern "C" int dpg_grad_desc_step(dpg_handle s, double alpha) {
     if (!s) return set_err(DPG_ERR_ARG, "null handle");
     LAUNCH(k_grad_desc, s->grid(s->n), s->tpb, s->d, alpha);

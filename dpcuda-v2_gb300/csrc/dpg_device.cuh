@@ -81,6 +81,8 @@ struct DevState {
     long long iter, max_steps, result_step;
     long long nve_steps_done;
     double damping;           // DampedNVE coefficient (0 in plain NVE)
+    int walls;                // NVE::wall_step: wall forces added before the pair forces
+    int pad3;
     // mixed form: FP64 pair arithmetic once fp64_now is set (FIRE refinement)
     int fp64_now;
     int pad2;

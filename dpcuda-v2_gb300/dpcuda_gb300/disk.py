@@ -276,6 +276,14 @@ class Disk:
         check(lib.dpg_state_count(str(directory).encode(), C.byref(n)))
         return n.value
 
+    def calculateWallForces(self):
+        """Disk::calculateWallForces: += hard-wall forces at 0 and L."""
+        check(self.lib.dpg_wall_forces(self.h))
+
+    def nveWallSteps(self, dt, n_steps):
+        """n NVE::wall_step (walls added before the pair forces)."""
+        check(self.lib.dpg_nve_wall_steps(self.h, float(dt), int(n_steps)))
+
     def calculateDampedForces(self, damping_coefficient):
         check(self.lib.dpg_damped_forces(self.h, float(damping_coefficient)))
 

@@ -119,6 +119,8 @@ SIGNATURES = {
     "dpg_write_state": [VP, C.c_char_p, I64],
     "dpg_read_state": [VP, C.c_char_p],
     "dpg_state_count": [C.c_char_p, I64P],
+    "dpg_wall_forces": [VP],
+    "dpg_nve_wall_steps": [VP, D, I64],
     "dpg_damped_forces": [VP, D],
     "dpg_damped_nve_steps": [VP, D, D, I64],
     "dpg_grad_desc_step": [VP, D],

@@ -198,6 +198,13 @@ int dpg_damped_forces(dpg_handle h, double damping);
 /* n DampedNVE::step (src/integrator/damped_nve.cu:15-27): kick dt/2, drift,
  * neighbour check, F = -damping v + pair forces, kick dt/2; one device loop */
 int dpg_damped_nve_steps(dpg_handle h, double dt, double damping, int64_t n_steps);
+/* Disk::calculateWallForces: += the hard-wall force and energy of walls at 0
+ * and the box length on both axes (src/particles/disk/disk.cu:257-259,
+ * include/particles/base/kernels.cuh:185-235) */
+int dpg_wall_forces(dpg_handle h);
+/* n NVE::wall_step (src/integrator/nve.cu:27-38): NVE with the wall forces
+ * added before the pair forces; one device loop */
+int dpg_nve_wall_steps(dpg_handle h, double dt, int64_t n_steps);
 /* updatePositionsGradDesc: x += alpha F (src/particles/base/particle.cu:267-269) */
 int dpg_grad_desc_step(dpg_handle h, double alpha);
 /* n GradDesc::step (src/integrator/grad_desc.cu:11-17): zero, neighbour check,

@@ -683,6 +683,46 @@ void orc_damped_nve_steps(orc_sys *s, double dt, double gamma, int64_t n_steps) 
     }
 }
 
+/* calcWallInteraction + kernelCalcDiskWallForces (+= into F, PE):
+ * include/particles/base/kernels.cuh:185-235, src/particles/disk/kernels.cu:59-71 */
+void orc_wall_forces(orc_sys *s) {
+    const int64_t n = s->n;
+    const double L0 = s->box[0], L1 = s->box[1], e_c = s->e_c, n_c = s->n_c;
+#pragma omp parallel for schedule(static) if (n >= PAR_MIN)
+    for (int64_t i = 0; i < n; i++) {
+        const double px = s->x[i], py = s->y[i], rad = s->r[i];
+        double fx = 0.0, fy = 0.0, en = 0.0;
+        const double dist[4] = {px, L0 - px, py, L1 - py};
+        const int near[4] = {px < rad, px > L0 - rad, py < rad, py > L1 - rad};
+        for (int w = 0; w < 4; w++) {
+            if (!near[w]) continue;
+            double ov = rad - dist[w];
+            if (!(ov > 0)) continue;
+            double ovp = pow(ov / rad, n_c - 1);
+            double f = e_c * ovp / rad;
+            if (w == 0) fx += f;
+            else if (w == 1) fx -= f;
+            else if (w == 2) fy += f;
+            else fy -= f;
+            en += e_c * ov * ovp / (n_c * rad);
+        }
+        s->fx[i] += fx; s->fy[i] += fy; s->pe[i] += en;
+    }
+}
+
+/* NVE::wall_step: src/integrator/nve.cu:27-38 */
+void orc_nve_wall_steps(orc_sys *s, double dt, int64_t n_steps) {
+    for (int64_t t = 0; t < n_steps; t++) {
+        orc_update_velocities(s, 0.5 * dt);
+        orc_update_positions(s, dt);
+        orc_check_for_neighbor_update(s);
+        orc_zero_force_and_pe(s);
+        orc_wall_forces(s);
+        orc_calculate_forces(s);
+        orc_update_velocities(s, 0.5 * dt);
+    }
+}
+
 /* kernelGradDescStep: src/particles/base/kernels.cu:613-637 */
 void orc_update_positions_grad_desc(orc_sys *s, double alpha) {
     const int64_t n = s->n;

@@ -78,6 +78,8 @@ void orc_damped_forces(orc_sys *s, double gamma);                    /* F -= gam
 void orc_damped_nve_steps(orc_sys *s, double dt, double gamma, int64_t n_steps);
 void orc_update_positions_grad_desc(orc_sys *s, double alpha);       /* x += alpha F */
 void orc_grad_desc_steps(orc_sys *s, double alpha, int64_t n_steps);
+void orc_wall_forces(orc_sys *s);                                    /* += wall force / energy */
+void orc_nve_wall_steps(orc_sys *s, double dt, int64_t n_steps);
 
 /* ---- FIRE -------------------------------------------------------------- */
 void orc_fire_init(orc_sys *s, double alpha_init, double dt);

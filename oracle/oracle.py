@@ -73,6 +73,8 @@ _SIGS = {
     "nve_steps": (None, [P, D, I64]),
     "damped_nve_steps": (None, [P, D, D, I64]),
     "grad_desc_steps": (None, [P, D, I64]),
+    "wall_forces": (None, [P]),
+    "nve_wall_steps": (None, [P, D, I64]),
     "fire_init": (None, [P, D, D]),
     "fire_step": (C.c_int, [P]),
     "fire_state": (None, [P, DP, DP, LP, LP, C.POINTER(C.c_int)]),
@@ -270,6 +272,12 @@ class DiskOracle:
 
     def damped_nve_steps(self, dt, gamma, n):
         self._f("damped_nve_steps")(self.h, float(dt), float(gamma), int(n))
+
+    def wall_forces(self):
+        self._f("wall_forces")(self.h)
+
+    def nve_wall_steps(self, dt, n):
+        self._f("nve_wall_steps")(self.h, float(dt), int(n))
 
     def grad_desc_steps(self, alpha, n):
         self._f("grad_desc_steps")(self.h, float(alpha), int(n))

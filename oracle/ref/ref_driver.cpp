@@ -483,6 +483,28 @@ void ref_damped_nve_steps(ref_sys *s, double dt, double gamma, int64_t n_steps) 
     }
 }
 
+/* Disk::calculateWallForces (src/particles/disk/disk.cu:257-259) */
+void ref_wall_forces(ref_sys *s) {
+    sync(s);
+    launch(s->n, [&] {
+        kernelCalcDiskWallForces(s->x.data(), s->y.data(), s->r.data(), s->fx.data(), s->fy.data(),
+                                 s->pe.data());
+    });
+}
+
+/* NVE::wall_step (src/integrator/nve.cu:27-38) over the reference kernels */
+void ref_nve_wall_steps(ref_sys *s, double dt, int64_t n_steps) {
+    for (int64_t t = 0; t < n_steps; t++) {
+        ref_update_velocities(s, 0.5 * dt);
+        ref_update_positions(s, dt);
+        ref_check_for_neighbor_update(s);
+        ref_zero_force_and_pe(s);
+        ref_wall_forces(s);
+        ref_calculate_forces(s);
+        ref_update_velocities(s, 0.5 * dt);
+    }
+}
+
 /* GradDesc::step (src/integrator/grad_desc.cu:11-17) over the reference kernels */
 void ref_grad_desc_steps(ref_sys *s, double alpha, int64_t n_steps) {
     for (int64_t t = 0; t < n_steps; t++) {

@@ -150,6 +150,22 @@ def make_damped_gd():
     np.savez_compressed(HERE / "disk_n512_damped_gd.npz", **d)
 
 
+def make_walls():
+    """Disk::calculateWallForces and NVE::wall_step (src/particles/disk/kernels.cu:59-71,
+    src/integrator/nve.cu:27-38)."""
+    d = {}
+    n, phi, seed = 256, 0.80, 11
+    o, st, vx, vy, meth = system(n, phi, seed, vel_T=1e-3)
+    d.update(x0=st["x"], y0=st["y"], r=st["r"], m=st["m"], box=st["box"], vx0=vx, vy0=vy,
+             method=meth)
+    o.zero_force_and_pe()
+    o.wall_forces()
+    snapshot(o, "wall", d)
+    o.nve_wall_steps(1e-2, 300)
+    snapshot(o, "wallnve300", d)
+    np.savez_compressed(HERE / "disk_n256_walls.npz", **d)
+
+
 def make_rng():
     d = {}
     for seed in (1, 7, 12345):
@@ -210,6 +226,7 @@ if __name__ == "__main__":
     make_cfg1()
     make_fire_min()
     make_damped_gd()
+    make_walls()
     make_bumpy(64, 0.80, 3, "bumpy_n64_verlet.npz")
     make_bumpy(256, 0.80, 5, "bumpy_n256_cell.npz")
     print("fixtures written to", HERE)

@@ -134,6 +134,32 @@ def test_damped_nve_and_gradient_descent_bitexact(dpg):
         np.testing.assert_array_equal(sa[k], sb[k])
 
 
+def test_wall_forces_and_wall_nve_bitexact(dpg):
+    """calculateWallForces and NVE::wall_step against the reference kernels'
+    results (walls at 0 and L, pair distances still periodic, as the reference)."""
+    d = load("disk_n256_walls.npz")
+    s = make(dpg, d)
+    s.zeroForceAndPotentialEnergy()
+    s.calculateWallForces()
+    assert_state(s, d, "wall")
+    s.nveWallSteps(1e-2, 300)
+    assert_state(s, d, "wallnve300")
+    # the per-method form of NVE::wall_step gives the same trajectory
+    a, b = make(dpg, d), make(dpg, d)
+    for _ in range(30):
+        a.updateVelocities(0.5e-2)
+        a.updatePositions(1e-2)
+        a.checkForNeighborUpdate()
+        a.zeroForceAndPotentialEnergy()
+        a.calculateWallForces()
+        a.calculateForces()
+        a.updateVelocities(0.5e-2)
+    b.nveWallSteps(1e-2, 30)
+    sa, sb = a.getState(), b.getState()
+    for k in KEYS:
+        np.testing.assert_array_equal(sa[k], sb[k])
+
+
 def test_fire_steps_bitexact(dpg):
     d = load("disk_n1024_cell.npz")
     s = make(dpg, d)

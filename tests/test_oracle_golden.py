@@ -145,3 +145,15 @@ def test_damped_nve_and_gradient_descent():
     o.grad_desc_steps(1e-2, 200)
     assert_state(o, d, "gd200")
     assert list(o.num_rebuilds()) == list(d["gd200_rebuilds"])
+
+
+def test_wall_forces_and_nve_wall_step():
+    """calcWallInteraction / kernelCalcDiskWallForces and NVE::wall_step
+    (include/particles/base/kernels.cuh:185-235, src/integrator/nve.cu:27-38)."""
+    d = load("disk_n256_walls.npz")
+    o = make(d)
+    o.zero_force_and_pe()
+    o.wall_forces()
+    assert_state(o, d, "wall")
+    o.nve_wall_steps(1e-2, 300)
+    assert_state(o, d, "wallnve300")
