@@ -286,6 +286,87 @@ __global__ void k_force_acc(DevSys *ds) {
     ds->w.pe[i] += en;
 }
 
+// ---- pair and Hessian dump -----------------------------------------------------
+struct PairOut {
+    double *d[16];  // see dpg_pair_dump in include/dpg.h for the order
+    long long *this_id, *other_id;
+};
+
+// the fills of Disk::calculateForceDistancePairs (src/particles/disk/disk.cu:229-247)
+__global__ void k_pair_fill(PairOut o, long long m) {
+    long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= m) return;
+    const double fill[16] = {-1, 0, 0, -1, -1, -1, -1, -1, 0, 0, 0, 0, 0, 0, 0, 0};
+#pragma unroll
+    for (int k = 0; k < 16; k++)
+        if (o.d[k]) o.d[k][q] = fill[k];
+    o.this_id[q] = -1;
+    o.other_id[q] = -1;
+}
+
+// kernelCalcDiskForceDistancePairs (src/particles/disk/kernels.cu:73-175):
+// entry [slot * cap + k] for the k-th neighbour of the particle in slot i
+__global__ void k_pair_dump(DevSys *ds, PairOut o) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = ds->p.n, cap = ds->p.cap;
+    if (i >= n) return;
+    int cnt = ds->w.count[i];
+    if (cnt == 0) return;
+    if (cnt > cap) cnt = cap;
+    const double2 *pos = ds->v.pos;
+    const double *rad = ds->v.rad;
+    const double2 pi = pos[i];
+    const double ri = rad[i];
+    const double bx = ds->p.box[0], by = ds->p.box[1], e_c = ds->p.e_c, n_c = ds->p.n_c;
+    for (int k = 0; k < cnt; k++) {
+        const int j = ds->v.nbr[(size_t)k * n + i];
+        const double2 pj = pos[j];
+        const double rj = rad[j];
+        double fx, fy;
+        const double e = disk_pair(pi.x, pi.y, ri, pj.x, pj.y, rj, bx, by, e_c, n_c, fx, fy);
+        const long long q = (long long)i * cap + k;
+        const double dx = pbc_dist(pi.x, pj.x, bx), dy = pbc_dist(pi.y, pj.y, by);
+        if (o.d[0]) o.d[0][q] = e;
+        if (o.d[1]) o.d[1][q] = fx;
+        if (o.d[2]) o.d[2][q] = fy;
+        if (o.d[3]) o.d[3][q] = dx;
+        if (o.d[4]) o.d[4][q] = dy;
+        o.this_id[q] = ds->v.sidx[i];
+        o.other_id[q] = ds->v.sidx[j];
+        const double dist = sqrt(dx * dx + dy * dy);
+        if (o.d[5]) o.d[5][q] = dist - (ri + rj);
+        if (o.d[6]) o.d[6][q] = ri + rj;
+        if (o.d[7]) o.d[7][q] = atan2(dy, dx);
+        if (dist < ri + rj) {
+            const double radsum = ri + rj;
+            const double t_ij = -e_c / radsum * (1 - dist / radsum);
+            const double c_ij = e_c / (radsum * radsum);
+            double hij[4] = {0.0, 0.0, 0.0, 0.0}, hii[4] = {0.0, 0.0, 0.0, 0.0};
+            for (int a = 0; a < 2; a++) {
+                for (int b = 0; b < 2; b++) {
+                    const double dia_x = 1 * (a == 0), dia_y = 1 * (a == 1);
+                    const double djb_x = -1 * (b == 0), djb_y = -1 * (b == 1);
+                    const double q_ia = dx * dia_x + dy * dia_y;
+                    const double q_jb = dx * djb_x + dy * djb_y;
+                    const double dia_q_jb = dia_x * djb_x + dx * 0.0 + dia_y * djb_y + dy * 0.0;
+                    hij[a * 2 + b] += c_ij * (q_ia * q_jb) / (dist * dist) +
+                                      t_ij * (dia_q_jb / dist - (q_ia * q_jb) / (dist * dist * dist));
+                    const double dib_x = 1 * (b == 0), dib_y = 1 * (b == 1);
+                    const double q_ib = dx * dib_x + dy * dib_y;
+                    const double dia_q_ib = dia_x * dib_x + dx * 0.0 + dia_y * dib_y + dy * 0.0;
+                    hii[a * 2 + b] += c_ij * (q_ia * q_ib) / (dist * dist) +
+                                      t_ij * (dia_q_ib / dist - (q_ia * q_ib) / (dist * dist * dist));
+                }
+            }
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                if (o.d[8 + c]) o.d[8 + c][q] += hij[c];
+                if (o.d[12 + c]) o.d[12 + c][q] += hii[c];
+            }
+        }
+    }
+}
+
 // calcWallInteraction (include/particles/base/kernels.cuh:185-235): hard walls
 // at 0 and L on both axes, terms in the reference's order (left, right,
 // bottom, top); returns the energy, force in (fx, fy) summed from 0

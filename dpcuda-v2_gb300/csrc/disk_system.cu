@@ -1123,6 +1123,52 @@ extern "C" int dpg_damped_nve_steps(dpg_handle s, double dt, double damping, int
     return rc != DPG_OK ? rc : rc2;
 }
 
+extern "C" int dpg_pair_dump(dpg_handle s, double *const *out, int64_t *this_id,
+                             int64_t *other_id, int where) {
+    TRY(need_neighbors(s));
+    if (!out || !this_id || !other_id) return set_err(DPG_ERR_ARG, "dpg_pair_dump: null argument");
+    if (where != DPG_HOST && where != DPG_DEVICE) return set_err(DPG_ERR_ARG, "bad where");
+    const long long m = (long long)s->n * s->cap;
+    PairOut o{};
+    std::vector<void *> tmp;
+    auto release = [&]() { for (void *p : tmp) cudaFree(p); };
+    for (int k = 0; k < 16; k++) {
+        if (!out[k]) continue;
+        if (where == DPG_DEVICE) { o.d[k] = out[k]; continue; }
+        void *p = nullptr;
+        cudaError_t e = cudaMalloc(&p, 8 * (size_t)m);
+        if (e != cudaSuccess) { release(); return set_err(DPG_ERR_CUDA, "pair dump: %s", cudaGetErrorString(e)); }
+        tmp.push_back(p);
+        o.d[k] = (double *)p;
+    }
+    if (where == DPG_DEVICE) {
+        o.this_id = (long long *)this_id;
+        o.other_id = (long long *)other_id;
+    } else {
+        void *a = nullptr, *b = nullptr;
+        cudaError_t e = cudaMalloc(&a, 8 * (size_t)m);
+        if (e == cudaSuccess) { tmp.push_back(a); e = cudaMalloc(&b, 8 * (size_t)m); }
+        if (e != cudaSuccess) { release(); return set_err(DPG_ERR_CUDA, "pair dump: %s", cudaGetErrorString(e)); }
+        tmp.push_back(b);
+        o.this_id = (long long *)a;
+        o.other_id = (long long *)b;
+    }
+    const int fb = (int)((m + 255) / 256);
+    k_pair_fill<<<fb, 256, 0, s->stream>>>(o, m);
+    k_pair_dump<<<s->grid(s->n), s->tpb, 0, s->stream>>>(s->d, o);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess && where == DPG_HOST) {
+        for (int k = 0; k < 16 && e == cudaSuccess; k++)
+            if (out[k]) e = cudaMemcpyAsync(out[k], o.d[k], 8 * (size_t)m, cudaMemcpyDeviceToHost, s->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(this_id, o.this_id, 8 * (size_t)m, cudaMemcpyDeviceToHost, s->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(other_id, o.other_id, 8 * (size_t)m, cudaMemcpyDeviceToHost, s->stream);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    release();
+    if (e != cudaSuccess) return set_err(DPG_ERR_CUDA, "pair dump: %s", cudaGetErrorString(e));
+    return DPG_OK;
+}
+
 extern "C" int dpg_wall_forces(dpg_handle s) {
     if (!s) return set_err(DPG_ERR_ARG, "null handle");
     LAUNCH(k_wall_force, s->grid(s->n), s->tpb, s->d);

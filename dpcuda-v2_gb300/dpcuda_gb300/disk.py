@@ -276,6 +276,24 @@ class Disk:
         check(lib.dpg_state_count(str(directory).encode(), C.byref(n)))
         return n.value
 
+    PAIR_KEYS = ("potential", "force_x", "force_y", "distance_x", "distance_y", "overlap",
+                 "radsum", "angle", "hess_xx", "hess_xy", "hess_yx", "hess_yy",
+                 "hess_ii_xx", "hess_ii_xy", "hess_ii_yx", "hess_ii_yy")
+
+    def calculateForceDistancePairs(self):
+        """Pair energies, forces, separations, ids, overlaps, angles and Hessian
+        blocks per neighbour-list entry ([slot * cap + k], current order), as
+        the reference's Disk::calculateForceDistancePairs."""
+        cap = self.neighborInfo()["capacity"]
+        m = self.n * cap
+        out = {k: np.zeros(m) for k in self.PAIR_KEYS}
+        ptrs = (DP * 16)(*[out[k].ctypes.data_as(DP) for k in self.PAIR_KEYS])
+        ti, oi = np.zeros(m, dtype=np.int64), np.zeros(m, dtype=np.int64)
+        check(self.lib.dpg_pair_dump(self.h, ptrs, ti.ctypes.data_as(C.POINTER(C.c_int64)),
+                                     oi.ctypes.data_as(C.POINTER(C.c_int64)), HOST))
+        out["this_id"], out["other_id"] = ti, oi
+        return out
+
     def calculateWallForces(self):
         """Disk::calculateWallForces: += hard-wall forces at 0 and L."""
         check(self.lib.dpg_wall_forces(self.h))

@@ -120,6 +120,7 @@ SIGNATURES = {
     "dpg_read_state": [VP, C.c_char_p],
     "dpg_state_count": [C.c_char_p, I64P],
     "dpg_wall_forces": [VP],
+    "dpg_pair_dump": [VP, C.POINTER(DP), I64P, I64P, I32],
     "dpg_nve_wall_steps": [VP, D, I64],
     "dpg_damped_forces": [VP, D],
     "dpg_damped_nve_steps": [VP, D, D, I64],

@@ -198,6 +198,16 @@ int dpg_damped_forces(dpg_handle h, double damping);
 /* n DampedNVE::step (src/integrator/damped_nve.cu:15-27): kick dt/2, drift,
  * neighbour check, F = -damping v + pair forces, kick dt/2; one device loop */
 int dpg_damped_nve_steps(dpg_handle h, double dt, double damping, int64_t n_steps);
+/* Disk::calculateForceDistancePairs (src/particles/disk/disk.cu:228-255, kernel
+ * src/particles/disk/kernels.cu:73-175): per neighbour-list entry, arrays of
+ * n * cap (cap from dpg_neighbor_info_get) laid out as the reference's,
+ * [slot * cap + k] in the current (cell-sorted) slot order, with the
+ * reference's fill values where an entry is unused.  out[16] (NULL entries
+ * skipped): pair energy, force x, force y, separation x, y, overlap (distance -
+ * radius sum), radius sum, separation angle, pair Hessian xx, xy, yx, yy,
+ * self Hessian xx, xy, yx, yy; this_id / other_id: static indices. */
+int dpg_pair_dump(dpg_handle h, double *const *out, int64_t *this_id, int64_t *other_id,
+                  int where);
 /* Disk::calculateWallForces: += the hard-wall force and energy of walls at 0
  * and the box length on both axes (src/particles/disk/disk.cu:257-259,
  * include/particles/base/kernels.cuh:185-235) */

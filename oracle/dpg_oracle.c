@@ -683,6 +683,69 @@ void orc_damped_nve_steps(orc_sys *s, double dt, double gamma, int64_t n_steps) 
     }
 }
 
+/* kernelCalcDiskForceDistancePairs (src/particles/disk/kernels.cu:73-175) after
+ * the fills of Disk::calculateForceDistancePairs (src/particles/disk/disk.cu:228-255).
+ * d[16]: potential, force x/y, distance x/y, overlap, radius sum, separation angle,
+ * pair Hessian xx/xy/yx/yy, self Hessian xx/xy/yx/yy; n * cap each, row-major
+ * [slot * cap + k] in the current order; ids are static indices. */
+void orc_pair_dump(orc_sys *s, double *const *d, int64_t *this_id, int64_t *other_id) {
+    const int64_t n = s->n, cap = s->cap, m = n * cap;
+    const double fill[16] = {-1, 0, 0, -1, -1, -1, -1, -1, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int k = 0; k < 16; k++)
+        if (d[k]) for (int64_t q = 0; q < m; q++) d[k][q] = fill[k];
+    for (int64_t q = 0; q < m; q++) { this_id[q] = -1; other_id[q] = -1; }
+    for (int64_t i = 0; i < n; i++) {
+        if (s->ncount[i] == 0) continue;
+        const double xi = s->x[i], yi = s->y[i], ri = s->r[i];
+        for (int64_t k = 0; k < cap; k++) {
+            const int64_t j = s->nlist[i * cap + k];
+            if (j == -1 || j == i) continue;
+            double fx, fy;
+            const double e = pair_interaction(s, xi, yi, ri, s->x[j], s->y[j], s->r[j], &fx, &fy);
+            const int64_t q = i * cap + k;
+            const double dx = pbc(xi, s->x[j], s->box[0]), dy = pbc(yi, s->y[j], s->box[1]);
+            const double rj = s->r[j];
+            if (d[0]) d[0][q] = e;
+            if (d[1]) d[1][q] = fx;
+            if (d[2]) d[2][q] = fy;
+            if (d[3]) d[3][q] = dx;
+            if (d[4]) d[4][q] = dy;
+            this_id[q] = s->sidx[i];
+            other_id[q] = s->sidx[j];
+            const double dist = sqrt(dx * dx + dy * dy);
+            if (d[5]) d[5][q] = dist - (ri + rj);
+            if (d[6]) d[6][q] = ri + rj;
+            if (d[7]) d[7][q] = atan2(dy, dx);
+            if (dist < ri + rj) {
+                const double radsum = ri + rj;
+                const double t_ij = -s->e_c / radsum * (1 - dist / radsum);
+                const double c_ij = s->e_c / (radsum * radsum);
+                double hij[4] = {0.0, 0.0, 0.0, 0.0}, hii[4] = {0.0, 0.0, 0.0, 0.0};
+                for (int a = 0; a < 2; a++) {
+                    for (int b = 0; b < 2; b++) {
+                        const double dia_x = 1 * (a == 0), dia_y = 1 * (a == 1);
+                        const double djb_x = -1 * (b == 0), djb_y = -1 * (b == 1);
+                        const double q_ia = dx * dia_x + dy * dia_y;
+                        const double q_jb = dx * djb_x + dy * djb_y;
+                        const double dia_q_jb = dia_x * djb_x + dx * 0.0 + dia_y * djb_y + dy * 0.0;
+                        hij[a * 2 + b] += c_ij * (q_ia * q_jb) / (dist * dist) +
+                                          t_ij * (dia_q_jb / dist - (q_ia * q_jb) / (dist * dist * dist));
+                        const double dib_x = 1 * (b == 0), dib_y = 1 * (b == 1);
+                        const double q_ib = dx * dib_x + dy * dib_y;
+                        const double dia_q_ib = dia_x * dib_x + dx * 0.0 + dia_y * dib_y + dy * 0.0;
+                        hii[a * 2 + b] += c_ij * (q_ia * q_ib) / (dist * dist) +
+                                          t_ij * (dia_q_ib / dist - (q_ia * q_ib) / (dist * dist * dist));
+                    }
+                }
+                for (int c = 0; c < 4; c++) {
+                    if (d[8 + c]) d[8 + c][q] += hij[c];
+                    if (d[12 + c]) d[12 + c][q] += hii[c];
+                }
+            }
+        }
+    }
+}
+
 /* calcWallInteraction + kernelCalcDiskWallForces (+= into F, PE):
  * include/particles/base/kernels.cuh:185-235, src/particles/disk/kernels.cu:59-71 */
 void orc_wall_forces(orc_sys *s) {

@@ -79,6 +79,7 @@ void orc_damped_nve_steps(orc_sys *s, double dt, double gamma, int64_t n_steps);
 void orc_update_positions_grad_desc(orc_sys *s, double alpha);       /* x += alpha F */
 void orc_grad_desc_steps(orc_sys *s, double alpha, int64_t n_steps);
 void orc_wall_forces(orc_sys *s);                                    /* += wall force / energy */
+void orc_pair_dump(orc_sys *s, double *const *d, int64_t *this_id, int64_t *other_id);
 void orc_nve_wall_steps(orc_sys *s, double dt, int64_t n_steps);
 
 /* ---- FIRE -------------------------------------------------------------- */

@@ -74,6 +74,7 @@ _SIGS = {
     "damped_nve_steps": (None, [P, D, D, I64]),
     "grad_desc_steps": (None, [P, D, I64]),
     "wall_forces": (None, [P]),
+    "pair_dump": (None, [P, C.POINTER(DP), LP, LP]),
     "nve_wall_steps": (None, [P, D, I64]),
     "fire_init": (None, [P, D, D]),
     "fire_step": (C.c_int, [P]),
@@ -272,6 +273,21 @@ class DiskOracle:
 
     def damped_nve_steps(self, dt, gamma, n):
         self._f("damped_nve_steps")(self.h, float(dt), float(gamma), int(n))
+
+    PAIR_KEYS = ("potential", "force_x", "force_y", "distance_x", "distance_y", "overlap",
+                 "radsum", "angle", "hess_xx", "hess_xy", "hess_yx", "hess_yy",
+                 "hess_ii_xx", "hess_ii_xy", "hess_ii_yx", "hess_ii_yy")
+
+    def pair_dump(self):
+        """calculateForceDistancePairs arrays, [slot * cap + k] in the current order."""
+        cap = self.neighbor_info()["cap"]
+        m = self.n * cap
+        out = {k: np.zeros(m) for k in self.PAIR_KEYS}
+        ptrs = (DP * 16)(*[_dp(out[k]) for k in self.PAIR_KEYS])
+        ti, oi = np.zeros(m, dtype=np.int64), np.zeros(m, dtype=np.int64)
+        self._f("pair_dump")(self.h, ptrs, ti.ctypes.data_as(LP), oi.ctypes.data_as(LP))
+        out["this_id"], out["other_id"] = ti, oi
+        return out
 
     def wall_forces(self):
         self._f("wall_forces")(self.h)

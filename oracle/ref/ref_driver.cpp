@@ -483,6 +483,28 @@ void ref_damped_nve_steps(ref_sys *s, double dt, double gamma, int64_t n_steps) 
     }
 }
 
+/* Disk::calculateForceDistancePairs (src/particles/disk/disk.cu:228-255): the
+ * reference's fills, then its kernel; 18 arrays of n * cap, row-major
+ * [slot * cap + k] in the current order (ids are static indices) */
+void ref_pair_dump(ref_sys *s, double *const *d, int64_t *this_id, int64_t *other_id) {
+    const long m = s->n * s->cap;
+    std::vector<double> v[16];
+    const double fill[16] = {-1, 0, 0, -1, -1, -1, -1, -1, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int k = 0; k < 16; k++) v[k].assign(m, fill[k]);
+    std::vector<long> ti(m, -1), oi(m, -1);
+    sync(s);
+    launch(s->n, [&] {
+        kernelCalcDiskForceDistancePairs(s->x.data(), s->y.data(), v[0].data(), v[1].data(), v[2].data(),
+                                         v[3].data(), v[4].data(), ti.data(), oi.data(), v[5].data(),
+                                         v[6].data(), s->r.data(), s->sidx.data(), v[7].data(),
+                                         v[8].data(), v[9].data(), v[10].data(), v[11].data(),
+                                         v[12].data(), v[13].data(), v[14].data(), v[15].data());
+    });
+    for (int k = 0; k < 16; k++)
+        if (d[k]) std::copy(v[k].begin(), v[k].end(), d[k]);
+    for (long q = 0; q < m; q++) { this_id[q] = ti[q]; other_id[q] = oi[q]; }
+}
+
 /* Disk::calculateWallForces (src/particles/disk/disk.cu:257-259) */
 void ref_wall_forces(ref_sys *s) {
     sync(s);

@@ -166,6 +166,22 @@ def make_walls():
     np.savez_compressed(HERE / "disk_n256_walls.npz", **d)
 
 
+def make_pairs():
+    """Disk::calculateForceDistancePairs (src/particles/disk/disk.cu:228-255,
+    src/particles/disk/kernels.cu:73-175) after 50 NVE steps of a cell-list system."""
+    d = {}
+    n, phi, seed = 256, 0.86, 13
+    o, st, vx, vy, meth = system(n, phi, seed, vel_T=1e-3)
+    d.update(x0=st["x"], y0=st["y"], r=st["r"], m=st["m"], box=st["box"], vx0=vx, vy0=vy,
+             method=meth)
+    o.nve_steps(1e-2, 50)
+    d["cap"] = o.neighbor_info()["cap"]
+    d["static_index"] = o.get_current()["static_index"]
+    for k, v in o.pair_dump().items():
+        d[f"pairs_{k}"] = v
+    np.savez_compressed(HERE / "disk_n256_pairs.npz", **d)
+
+
 def make_rng():
     d = {}
     for seed in (1, 7, 12345):
@@ -227,6 +243,7 @@ if __name__ == "__main__":
     make_fire_min()
     make_damped_gd()
     make_walls()
+    make_pairs()
     make_bumpy(64, 0.80, 3, "bumpy_n64_verlet.npz")
     make_bumpy(256, 0.80, 5, "bumpy_n256_cell.npz")
     print("fixtures written to", HERE)

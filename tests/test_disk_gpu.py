@@ -160,6 +160,22 @@ def test_wall_forces_and_wall_nve_bitexact(dpg):
         np.testing.assert_array_equal(sa[k], sb[k])
 
 
+def test_pair_and_hessian_dump_bitexact(dpg):
+    """calculateForceDistancePairs in the reference's layout ([slot * cap + k],
+    current order): every array bit-identical to the reference kernels' except
+    the separation angle, which comes from CUDA's atan2 (2 ulp of glibc's)."""
+    d = load("disk_n256_pairs.npz")
+    s = make(dpg, d)
+    s.nveSteps(1e-2, 50)
+    assert s.neighborInfo()["capacity"] == int(d["cap"])
+    got = s.calculateForceDistancePairs()
+    for k, v in got.items():
+        if k == "angle":
+            np.testing.assert_allclose(v, d["pairs_angle"], rtol=0, atol=2e-15)
+        else:
+            np.testing.assert_array_equal(v, d[f"pairs_{k}"], err_msg=k)
+
+
 def test_fire_steps_bitexact(dpg):
     d = load("disk_n1024_cell.npz")
     s = make(dpg, d)

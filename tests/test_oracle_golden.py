@@ -157,3 +157,16 @@ def test_wall_forces_and_nve_wall_step():
     assert_state(o, d, "wall")
     o.nve_wall_steps(1e-2, 300)
     assert_state(o, d, "wallnve300")
+
+
+def test_pair_and_hessian_dump():
+    """kernelCalcDiskForceDistancePairs after the reference's fills: pair
+    energies, forces, separations, ids, overlaps, angles and the pair / self
+    Hessian blocks (src/particles/disk/kernels.cu:73-175)."""
+    d = load("disk_n256_pairs.npz")
+    o = make(d)
+    o.nve_steps(1e-2, 50)
+    assert o.neighbor_info()["cap"] == int(d["cap"])
+    got = o.pair_dump()
+    for k, v in got.items():
+        np.testing.assert_array_equal(v, d[f"pairs_{k}"], err_msg=k)
