@@ -634,7 +634,12 @@ __device__ void e_force_epilogue(EDev *e, ESys &s, const double (&v)[5], bool se
         }
         const double exit_f = s.prec == 0 ? p.switch_fmax : (p.fmax_target > 0 ? p.fmax_target : 1e-10);
         const bool stalled = fmax < 100.0 * exit_f && s.iter - s.best_it > kStallIters;
-        if (fmax <= exit_f || s.nbad > 5 || stalled) {
+        // a PE-change stop (pe_diff_target > 0) is only decided in FP64: once
+        // the double-word energy has stopped changing at its own precision
+        // (1e-12 relative), hand over so the FP64 test can fire
+        const bool pe_flat = s.prec == 2 && p.pe_diff_target > 0 &&
+                             fabs(s.pe / (double)s.n / s.last_avg_pe - 1) < 1e-12;
+        if (fmax <= exit_f || s.nbad > 5 || stalled || pe_flat) {
             if (s.prec == 0 && p.dw_ok) {
                 s.prec = 2;
                 s.best_f2 = s.fmax2;
@@ -712,7 +717,9 @@ __device__ void e_force_epilogue(EDev *e, ESys &s, const double (&v)[5], bool se
     s.scale = Lnew / L_prior;
 }
 
-__global__ void __launch_bounds__(kEB) e_force(EDev *e) {
+// at most 102 registers, so 5 blocks (20 warps) fit an SM: measured 12 % faster
+// than the unbounded 108-register build on 16 x 16384 disks
+__global__ void __launch_bounds__(kEB, 5) e_force(EDev *e) {
     if (e->overflow) return;  // lists truncated: the host grows them and reruns this pass
     const int sid = e->blk_sys[blockIdx.x];
     ESys &s = e->sys[sid];

@@ -76,7 +76,9 @@ def test_ragged_ensemble_with_tiny_systems(dpg):
     """Systems of 1, 2, 3 and 64 disks in one ensemble: FP64 forces equal the
     plain path's, a lone disk has none, and a FIRE run finishes every system."""
     from oracle.oracle import disk_packing
-    sts = [disk_packing(n, 0.7, 90 + n) for n in (1, 2, 3, 64)]
+    # dilute tiny systems (boxes wider than twice the cutoff, so the minimum
+    # image is unambiguous), a dense 64-disk one
+    sts = [disk_packing(n, 0.1 if n < 4 else 0.7, 90 + n) for n in (1, 2, 3, 64)]
     e = dpg.Ensemble([len(s["r"]) for s in sts], [s["box"] for s in sts], 1.7, 0.3,
                      precision=dpg.FP64)
     e.setState(*[np.concatenate([s[c] for s in sts]) for c in ("x", "y", "r", "m")])
@@ -98,5 +100,5 @@ def test_ragged_ensemble_with_tiny_systems(dpg):
         s.close()
     assert got["fx"][0] == 0.0 and got["fy"][0] == 0.0
     res = e.minimizeFire(0.1, 1e-2, 0.0, 0.0, 200_000, fmax_target=1e-12)
-    assert all(r["converged"] == 1 and r["max_force"] <= 1e-12 for r in res)
+    assert all(r["converged"] == 1 and r["max_force"] <= 1e-12 for r in res), res
     e.close()
