@@ -40,6 +40,13 @@ struct BumpyExt {
     double *s_w, *s_th, *s_tq;
     double2 *s_vpos;
     int *s_nvb, *s_start, *s_vbody, *s_svidx;
+    // per slot, never re-sorted (like the reference's angle_delta and angular
+    // Adam moments): the last angle increment and the angular Adam moments
+    double *adelta, *m1a, *m2a;
+    // per-body results of the stress and contact passes (body-slot order)
+    double *stress_b;   // [4][nb]: xx, xy, yx, yy
+    int *ccount, *vccount;
+    double vcontacts;
 };
 
 struct BumpySys {
@@ -91,6 +98,7 @@ __device__ __forceinline__ void body_move(BumpySys *bs, int b, int lane, double 
     if (lane == 0) {
         d.v.pos[b] = make_double2(nx, ny);
         x.th[b] = ang + dth;
+        x.adelta[b] = dth;
         double2 a = d.w.pos_n[b], c = d.w.pos_c[b];
         double a1 = nx - a.x, a2 = ny - a.y, c1 = nx - c.x, c2 = ny - c.y;
         nd2 = a1 * a1 + a2 * a2;
@@ -119,9 +127,12 @@ __global__ void kb_drift(BumpySys *bs, double dt) {
 
 // ---- forces: kernelCalcRigidBumpyForces1 + kernelCalcRigidBumpyParticleForces1
 // (kernels.cu:366-442) fused, one warp per body.  Outputs the body sums (every
-// lane holds the same values).
+// lane holds the same values).  walls: kernelCalcRigidBumpyWallForces
+// (kernels.cu:348-362) first, as NVE::wall_step calls it before the pairs, so
+// a vertex carries (0 + wall) + pair sum.
 __device__ __forceinline__ void body_forces(const BumpySys *__restrict__ bs, int b, int lane,
-                                            double &bfx, double &bfy, double &btq, double &bpe) {
+                                            bool walls, double &bfx, double &bfy, double &btq,
+                                            double &bpe) {
     const DevSys &d = bs->b;
     const BumpyExt &x = bs->x;
     const int nv = x.nv, capv = x.capv;
@@ -162,11 +173,19 @@ __device__ __forceinline__ void body_forces(const BumpySys *__restrict__ bs, int
                     en += e;
                 }
             }
+            if (walls) {
+                double wx, wy;
+                const double we = wall_force(d.p, q, rv, wx, wy);
+                vfx = 0.0 + wx;
+                vfy = 0.0 + wy;
+                vtq = 0.0 + torque_of(wx, wy, q.x, q.y, c.x, c.y);
+                vpe = 0.0 + we;
+            }
             if (cnt > 0) {
-                vfx = 0.0 + ax;
-                vfy = 0.0 + ay;
-                vtq = 0.0 + torque_of(ax, ay, q.x, q.y, c.x, c.y);
-                vpe = 0.0 + en;
+                vfx = vfx + ax;
+                vfy = vfy + ay;
+                vtq = vtq + torque_of(ax, ay, q.x, q.y, c.x, c.y);
+                vpe = vpe + en;
             }
         }
         int lim = min(32, nvb - base);
@@ -186,13 +205,14 @@ __global__ void kb_mixed_refresh(BumpySys *bs) {
     bs->x.vpk[v] = mixed_pack(bs->b.p, bs->x.vpos[v], bs->x.rv);
 }
 
-// drop-in calculateForces (+= into the body arrays)
-__global__ void kb_force_acc(BumpySys *bs) {
+// drop-in calculateForces (+= into the body arrays); walls = 1: calculateWallForces
+// then calculateForces
+__global__ void kb_force_acc(BumpySys *bs, int walls) {
     const int lane = threadIdx.x & 31;
     const int b = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
     if (b >= bs->b.p.n) return;
     double fx, fy, tq, pe;
-    body_forces(bs, b, lane, fx, fy, tq, pe);
+    body_forces(bs, b, lane, walls != 0, fx, fy, tq, pe);
     if (lane == 0) {
         double2 f = bs->b.v.frc[b];
         f.x += fx;
@@ -456,10 +476,21 @@ __global__ void kb_nve_second(BumpySys *bs, double dt_half) {
     const int b = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
     if (b < bs->b.p.n) {
         double fx, fy, tq, pe;
-        body_forces(bs, b, lane, fx, fy, tq, pe);
+        body_forces(bs, b, lane, bs->b.s.walls != 0, fx, fy, tq, pe);
         if (lane == 0) {
-            bs->b.v.frc[b] = make_double2(0.0 + fx, 0.0 + fy);
-            bs->x.tq[b] = 0.0 + tq;
+            const double g = bs->b.s.damping;
+            if (g != 0.0) {
+                // DampedNVE::step (src/integrator/damped_nve.cu:22-23) with
+                // kernelCalculateRigidDampedForces (kernels.cu:80-87): body
+                // F = 0 - g v, tau = 0 - g omega, then += the vertex sums
+                const double2 u = bs->b.v.vel[b];
+                const double w = bs->x.w[b];
+                bs->b.v.frc[b] = make_double2((0.0 - g * u.x) + fx, (0.0 - g * u.y) + fy);
+                bs->x.tq[b] = (0.0 - g * w) + tq;
+            } else {
+                bs->b.v.frc[b] = make_double2(0.0 + fx, 0.0 + fy);
+                bs->x.tq[b] = 0.0 + tq;
+            }
             bs->b.w.pe[b] = 0.0 + pe;
             body_kick(bs, b, dt_half);
         }
@@ -516,7 +547,7 @@ __global__ void kb_fire_force(BumpySys *bs, int mode, double tmax_target) {
     double v[4] = {0.0, 0.0, 0.0, 0.0};
     if (b < ds->p.n) {
         double fx, fy, tq, pe;
-        body_forces(bs, b, lane, fx, fy, tq, pe);
+        body_forces(bs, b, lane, false, fx, fy, tq, pe);
         if (lane == 0) {
             double2 f = make_double2(0.0 + fx, 0.0 + fy);
             ds->v.frc[b] = f;
@@ -707,6 +738,274 @@ __global__ void kb_scale(BumpySys *bs, double f) {
         q.x += (nx - p.x);
         q.y += (ny - p.y);
         bs->x.vpos[s0 + k] = q;
+    }
+}
+
+// ---- kernelCalculateRigidDampedForces (kernels.cu:80-87) ---------------------
+__global__ void kb_damp(BumpySys *bs, double g) {
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= bs->b.p.n) return;
+    double2 f = bs->b.v.frc[b], u = bs->b.v.vel[b];
+    f.x -= g * u.x;
+    f.y -= g * u.y;
+    bs->b.v.frc[b] = f;
+    bs->x.tq[b] -= g * bs->x.w[b];
+}
+
+// ---- calculateWallForces_onlyWallContacts (rigid_bumpy.cu:1495-1499): the wall
+// terms of every vertex (kernelCalcRigidBumpyWallForces, kernels.cu:348-362)
+// summed per body in vertex order (kernelCalcRigidBumpyParticleForces1), += into
+// the body arrays; one warp per body
+__global__ void kb_wall_only(BumpySys *bs) {
+    const int lane = threadIdx.x & 31;
+    const int b = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
+    if (b >= bs->b.p.n) return;
+    const DevSys &d = bs->b;
+    const BumpyExt &x = bs->x;
+    const double2 c = d.v.pos[b];
+    const int f = x.start[b], nvb = x.nvb[b];
+    double bfx = 0.0, bfy = 0.0, btq = 0.0, bpe = 0.0;
+    for (int base = 0; base < nvb; base += 32) {
+        int k = base + lane;
+        double vfx = 0.0, vfy = 0.0, vtq = 0.0, vpe = 0.0;
+        if (k < nvb) {
+            const double2 q = x.vpos[f + k];
+            double wx, wy;
+            const double we = wall_force(d.p, q, x.rv, wx, wy);
+            vfx = 0.0 + wx;
+            vfy = 0.0 + wy;
+            vtq = 0.0 + torque_of(wx, wy, q.x, q.y, c.x, c.y);
+            vpe = 0.0 + we;
+        }
+        int lim = min(32, nvb - base);
+        for (int l = 0; l < lim; l++) {
+            bfx += __shfl_sync(0xffffffffu, vfx, l);
+            bfy += __shfl_sync(0xffffffffu, vfy, l);
+            btq += __shfl_sync(0xffffffffu, vtq, l);
+            bpe += __shfl_sync(0xffffffffu, vpe, l);
+        }
+    }
+    if (lane == 0) {
+        double2 g = bs->b.v.frc[b];
+        g.x += bfx;
+        g.y += bfy;
+        bs->b.v.frc[b] = g;
+        bs->x.tq[b] += btq;
+        bs->b.w.pe[b] += bpe;
+    }
+}
+
+// ---- RigidBumpy::updatePositionsAdam: kernelRigidBumpyAdamStep then
+// kernelTranslateAndRotateVertices1 (rigid_bumpy.cu:1473-1486, kernels.cu:1004-1093,
+// 152-201), one warp per body.  The translational moments live in DevView (m1,
+// m2: swapped with their twins on a re-sort, never gathered), the angular ones
+// stay with the slot.  With rotation off the angle is left alone and the
+// vertices turn by the slot's last angle increment, as the reference's stale
+// angle_delta does (0 after any kick, which zeroes omega without rotation).
+__global__ void kb_adam(BumpySys *bs, double alpha, double b1, double b2, double c1, double c2,
+                        double eps) {
+    const int lane = threadIdx.x & 31;
+    const int b = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
+    double v[2] = {0.0, 0.0};
+    if (b < bs->b.p.n) {
+        DevSys &d = bs->b;
+        BumpyExt &x = bs->x;
+        const double2 f = d.v.frc[b], p = d.v.pos[b];
+        double2 m1 = d.v.m1[b], m2 = d.v.m2[b];
+        const double t = x.tq[b], ang = x.th[b], adel = x.adelta[b];
+        double m1a = x.m1a[b], m2a = x.m2a[b];
+        m1.x = fma(b1, m1.x, (b1 - 1) * f.x);
+        m1.y = fma(b1, m1.y, (b1 - 1) * f.y);
+        m1a = fma(b1, m1a, (b1 - 1) * t);
+        m2.x = fma(b2, m2.x, (1 - b2) * f.x * f.x);
+        m2.y = fma(b2, m2.y, (1 - b2) * f.y * f.y);
+        m2a = fma(b2, m2a, (1 - b2) * t * t);
+        const double ux = -alpha * (m1.x / c1) / (sqrt(m2.x / c2) + eps);
+        const double uy = -alpha * (m1.y / c1) / (sqrt(m2.y / c2) + eps);
+        const double ua = -alpha * (m1a / c1) / (sqrt(m2a / c2) + eps);
+        const double nx = p.x + ux, ny = p.y + uy;
+        const double dth = x.rotation ? ua : adel;
+        __syncwarp();
+        if (lane == 0) {
+            d.v.pos[b] = make_double2(nx, ny);
+            if (x.rotation) {
+                x.th[b] = ang + ua;
+                x.adelta[b] = ua;
+            }
+            d.v.m1[b] = m1;
+            d.v.m2[b] = m2;
+            x.m1a[b] = m1a;
+            x.m2a[b] = m2a;
+            const double2 a = d.w.pos_n[b], c = d.w.pos_c[b];
+            const double a1 = nx - a.x, a2 = ny - a.y, e1 = nx - c.x, e2 = ny - c.y;
+            v[0] = a1 * a1 + a2 * a2;
+            v[1] = e1 * e1 + e2 * e2;
+        }
+        const double ca = cos(dth), sa = sin(dth);
+        const int f0 = x.start[b], nvb = x.nvb[b];
+        for (int k = lane; k < nvb; k += 32) {
+            const double2 q = x.vpos[f0 + k];
+            const double rx = q.x - p.x, ry = q.y - p.y;
+            const double rxr = rx * ca - ry * sa, ryr = rx * sa + ry * ca;
+            const double2 nq = make_double2(nx + rxr, ny + ryr);
+            x.vpos[f0 + k] = nq;
+            if (x.mixed) x.vpk[f0 + k] = mixed_pack(d.p, nq, x.rv);
+        }
+    }
+    const int ops[2] = {1, 1};
+    if (grid_reduce<2>(v, ops, &bs->b)) { bs->b.s.max_nd2 = v[0]; bs->b.s.max_cd2 = v[1]; }
+}
+
+// ---- kernelCalcRigidBumpyStressTensor (kernels.cu:705-789): one thread per
+// body in the reference's accumulation order (per vertex: the kinetic term with
+// omega x r through atan2 / sin / cos when omega != 0, then half the virial of
+// each listed vertex of another body), divided by the box area.  Per-body
+// values go to stress_b, the component sums to DevState.stress.
+__global__ void kb_stress(BumpySys *bs) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    double v[4] = {0.0, 0.0, 0.0, 0.0};
+    const DevSys &d = bs->b;
+    const BumpyExt &x = bs->x;
+    const int nb = d.p.n;
+    if (b < nb) {
+        const int nv = x.nv, capv = x.capv;
+        const double bx = d.p.box[0], by = d.p.box[1], e_c = d.p.e_c, n_c = d.p.n_c, rv = x.rv;
+        const double2 c = d.v.pos[b], u = d.v.vel[b];
+        const double w = x.w[b];
+        double axx = 0.0, axy = 0.0, ayx = 0.0, ayy = 0.0;
+        const int f0 = x.start[b], nvb = x.nvb[b];
+        for (int k = 0; k < nvb; k++) {
+            const int vv = f0 + k;
+            const double2 q = x.vpos[vv];
+            const double mv = x.vmass[vv];
+            const double rx = q.x - c.x, ry = q.y - c.y;
+            const double prad = sqrt(rx * rx + ry * ry);
+            double wx = u.x, wy = u.y;
+            if (w != 0.0) {
+                const double a = atan2(ry, rx);
+                wx -= sin(a) * w * prad;
+                wy += cos(a) * w * prad;
+            }
+            axx += mv * wx * wx;
+            axy += mv * wx * wy;
+            ayx += mv * wy * wx;
+            ayy += mv * wy * wy;
+            const int cnt = min(x.vcount[vv], capv);
+            for (int t = 0; t < cnt; t++) {
+                const int o = x.vnbr[(size_t)t * nv + vv];
+                if (o == vv || x.vbody[o] == b) continue;
+                const double2 op = x.vpos[o];
+                const double dx = pbc_dist(q.x, op.x, bx), dy = pbc_dist(q.y, op.y, by);
+                double fx, fy;
+                disk_pair(q.x, q.y, rv, op.x, op.y, rv, bx, by, e_c, n_c, fx, fy);
+                axx += dx * fx / 2;
+                axy += dx * fy / 2;
+                ayx += dy * fx / 2;
+                ayy += dy * fy / 2;
+            }
+        }
+        const double area = bx * by;
+        v[0] = axx / area;
+        v[1] = axy / area;
+        v[2] = ayx / area;
+        v[3] = ayy / area;
+        for (int k = 0; k < 4; k++) x.stress_b[(size_t)k * nb + b] = v[k];
+    }
+    const int ops[4] = {0, 0, 0, 0};
+    if (grid_reduce<4>(v, ops, &bs->b))
+        for (int k = 0; k < 4; k++) bs->b.s.stress[k] = v[k];
+}
+
+// ---- kernelCountRigidBumpyContacts (kernels.cu:924-997): per body, the
+// neighbour bodies with at least one overlapping vertex pair, and per such
+// neighbour the overlapping partners of the first vertex (in body vertex
+// order) that has one.  Totals (getContactCount and the vertex count) go to
+// DevState.contacts and BumpyExt.vcontacts.
+__global__ void kb_contacts(BumpySys *bs) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    double v[2] = {0.0, 0.0};
+    const DevSys &d = bs->b;
+    const BumpyExt &x = bs->x;
+    const int nb = d.p.n;
+    if (b < nb) {
+        const int nv = x.nv, capv = x.capv;
+        const double bx = d.p.box[0], by = d.p.box[1], rs = 2 * x.rv;
+        const int nn = min(d.w.count[b], d.p.cap), f0 = x.start[b], nvb = x.nvb[b];
+        int nc = 0, nvc = 0;
+        for (int k = 0; k < nn; k++) {
+            const int ob = d.v.nbr[(size_t)k * nb + b];
+            if (ob == b) continue;
+            bool contact = false;
+            for (int i = 0; i < nvb; i++) {
+                const int vv = f0 + i;
+                const double2 q = x.vpos[vv];
+                const int cnt = min(x.vcount[vv], capv);
+                for (int t = 0; t < cnt; t++) {
+                    const int o = x.vnbr[(size_t)t * nv + vv];
+                    if (o == vv || x.vbody[o] != ob) continue;
+                    const double2 op = x.vpos[o];
+                    const double dx = pbc_dist(q.x, op.x, bx), dy = pbc_dist(q.y, op.y, by);
+                    if (sqrt(dx * dx + dy * dy) < rs) {
+                        if (!contact) nc++;
+                        nvc++;
+                        contact = true;
+                    }
+                }
+                if (contact) break;
+            }
+        }
+        x.ccount[b] = nc;
+        x.vccount[b] = nvc;
+        v[0] = (double)nc;
+        v[1] = (double)nvc;
+    }
+    const int ops[2] = {0, 0};
+    if (grid_reduce<2>(v, ops, &bs->b)) {
+        bs->b.s.contacts = v[0];
+        bs->x.vcontacts = v[1];
+    }
+}
+
+// per-body stress components [4][nb] and contact counts in static order
+__global__ void kb_get_stress_contacts(BumpySys *bs, double *stress, int *cc, int *vcc) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nb = bs->b.p.n;
+    if (b >= nb) return;
+    const int k = bs->b.v.sidx[b];
+    if (stress)
+        for (int c = 0; c < 4; c++) stress[(size_t)c * nb + k] = bs->x.stress_b[(size_t)c * nb + b];
+    if (cc) cc[k] = bs->x.ccount[b];
+    if (vcc) vcc[k] = bs->x.vccount[b];
+}
+
+// ---- RigidBumpy::setLastState (dir 0) / revertToLastStateVariables (dir 1)
+// (rigid_bumpy.cu:1144-1179 over particle.cu:956-985): slot-by-slot copies of
+// the body and vertex arrays the reference keeps; moments of inertia, vertex
+// masses, Adam moments and cell arrays are not part of the snapshot.
+__global__ void kb_snapshot(BumpySys *bs, int dir) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    DevView &v = bs->b.v;
+    DevScratch &w = bs->b.w;
+    BumpyExt &x = bs->x;
+    if (i < bs->b.p.n) {
+        if (dir == 0) {
+            w.s_pos[i] = v.pos[i]; w.s_vel[i] = v.vel[i]; w.s_frc[i] = v.frc[i];
+            w.s_rad[i] = v.rad[i]; w.s_mass[i] = v.mass[i]; w.s_sidx[i] = v.sidx[i];
+            x.s_w[i] = x.w[i]; x.s_th[i] = x.th[i]; x.s_tq[i] = x.tq[i];
+            x.s_nvb[i] = x.nvb[i]; x.s_start[i] = x.start[i];
+        } else {
+            v.pos[i] = w.s_pos[i]; v.vel[i] = w.s_vel[i]; v.frc[i] = w.s_frc[i];
+            v.rad[i] = w.s_rad[i]; v.mass[i] = w.s_mass[i]; v.sidx[i] = w.s_sidx[i];
+            x.w[i] = x.s_w[i]; x.th[i] = x.s_th[i]; x.tq[i] = x.s_tq[i];
+            x.nvb[i] = x.s_nvb[i]; x.start[i] = x.s_start[i];
+        }
+    }
+    if (i < x.nv) {
+        if (dir == 0) {
+            x.s_vpos[i] = x.vpos[i]; x.s_vbody[i] = x.vbody[i]; x.s_svidx[i] = x.svidx[i];
+        } else {
+            x.vpos[i] = x.s_vpos[i]; x.vbody[i] = x.s_vbody[i]; x.svidx[i] = x.s_svidx[i];
+        }
     }
 }
 

@@ -43,6 +43,8 @@ struct dpg_bumpy_system {
     cudaGraphExec_t loop_exec[2] = {nullptr, nullptr};
     cudaGraphConditionalHandle h_loop[2] = {0, 0}, h_rb[2] = {0, 0};
     double loop_dt = 0.0, loop_tmax = 0.0;
+    bool adam_ready = false, have_snapshot = false;
+    double snap_box[2] = {0.0, 0.0};
     double switch_fmax = 1e-6;  // mixed form: FP32 vertex pairs until max(|F|, |tau|) <= this
     int gb(int count) const { return std::max(1, (count + kTPB - 1) / kTPB); }
     int gw(int bodies) const { return std::max(1, (bodies + kWarpsPerBlock - 1) / kWarpsPerBlock); }
@@ -154,7 +156,14 @@ extern "C" int dpg_bumpy_create(const dpg_bumpy_params *p, void *cuda_stream, dp
     A((void **)&x.vmass_t, nv * 8); A((void **)&x.vbody, nv * 4); A((void **)&x.vbody_t, nv * 4);
     A((void **)&x.svidx, nv * 4); A((void **)&x.svidx_t, nv * 4); A((void **)&x.vcount, nv * 4);
     if (p->precision == DPG_MIXED) A((void **)&x.vpk, nv * 16);
-    A((void **)&s->xfer, std::max(nb, nv) * 16);
+    A((void **)&x.adelta, nb * 8); A((void **)&x.m1a, nb * 8); A((void **)&x.m2a, nb * 8);
+    A((void **)&x.stress_b, nb * 32); A((void **)&x.ccount, nb * 4); A((void **)&x.vccount, nb * 4);
+    A((void **)&w.s_pos, nb * 16); A((void **)&w.s_vel, nb * 16); A((void **)&w.s_frc, nb * 16);
+    A((void **)&w.s_rad, nb * 8); A((void **)&w.s_mass, nb * 8); A((void **)&w.s_sidx, nb * 4);
+    A((void **)&x.s_w, nb * 8); A((void **)&x.s_th, nb * 8); A((void **)&x.s_tq, nb * 8);
+    A((void **)&x.s_nvb, nb * 4); A((void **)&x.s_start, nb * 4); A((void **)&x.s_vpos, nv * 16);
+    A((void **)&x.s_vbody, nv * 4); A((void **)&x.s_svidx, nv * 4);
+    A((void **)&s->xfer, std::max(nb * 32, nv * 16));  // also 4 doubles per body (stress)
     A((void **)&s->d, sizeof(BumpySys));
     if (rc == DPG_OK) {
         cudaError_t e = cudaMallocHost((void **)&s->hs, sizeof(DevState));
@@ -245,6 +254,7 @@ extern "C" int dpg_bumpy_set_bodies(dpg_bumpy_handle s, const double *x, const d
     int acc = 0;
     for (int b = 0; b < s->nb; b++) { start[b] = acc; acc += nvb[b]; }
     CK(cudaMemcpyAsync(s->h.x.start, start.data(), 4 * (size_t)s->nb, cudaMemcpyHostToDevice, s->stream));
+    CK(cudaMemsetAsync(s->h.x.adelta, 0, 8 * (size_t)s->nb, s->stream));
     LAUNCH(k_iota_sidx, s->gb(s->nb), kTPB, &s->d->b);
     LAUNCH(kb_index_vertices, s->gw(s->nb), kTPB, s->d);
     LAUNCH(kb_init_vertices, s->gw(s->nb), kTPB, s->d);
@@ -503,7 +513,7 @@ extern "C" int dpg_bumpy_setup_neighbors(dpg_bumpy_handle s, const dpg_neighbor_
     TRY(rebuild_now(s, s->method == DPG_NEIGH_CELL ? 2 : 1));
     s->have_neighbors = true;
     TRY(vrefresh(s));
-    LAUNCH(kb_force_acc, s->gw(s->nb), kTPB, s->d);
+    LAUNCH(kb_force_acc, s->gw(s->nb), kTPB, s->d, 0);
     CK(cudaStreamSynchronize(s->stream));
     if (info) return dpg_bumpy_neighbor_info_get(s, info, nullptr);
     return DPG_OK;
@@ -558,7 +568,7 @@ extern "C" int dpg_bumpy_zero_forces(dpg_bumpy_handle s) {
 extern "C" int dpg_bumpy_compute_forces(dpg_bumpy_handle s) {
     TRY(need(s));
     TRY(vrefresh(s));
-    LAUNCH(kb_force_acc, s->gw(s->nb), kTPB, s->d);
+    LAUNCH(kb_force_acc, s->gw(s->nb), kTPB, s->d, 0);
     return DPG_OK;
 }
 
@@ -843,4 +853,146 @@ extern "C" int dpg_bumpy_fire_minimize(dpg_bumpy_handle s, const dpg_fire_params
     }
     TRY(put(s, &s->d->b.s.flags, 0));
     return DPG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Adam, damping, walls, stress, contacts, snapshots
+// ---------------------------------------------------------------------------
+extern "C" int dpg_bumpy_adam_init(dpg_bumpy_handle s) {
+    if (!s) return set_err(DPG_ERR_ARG, "null handle");
+    // every moment and the twins the translational ones swap with start at zero
+    const DevView &v = s->h.b.v;
+    double2 *bufs[4] = {v.m1, v.m2, v.m1_t, v.m2_t};
+    for (double2 *b : bufs) CK(cudaMemsetAsync(b, 0, 16 * (size_t)s->nb, s->stream));
+    CK(cudaMemsetAsync(s->h.x.m1a, 0, 8 * (size_t)s->nb, s->stream));
+    CK(cudaMemsetAsync(s->h.x.m2a, 0, 8 * (size_t)s->nb, s->stream));
+    s->adam_ready = true;
+    return DPG_OK;
+}
+
+extern "C" int dpg_bumpy_adam_step(dpg_bumpy_handle s, int64_t step, double alpha, double b1,
+                                   double b2, double eps) {
+    if (!s) return set_err(DPG_ERR_ARG, "null handle");
+    if (!s->adam_ready) return set_err(DPG_ERR_STATE, "call dpg_bumpy_adam_init first");
+    const double c1 = 1 - std::pow(b1, step + 1), c2 = 1 - std::pow(b2, step + 1);
+    LAUNCH(kb_adam, s->gw(s->nb), kTPB, s->d, alpha, b1, b2, c1, c2, eps);
+    return DPG_OK;
+}
+
+// minimizeAdam (src/routines/minimization.cu:3-33) over Adam::minimize
+// (src/integrator/adam.cu:11-17): zero, neighbour check, forces, Adam step,
+// then the PE test on the host, as the reference (its bias corrections are
+// host scalars)
+extern "C" int dpg_bumpy_adam_minimize(dpg_bumpy_handle s, double alpha, double b1, double b2,
+                                       double eps, double pe_target, double pe_diff_target,
+                                       int64_t max_steps, int64_t *steps) {
+    TRY(need(s));
+    TRY(dpg_bumpy_adam_init(s));
+    const double dof = (double)((int64_t)s->nb * (s->prm.rotation ? 3 : 2));
+    double last = 0.0;
+    int64_t step = 0;
+    while (step < max_steps) {
+        TRY(dpg_bumpy_zero_forces(s));
+        TRY(dpg_bumpy_check_neighbors(s, nullptr));
+        TRY(dpg_bumpy_compute_forces(s));
+        TRY(dpg_bumpy_adam_step(s, step, alpha, b1, b2, eps));
+        double pe = 0.0;
+        TRY(dpg_bumpy_observables(s, &pe, nullptr, nullptr, nullptr, nullptr));
+        const double avg = pe / dof, diff = std::fabs(avg / last - 1);
+        last = avg;
+        if (diff < pe_diff_target || avg < pe_target) break;
+        step++;
+    }
+    if (steps) *steps = step;
+    return DPG_OK;
+}
+
+extern "C" int dpg_bumpy_damped_forces(dpg_bumpy_handle s, double damping) {
+    if (!s) return set_err(DPG_ERR_ARG, "null handle");
+    LAUNCH(kb_damp, s->gb(s->nb), kTPB, s->d, damping);
+    return DPG_OK;
+}
+
+extern "C" int dpg_bumpy_damped_nve_steps(dpg_bumpy_handle s, double dt, double damping,
+                                          int64_t n_steps) {
+    if (!s) return set_err(DPG_ERR_ARG, "null handle");
+    TRY(put(s, &s->d->b.s.damping, damping));
+    int rc = dpg_bumpy_nve_steps(s, dt, n_steps);
+    int rc2 = put(s, &s->d->b.s.damping, 0.0);
+    return rc != DPG_OK ? rc : rc2;
+}
+
+extern "C" int dpg_bumpy_wall_forces(dpg_bumpy_handle s, int with_pairs) {
+    if (!s) return set_err(DPG_ERR_ARG, "null handle");
+    if (with_pairs) {
+        TRY(need(s));
+        TRY(vrefresh(s));
+        LAUNCH(kb_force_acc, s->gw(s->nb), kTPB, s->d, 1);
+    } else {
+        LAUNCH(kb_wall_only, s->gw(s->nb), kTPB, s->d);
+    }
+    return DPG_OK;
+}
+
+extern "C" int dpg_bumpy_nve_wall_steps(dpg_bumpy_handle s, double dt, int64_t n_steps) {
+    if (!s) return set_err(DPG_ERR_ARG, "null handle");
+    TRY(put(s, &s->d->b.s.walls, 1));
+    int rc = dpg_bumpy_nve_steps(s, dt, n_steps);
+    int rc2 = put(s, &s->d->b.s.walls, 0);
+    return rc != DPG_OK ? rc : rc2;
+}
+
+extern "C" int dpg_bumpy_stress(dpg_bumpy_handle s, double *stress, double *pressure,
+                                double *per_body) {
+    TRY(need(s));
+    LAUNCH(kb_stress, s->gb(s->nb), kTPB, s->d);
+    if (per_body) {
+        double *d0 = s->xfer;  // 4 * nb doubles fit: xfer holds 2 * max(nb, nv) double2
+        LAUNCH(kb_get_stress_contacts, s->gb(s->nb), kTPB, s->d, d0, (int *)nullptr, (int *)nullptr);
+        CK(cudaMemcpyAsync(per_body, d0, 32 * (size_t)s->nb, cudaMemcpyDeviceToHost, s->stream));
+    }
+    TRY(pull(s));
+    const double *t = s->hs->stress;
+    if (stress) for (int k = 0; k < 4; k++) stress[k] = t[k];
+    if (pressure) *pressure = (t[0] + t[3]) / 2;
+    return DPG_OK;
+}
+
+extern "C" int dpg_bumpy_contacts(dpg_bumpy_handle s, double *contacts, double *vertex_contacts,
+                                  int32_t *per_body, int32_t *vertex_per_body) {
+    TRY(need(s));
+    LAUNCH(kb_contacts, s->gb(s->nb), kTPB, s->d);
+    if (per_body || vertex_per_body) {
+        int *c0 = (int *)s->xfer, *c1 = c0 + s->nb;
+        LAUNCH(kb_get_stress_contacts, s->gb(s->nb), kTPB, s->d, (double *)nullptr, c0, c1);
+        if (per_body) CK(cudaMemcpyAsync(per_body, c0, 4 * (size_t)s->nb, cudaMemcpyDeviceToHost, s->stream));
+        if (vertex_per_body)
+            CK(cudaMemcpyAsync(vertex_per_body, c1, 4 * (size_t)s->nb, cudaMemcpyDeviceToHost, s->stream));
+    }
+    TRY(pull(s));
+    if (contacts) *contacts = s->hs->contacts;
+    if (vertex_contacts) *vertex_contacts = s->hx->vcontacts;
+    return DPG_OK;
+}
+
+extern "C" int dpg_bumpy_save_state(dpg_bumpy_handle s) {
+    if (!s) return set_err(DPG_ERR_ARG, "null handle");
+    LAUNCH(kb_snapshot, s->gb(std::max(s->nb, s->nv)), kTPB, s->d, 0);
+    s->snap_box[0] = s->h.b.p.box[0];
+    s->snap_box[1] = s->h.b.p.box[1];
+    s->have_snapshot = true;
+    return DPG_OK;
+}
+
+extern "C" int dpg_bumpy_restore_state(dpg_bumpy_handle s) {
+    TRY(need(s));
+    if (!s->have_snapshot) return set_err(DPG_ERR_STATE, "call dpg_bumpy_save_state first");
+    LAUNCH(kb_snapshot, s->gb(std::max(s->nb, s->nv)), kTPB, s->d, 1);
+    // Particle::setBoxSize: the box only; the cell size keeps its value
+    s->h.b.p.box[0] = s->snap_box[0];
+    s->h.b.p.box[1] = s->snap_box[1];
+    mixed_grid_update(s->h.b.p);
+    CK(cudaMemcpyAsync(&s->d->b.p, &s->h.b.p, sizeof(DevParams), cudaMemcpyHostToDevice, s->stream));
+    TRY(rebuild_now(s, 1));
+    return vrefresh(s);
 }

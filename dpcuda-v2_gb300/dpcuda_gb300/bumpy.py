@@ -10,8 +10,8 @@ import ctypes as C
 import numpy as np
 
 from .disk import _METHODS
-from .lib import (D, DP, I32P, BumpyParams, FireParams, FireResult, NeighborConfig, NeighborInfo,
-                  check, load_library)
+from .lib import (D, DP, I32P, I64, BumpyParams, FireParams, FireResult, NeighborConfig,
+                  NeighborInfo, check, load_library)
 
 
 def _d(a):
@@ -172,3 +172,82 @@ class RigidBumpy:
 
     def scaleBox(self, factor):
         check(self.lib.dpg_bumpy_scale_box(self.h, float(factor)))
+
+    # ---- Adam (RigidBumpy::updatePositionsAdam, minimizeAdam) ------------------
+    def initAdamVariables(self):
+        check(self.lib.dpg_bumpy_adam_init(self.h))
+
+    def updatePositionsAdam(self, step, alpha, beta1, beta2, epsilon):
+        check(self.lib.dpg_bumpy_adam_step(self.h, int(step), float(alpha), float(beta1),
+                                           float(beta2), float(epsilon)))
+
+    def adamMinimizeStep(self, step, alpha=1e-4, beta1=0.9, beta2=0.999, epsilon=1e-8):
+        """Adam::minimize(step): zero, neighbour check, forces, Adam update."""
+        self.zeroForceAndPotentialEnergy()
+        self.checkForNeighborUpdate()
+        self.calculateForces()
+        self.updatePositionsAdam(step, alpha, beta1, beta2, epsilon)
+
+    def minimizeAdam(self, alpha=1e-4, beta1=0.9, beta2=0.999, epsilon=1e-8, avg_pe_target=1e-16,
+                     avg_pe_diff_target=1e-16, num_steps=100000):
+        steps = I64()
+        check(self.lib.dpg_bumpy_adam_minimize(self.h, float(alpha), float(beta1), float(beta2),
+                                               float(epsilon), float(avg_pe_target),
+                                               float(avg_pe_diff_target), int(num_steps),
+                                               C.byref(steps)))
+        return steps.value
+
+    # ---- DampedNVE and walls ------------------------------------------------------
+    def calculateDampedForces(self, damping_coefficient):
+        check(self.lib.dpg_bumpy_damped_forces(self.h, float(damping_coefficient)))
+
+    def dampedNveSteps(self, dt, damping_coefficient, n):
+        check(self.lib.dpg_bumpy_damped_nve_steps(self.h, float(dt), float(damping_coefficient),
+                                                  int(n)))
+
+    def calculateWallForces_onlyWallContacts(self):
+        check(self.lib.dpg_bumpy_wall_forces(self.h, 0))
+
+    def calculateWallAndPairForces(self):
+        """calculateWallForces() then calculateForces(), as NVE::wall_step calls them."""
+        check(self.lib.dpg_bumpy_wall_forces(self.h, 1))
+
+    def nveWallSteps(self, dt, n):
+        check(self.lib.dpg_bumpy_nve_wall_steps(self.h, float(dt), int(n)))
+
+    # ---- stress, pressure, contacts ----------------------------------------------
+    def calculateStressTensor(self):
+        """(component sums [xx, xy, yx, yy], per-body components (4, nb) in static order)."""
+        t = np.zeros(4)
+        per = np.zeros((4, self.nb))
+        p = D()
+        check(self.lib.dpg_bumpy_stress(self.h, t.ctypes.data_as(DP), C.byref(p),
+                                        per.ctypes.data_as(DP)))
+        return t, per
+
+    def getPressure(self):
+        p = D()
+        check(self.lib.dpg_bumpy_stress(self.h, None, C.byref(p), None))
+        return p.value
+
+    def countContacts(self):
+        """(getContactCount, getVertexContactCount, per-body contacts, per-body
+        vertex contacts), static order."""
+        c, vc = D(), D()
+        cc = np.zeros(self.nb, dtype=np.int32)
+        vcc = np.zeros(self.nb, dtype=np.int32)
+        check(self.lib.dpg_bumpy_contacts(self.h, C.byref(c), C.byref(vc), cc.ctypes.data_as(I32P),
+                                          vcc.ctypes.data_as(I32P)))
+        return c.value, vc.value, cc, vcc
+
+    def getContactCount(self):
+        c = D()
+        check(self.lib.dpg_bumpy_contacts(self.h, C.byref(c), None, None, None))
+        return c.value
+
+    # ---- setLastState / revertToLastState ----------------------------------------
+    def setLastState(self):
+        check(self.lib.dpg_bumpy_save_state(self.h))
+
+    def revertToLastState(self):
+        check(self.lib.dpg_bumpy_restore_state(self.h))

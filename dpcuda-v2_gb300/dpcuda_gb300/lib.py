@@ -180,6 +180,17 @@ SIGNATURES = {
     "dpg_bumpy_fire_minimize": [VP, C.POINTER(FireParams), D, C.POINTER(FireResult)],
     "dpg_bumpy_set_mixed_switch": [VP, D],
     "dpg_bumpy_scale_box": [VP, D],
+    "dpg_bumpy_adam_init": [VP],
+    "dpg_bumpy_adam_step": [VP, I64, D, D, D, D],
+    "dpg_bumpy_adam_minimize": [VP, D, D, D, D, D, D, I64, I64P],
+    "dpg_bumpy_damped_forces": [VP, D],
+    "dpg_bumpy_damped_nve_steps": [VP, D, D, I64],
+    "dpg_bumpy_wall_forces": [VP, I32],
+    "dpg_bumpy_nve_wall_steps": [VP, D, I64],
+    "dpg_bumpy_stress": [VP, DP, DP, DP],
+    "dpg_bumpy_contacts": [VP, DP, DP, I32P, I32P],
+    "dpg_bumpy_save_state": [VP],
+    "dpg_bumpy_restore_state": [VP],
 }
 _RESTYPES = {"dpg_last_error": C.c_char_p}
 

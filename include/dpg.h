@@ -395,6 +395,42 @@ int dpg_bumpy_fire_minimize(dpg_bumpy_handle h, const dpg_fire_params *p, double
                             dpg_fire_result *r);
 /* scalePositionsFull (rigid_bumpy.cu:1044-1048) with the box: Particle::scaleBox */
 int dpg_bumpy_scale_box(dpg_bumpy_handle h, double factor);
+/* RigidBumpy::initAdamVariables / updatePositionsAdam (rigid_bumpy.cu:1461-1486,
+ * kernels.cu:1004-1093): translational and angular moments; the translational
+ * ones follow the reference's re-sort (swapped with never-gathered twins), the
+ * angular ones stay with their slot */
+int dpg_bumpy_adam_init(dpg_bumpy_handle h);
+int dpg_bumpy_adam_step(dpg_bumpy_handle h, int64_t step, double alpha, double beta1,
+                        double beta2, double epsilon);
+/* minimizeAdam (src/routines/minimization.cu:3-33) with dof = 3 N (rotation) or 2 N;
+ * *steps = the final step index */
+int dpg_bumpy_adam_minimize(dpg_bumpy_handle h, double alpha, double beta1, double beta2,
+                            double epsilon, double avg_pe_target, double avg_pe_diff_target,
+                            int64_t max_steps, int64_t *steps);
+/* RigidBumpy::calculateDampedForces (rigid_bumpy.cu:1501-1503): F -= g v, tau -= g omega */
+int dpg_bumpy_damped_forces(dpg_bumpy_handle h, double damping);
+/* DampedNVE::step (src/integrator/damped_nve.cu:15-25) n times, device-resident */
+int dpg_bumpy_damped_nve_steps(dpg_bumpy_handle h, double dt, double damping, int64_t n_steps);
+/* with_pairs = 0: calculateWallForces_onlyWallContacts (rigid_bumpy.cu:1495-1499);
+ * with_pairs = 1: calculateWallForces then calculateForces (the pair NVE::wall_step
+ * calls); += into the body arrays.  Walls at 0 and L on both axes
+ * (calcWallInteraction, include/particles/base/kernels.cuh:185-235) act on vertices */
+int dpg_bumpy_wall_forces(dpg_bumpy_handle h, int with_pairs);
+/* NVE::wall_step (src/integrator/nve.cu:27-38) n times, device-resident */
+int dpg_bumpy_nve_wall_steps(dpg_bumpy_handle h, double dt, int64_t n_steps);
+/* calculateStressTensor + getPressure / getStressTensor (rigid_bumpy.cu:1513-1519,
+ * kernels.cu:705-789, particle.cu:1371-1385).  stress = {xx, xy, yx, yy} sums;
+ * per_body (nullable, host, 4 * n_bodies: [component][body], static order) */
+int dpg_bumpy_stress(dpg_bumpy_handle h, double *stress, double *pressure, double *per_body);
+/* countContacts + getContactCount / getVertexContactCount (rigid_bumpy.cu:1505-1511,
+ * 779-781, kernels.cu:924-997); per-body arrays nullable, host, static order */
+int dpg_bumpy_contacts(dpg_bumpy_handle h, double *contacts, double *vertex_contacts,
+                       int32_t *per_body, int32_t *vertex_per_body);
+/* setLastState / revertToLastState (rigid_bumpy.cu:1144-1179, particle.cu:956-991):
+ * device-side snapshot; the revert restores the box and rebuilds the body and
+ * vertex lists from the cell arrays as they are */
+int dpg_bumpy_save_state(dpg_bumpy_handle h);
+int dpg_bumpy_restore_state(dpg_bumpy_handle h);
 
 /* ======================================================================
  *  Ensembles: the batched form.  Many independent disk systems of uneven

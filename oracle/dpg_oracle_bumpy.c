@@ -50,6 +50,16 @@ typedef struct orcb_sys {
     double f_alpha, f_alpha0, f_dt, f_dtmax, f_dtmin;
     int64_t f_ngood, f_nbad;
     int f_stopped;
+    /* Adam moments: the translational ones are swapped with never-gathered
+     * twins on a re-sort, the angular ones stay with their slot */
+    double *m1x, *m1y, *m2x, *m2y, *tm1x, *tm1y, *tm2x, *tm2y, *m1a, *m2a;
+    /* per-body stress tensor and contact counts */
+    double *sxx, *sxy, *syx, *syy;
+    int64_t *cc, *vcc;
+    /* setLastState snapshot */
+    double *s_x, *s_y, *s_vx, *s_vy, *s_fx, *s_fy, *s_r, *s_m, *s_th, *s_w, *s_tq, *s_px, *s_py;
+    int64_t *s_pidx, *s_sidx, *s_nvb, *s_start, *s_vbody, *s_svidx;
+    double s_box[2];
 } orcb_sys;
 
 static double *dz(int64_t n) { return (double *)calloc((size_t)(n > 0 ? n : 1), sizeof(double)); }
@@ -91,14 +101,21 @@ orcb_sys *orcb_create(int64_t nb, int64_t nv, double bx, double by, double e_c, 
     double **bd[] = {&s->x, &s->y, &s->th, &s->vx, &s->vy, &s->w, &s->fx, &s->fy, &s->tq, &s->pe,
                      &s->m, &s->r, &s->I, &s->ke, &s->lpx, &s->lpy, &s->dx, &s->dy, &s->dth,
                      &s->tx, &s->ty, &s->tth, &s->tvx, &s->tvy, &s->tw, &s->tfx, &s->tfy, &s->ttq,
-                     &s->tm, &s->tr, &s->tI, &s->lnx, &s->lny, &s->lcx, &s->lcy, &s->nd2, &s->cd2};
+                     &s->tm, &s->tr, &s->tI, &s->lnx, &s->lny, &s->lcx, &s->lcy, &s->nd2, &s->cd2,
+                     &s->m1x, &s->m1y, &s->m2x, &s->m2y, &s->tm1x, &s->tm1y, &s->tm2x, &s->tm2y,
+                     &s->m1a, &s->m2a, &s->sxx, &s->sxy, &s->syx, &s->syy, &s->s_x, &s->s_y,
+                     &s->s_vx, &s->s_vy, &s->s_fx, &s->s_fy, &s->s_r, &s->s_m, &s->s_th, &s->s_w,
+                     &s->s_tq};
     for (size_t k = 0; k < sizeof(bd) / sizeof(bd[0]); k++) *bd[k] = dz(nb);
     int64_t **bl[] = {&s->nvb, &s->start, &s->tnvb, &s->tstart, &s->o2n, &s->cell_index, &s->pidx,
-                      &s->sidx, &s->key_tmp, &s->pidx_tmp, &s->sidx_tmp, &s->ncount};
+                      &s->sidx, &s->key_tmp, &s->pidx_tmp, &s->sidx_tmp, &s->ncount, &s->cc,
+                      &s->vcc, &s->s_pidx, &s->s_sidx, &s->s_nvb, &s->s_start};
     for (size_t k = 0; k < sizeof(bl) / sizeof(bl[0]); k++) *bl[k] = lz(nb);
-    double **vd[] = {&s->px, &s->py, &s->vfx, &s->vfy, &s->vtq, &s->vpe, &s->vm, &s->tpx, &s->tpy, &s->tvm};
+    double **vd[] = {&s->px, &s->py, &s->vfx, &s->vfy, &s->vtq, &s->vpe, &s->vm, &s->tpx, &s->tpy,
+                     &s->tvm, &s->s_px, &s->s_py};
     for (size_t k = 0; k < sizeof(vd) / sizeof(vd[0]); k++) *vd[k] = dz(nv);
-    int64_t **vl[] = {&s->vbody, &s->svidx, &s->tvbody, &s->tsvidx, &s->vncount};
+    int64_t **vl[] = {&s->vbody, &s->svidx, &s->tvbody, &s->tsvidx, &s->vncount, &s->s_vbody,
+                      &s->s_svidx};
     for (size_t k = 0; k < sizeof(vl) / sizeof(vl[0]); k++) *vl[k] = lz(nv);
     for (int64_t i = 0; i < nb; i++) { s->pidx[i] = i; s->sidx[i] = i; }
     for (int64_t v = 0; v < nv; v++) s->svidx[v] = v;
@@ -119,7 +136,11 @@ void orcb_destroy(orcb_sys *s) {
                     s->cell_index, s->pidx, s->sidx, s->key_tmp, s->pidx_tmp, s->sidx_tmp,
                     s->ncount, s->px, s->py, s->vfx, s->vfy, s->vtq, s->vpe, s->vm, s->tpx, s->tpy,
                     s->tvm, s->vbody, s->svidx, s->tvbody, s->tsvidx, s->vncount, s->nlist,
-                    s->vnlist, s->cell_start};
+                    s->vnlist, s->cell_start, s->m1x, s->m1y, s->m2x, s->m2y, s->tm1x, s->tm1y,
+                    s->tm2x, s->tm2y, s->m1a, s->m2a, s->sxx, s->sxy, s->syx, s->syy, s->cc, s->vcc,
+                    s->s_x, s->s_y, s->s_vx, s->s_vy, s->s_fx, s->s_fy, s->s_r, s->s_m, s->s_th,
+                    s->s_w, s->s_tq, s->s_px, s->s_py, s->s_pidx, s->s_sidx, s->s_nvb, s->s_start,
+                    s->s_vbody, s->s_svidx};
     for (size_t k = 0; k < sizeof(ptrs) / sizeof(ptrs[0]); k++) free(ptrs[k]);
     free(s);
 }
@@ -384,6 +405,9 @@ static void update_cell_list(orcb_sys *s) {
     SWAPP(s->nvb, s->tnvb); SWAPP(s->start, s->tstart);
     SWAPP(s->px, s->tpx); SWAPP(s->py, s->tpy); SWAPP(s->vm, s->tvm);
     SWAPP(s->vbody, s->tvbody); SWAPP(s->svidx, s->tsvidx);
+    /* first_moment.swap(), second_moment.swap() without a gather (rigid_bumpy.cu:1370-1371);
+     * the angular moments are neither gathered nor swapped */
+    SWAPP(s->m1x, s->tm1x); SWAPP(s->m1y, s->tm1y); SWAPP(s->m2x, s->tm2x); SWAPP(s->m2y, s->tm2y);
     s->n_cell_rebuilds++;
 }
 
@@ -654,6 +678,330 @@ int64_t orcb_minimize_fire(orcb_sys *s, double alpha_init, double dt, double pe_
     orcb_set_velocities_zero(s);
     if (stopped_out) *stopped_out = s->f_stopped;
     return step;
+}
+
+/* ---------------- Adam --------------------------------------------------- */
+/* RigidBumpy::initAdamVariables (rigid_bumpy.cu:1461-1465): every moment, and
+ * the twins the translational ones swap with, starts at zero */
+void orcb_adam_init(orcb_sys *s) {
+    double *arr[] = {s->m1x, s->m1y, s->m2x, s->m2y, s->tm1x, s->tm1y, s->tm2x, s->tm2y, s->m1a, s->m2a};
+    for (size_t k = 0; k < sizeof(arr) / sizeof(arr[0]); k++)
+        for (int64_t b = 0; b < s->nb; b++) arr[k][b] = 0.0;
+}
+
+/* RigidBumpy::updatePositionsAdam: kernelRigidBumpyAdamStep then
+ * kernelTranslateAndRotateVertices1 (rigid_bumpy.cu:1473-1486,
+ * kernels.cu:1004-1093,152-201).  With rotation off the angle and its delta
+ * are left alone, so the vertices turn by the slot's last angle delta. */
+void orcb_adam_step(orcb_sys *s, int64_t step, double alpha, double b1, double b2, double eps) {
+    const double c1 = 1 - pow(b1, step + 1), c2 = 1 - pow(b2, step + 1);
+    for (int64_t b = 0; b < s->nb; b++) {
+        double fx = s->fx[b], fy = s->fy[b], t = s->tq[b];
+        double m1x = fma(b1, s->m1x[b], (b1 - 1) * fx);
+        double m1y = fma(b1, s->m1y[b], (b1 - 1) * fy);
+        double m1a = fma(b1, s->m1a[b], (b1 - 1) * t);
+        double m2x = fma(b2, s->m2x[b], (1 - b2) * fx * fx);
+        double m2y = fma(b2, s->m2y[b], (1 - b2) * fy * fy);
+        double m2a = fma(b2, s->m2a[b], (1 - b2) * t * t);
+        double ux = -alpha * (m1x / c1) / (sqrt(m2x / c2) + eps);
+        double uy = -alpha * (m1y / c1) / (sqrt(m2y / c2) + eps);
+        double ua = -alpha * (m1a / c1) / (sqrt(m2a / c2) + eps);
+        double px = s->x[b], py = s->y[b];
+        s->lpx[b] = px; s->lpy[b] = py;
+        px += ux; py += uy;
+        s->dx[b] = ux; s->dy[b] = uy;
+        if (s->rotation) { s->th[b] += ua; s->dth[b] = ua; }
+        s->x[b] = px; s->y[b] = py;
+        double a1 = px - s->lnx[b], a2 = py - s->lny[b];
+        s->nd2[b] = a1 * a1 + a2 * a2;
+        double e1 = px - s->lcx[b], e2 = py - s->lcy[b];
+        s->cd2[b] = e1 * e1 + e2 * e2;
+        s->m1x[b] = m1x; s->m1y[b] = m1y; s->m1a[b] = m1a;
+        s->m2x[b] = m2x; s->m2y[b] = m2y; s->m2a[b] = m2a;
+    }
+    for (int64_t v = 0; v < s->nv; v++) {
+        int64_t b = s->vbody[v];
+        double rx = s->px[v] - s->lpx[b], ry = s->py[v] - s->lpy[b];
+        double ca = cos(s->dth[b]), sa = sin(s->dth[b]);
+        s->px[v] = s->x[b] + (rx * ca - ry * sa);
+        s->py[v] = s->y[b] + (rx * sa + ry * ca);
+    }
+}
+
+/* minimizeAdam (src/routines/minimization.cu:3-33) with Adam::minimize
+ * (src/integrator/adam.cu:11-17); dof = n_dof = 3 N with rotation, else 2 N
+ * (rigid_bumpy.cu:618-624).  Returns the final step index. */
+int64_t orcb_minimize_adam(orcb_sys *s, double alpha, double b1, double b2, double eps,
+                           double pe_target, double pe_diff_target, int64_t num_steps) {
+    orcb_adam_init(s);
+    int64_t step = 0;
+    double dof = (double)(s->nb * (s->rotation ? 3 : 2)), last = 0.0;
+    while (step < num_steps) {
+        orcb_zero(s);
+        orcb_check_for_neighbor_update(s);
+        orcb_calculate_forces(s);
+        orcb_adam_step(s, step, alpha, b1, b2, eps);
+        double avg = orcb_total_pe(s) / dof;
+        double diff = fabs(avg / last - 1);
+        last = avg;
+        if (diff < pe_diff_target || avg < pe_target) break;
+        step++;
+    }
+    return step;
+}
+
+/* n steps of Adam::minimize (src/integrator/adam.cu:11-17) without the stop test */
+void orcb_adam_steps(orcb_sys *s, double alpha, double b1, double b2, double eps, int64_t n) {
+    orcb_adam_init(s);
+    for (int64_t t = 0; t < n; t++) {
+        orcb_zero(s);
+        orcb_check_for_neighbor_update(s);
+        orcb_calculate_forces(s);
+        orcb_adam_step(s, t, alpha, b1, b2, eps);
+    }
+}
+
+/* ---------------- damping and walls --------------------------------------- */
+/* kernelCalculateRigidDampedForces: kernels.cu:80-87 */
+void orcb_damped_forces(orcb_sys *s, double g) {
+    for (int64_t b = 0; b < s->nb; b++) {
+        s->fx[b] -= g * s->vx[b];
+        s->fy[b] -= g * s->vy[b];
+        s->tq[b] -= g * s->w[b];
+    }
+}
+
+/* DampedNVE::step with the rigid overrides: src/integrator/damped_nve.cu:15-25 */
+void orcb_damped_nve_steps(orcb_sys *s, double dt, double g, int64_t n) {
+    for (int64_t t = 0; t < n; t++) {
+        orcb_update_velocities(s, 0.5 * dt);
+        orcb_update_positions(s, dt);
+        orcb_check_for_neighbor_update(s);
+        orcb_zero(s);
+        orcb_damped_forces(s, g);
+        orcb_calculate_forces(s);
+        orcb_update_velocities(s, 0.5 * dt);
+    }
+}
+
+/* calcWallInteraction: include/particles/base/kernels.cuh:185-235 (box walls
+ * at 0 and L on both axes) */
+static double bwall(const orcb_sys *s, double x, double y, double rad, double *fx, double *fy) {
+    double en = 0.0;
+    const double pos[4] = {x, x, y, y};
+    const double dist[4] = {x, s->box[0] - x, y, s->box[1] - y};
+    *fx = 0.0; *fy = 0.0;
+    for (int k = 0; k < 4; k++) {
+        int near = (k % 2 == 0) ? (pos[k] < rad) : (pos[k] > s->box[k / 2] - rad);
+        if (!near) continue;
+        double ov = rad - dist[k];
+        if (!(ov > 0)) continue;
+        double ovp = pow(ov / rad, s->n_c - 1);
+        double f = s->e_c * ovp / rad;
+        if (k == 0) *fx += f;
+        else if (k == 1) *fx -= f;
+        else if (k == 2) *fy += f;
+        else *fy -= f;
+        en += s->e_c * ov * ovp / (s->n_c * rad);
+    }
+    return en;
+}
+
+/* kernelCalcRigidBumpyWallForces (kernels.cu:348-362): += into the vertex
+ * arrays, torque about the body centre without the minimum image */
+void orcb_wall_forces(orcb_sys *s) {
+    for (int64_t v = 0; v < s->nv; v++) {
+        int64_t b = s->vbody[v];
+        double fx, fy;
+        double e = bwall(s, s->px[v], s->py[v], s->rv, &fx, &fy);
+        double rx = s->px[v] - s->x[b], ry = s->py[v] - s->y[b];
+        s->vfx[v] += fx; s->vfy[v] += fy; s->vtq[v] += fy * rx - fx * ry; s->vpe[v] += e;
+    }
+}
+
+/* calculateWallForces_onlyWallContacts (rigid_bumpy.cu:1495-1499): the wall
+ * terms, then kernelCalcRigidBumpyParticleForces1's per-body sums */
+void orcb_wall_only(orcb_sys *s) {
+    orcb_wall_forces(s);
+    for (int64_t b = 0; b < s->nb; b++) {
+        double ax = 0.0, ay = 0.0, at = 0.0, en = 0.0;
+        for (int64_t k = 0; k < s->nvb[b]; k++) {
+            int64_t v = s->start[b] + k;
+            ax += s->vfx[v]; ay += s->vfy[v]; at += s->vtq[v]; en += s->vpe[v];
+        }
+        s->fx[b] += ax; s->fy[b] += ay; s->tq[b] += at; s->pe[b] += en;
+    }
+}
+
+/* calculateWallForces then calculateForces, the pair NVE::wall_step calls */
+void orcb_wall_and_pair_forces(orcb_sys *s) {
+    orcb_wall_forces(s);
+    orcb_calculate_forces(s);
+}
+
+/* NVE::wall_step with the rigid overrides: src/integrator/nve.cu:27-38 */
+void orcb_nve_wall_steps(orcb_sys *s, double dt, int64_t n) {
+    for (int64_t t = 0; t < n; t++) {
+        orcb_update_velocities(s, 0.5 * dt);
+        orcb_update_positions(s, dt);
+        orcb_check_for_neighbor_update(s);
+        orcb_zero(s);
+        orcb_wall_forces(s);
+        orcb_calculate_forces(s);
+        orcb_update_velocities(s, 0.5 * dt);
+    }
+}
+
+/* ---------------- stress, pressure, contacts ------------------------------ */
+/* kernelCalcRigidBumpyStressTensor (kernels.cu:705-789): per body, the kinetic
+ * term of every vertex (body velocity plus omega x r through atan2 / sin /
+ * cos when omega != 0) and half the virial of its vertex contacts with other
+ * bodies, in vertex then list order, divided by the box area.  out = the four
+ * component sums over bodies (xx, xy, yx, yy). */
+void orcb_stress(orcb_sys *s, double *out) {
+    const double area = s->box[0] * s->box[1];
+#pragma omp parallel for schedule(static) if (s->nb >= PAR_MIN)
+    for (int64_t b = 0; b < s->nb; b++) {
+        double axx = 0.0, axy = 0.0, ayx = 0.0, ayy = 0.0;
+        double cx = s->x[b], cy = s->y[b], ux = s->vx[b], uy = s->vy[b], w = s->w[b];
+        for (int64_t k = 0; k < s->nvb[b]; k++) {
+            int64_t v = s->start[b] + k;
+            double qx = s->px[v], qy = s->py[v], mv = s->vm[v];
+            double rx = qx - cx, ry = qy - cy;
+            double prad = sqrt(rx * rx + ry * ry);
+            double wx = ux, wy = uy;
+            if (w != 0.0) {
+                double a = atan2(ry, rx);
+                wx -= sin(a) * w * prad;
+                wy += cos(a) * w * prad;
+            }
+            axx += mv * wx * wx;
+            axy += mv * wx * wy;
+            ayx += mv * wy * wx;
+            ayy += mv * wy * wy;
+            for (int64_t t = 0; t < s->vncount[v]; t++) {
+                int64_t u = s->vnlist[v * s->vcap + t];
+                if (u == -1 || u == v || s->vbody[u] == b) continue;
+                double dx = bpbc(qx, s->px[u], s->box[0]);
+                double dy = bpbc(qy, s->py[u], s->box[1]);
+                double fx, fy;
+                vpair(s, qx, qy, s->px[u], s->py[u], &fx, &fy);
+                axx += dx * fx / 2;
+                axy += dx * fy / 2;
+                ayx += dy * fx / 2;
+                ayy += dy * fy / 2;
+            }
+        }
+        s->sxx[b] = axx / area; s->sxy[b] = axy / area; s->syx[b] = ayx / area; s->syy[b] = ayy / area;
+    }
+    double t[4] = {0, 0, 0, 0};
+    for (int64_t b = 0; b < s->nb; b++) { t[0] += s->sxx[b]; t[1] += s->sxy[b]; t[2] += s->syx[b]; t[3] += s->syy[b]; }
+    if (out) for (int k = 0; k < 4; k++) out[k] = t[k];
+}
+
+/* getPressure after calculateStressTensor (src/particles/base/particle.cu:1371-1376) */
+double orcb_pressure(orcb_sys *s) {
+    double t[4];
+    orcb_stress(s, t);
+    return (t[0] + t[3]) / 2;
+}
+
+/* kernelCountRigidBumpyContacts (kernels.cu:924-997): a neighbour body counts
+ * once if any vertex pair of the two bodies overlaps; the vertex count adds,
+ * per neighbour body, the overlapping partners of the FIRST vertex (in body
+ * vertex order) that has one.  Returns getContactCount (the sum of the body
+ * counts). */
+double orcb_count_contacts(orcb_sys *s) {
+    const double rs = 2 * s->rv;
+#pragma omp parallel for schedule(static) if (s->nb >= PAR_MIN)
+    for (int64_t b = 0; b < s->nb; b++) {
+        int64_t nc = 0, nvc = 0;
+        for (int64_t k = 0; k < s->ncount[b]; k++) {
+            int64_t ob = s->nlist[b * s->cap + k];
+            if (ob == -1 || ob == b) continue;
+            int contact = 0;
+            for (int64_t i = 0; i < s->nvb[b]; i++) {
+                int64_t v = s->start[b] + i;
+                for (int64_t t = 0; t < s->vncount[v]; t++) {
+                    int64_t u = s->vnlist[v * s->vcap + t];
+                    if (u == -1 || u == v || s->vbody[u] != ob) continue;
+                    double dx = bpbc(s->px[v], s->px[u], s->box[0]);
+                    double dy = bpbc(s->py[v], s->py[u], s->box[1]);
+                    if (sqrt(dx * dx + dy * dy) < rs) {
+                        if (!contact) nc++;
+                        nvc++;
+                        contact = 1;
+                    }
+                }
+                if (contact) break;
+            }
+        }
+        s->cc[b] = nc;
+        s->vcc[b] = nvc;
+    }
+    int64_t tot = 0;
+    for (int64_t b = 0; b < s->nb; b++) tot += s->cc[b];
+    return (double)tot;
+}
+
+/* per-body stress components and contact counts in static order */
+void orcb_get_stress(const orcb_sys *s, double *sxx, double *sxy, double *syx, double *syy) {
+    for (int64_t b = 0; b < s->nb; b++) {
+        int64_t k = s->sidx[b];
+        if (sxx) sxx[k] = s->sxx[b];
+        if (sxy) sxy[k] = s->sxy[b];
+        if (syx) syx[k] = s->syx[b];
+        if (syy) syy[k] = s->syy[b];
+    }
+}
+
+void orcb_get_contacts(const orcb_sys *s, int64_t *cc, int64_t *vcc) {
+    for (int64_t b = 0; b < s->nb; b++) {
+        int64_t k = s->sidx[b];
+        if (cc) cc[k] = s->cc[b];
+        if (vcc) vcc[k] = s->vcc[b];
+    }
+}
+
+/* ---------------- setLastState / revertToLastState ------------------------- */
+/* RigidBumpy::setLastState (rigid_bumpy.cu:1144-1166 over particle.cu:956-973) */
+void orcb_save_state(orcb_sys *s) {
+    const size_t B = (size_t)s->nb * sizeof(double), L = (size_t)s->nb * sizeof(int64_t);
+    const size_t VB = (size_t)s->nv * sizeof(double), VL = (size_t)s->nv * sizeof(int64_t);
+    memcpy(s->s_x, s->x, B); memcpy(s->s_y, s->y, B); memcpy(s->s_vx, s->vx, B);
+    memcpy(s->s_vy, s->vy, B); memcpy(s->s_fx, s->fx, B); memcpy(s->s_fy, s->fy, B);
+    memcpy(s->s_r, s->r, B); memcpy(s->s_m, s->m, B); memcpy(s->s_th, s->th, B);
+    memcpy(s->s_w, s->w, B); memcpy(s->s_tq, s->tq, B);
+    memcpy(s->s_pidx, s->pidx, L); memcpy(s->s_sidx, s->sidx, L);
+    memcpy(s->s_nvb, s->nvb, L); memcpy(s->s_start, s->start, L);
+    memcpy(s->s_px, s->px, VB); memcpy(s->s_py, s->py, VB);
+    memcpy(s->s_vbody, s->vbody, VL); memcpy(s->s_svidx, s->svidx, VL);
+    s->s_box[0] = s->box[0]; s->s_box[1] = s->box[1];
+}
+
+/* RigidBumpy::revertToLastStateVariables + Particle::revertToLastState
+ * (rigid_bumpy.cu:1168-1179, particle.cu:975-991): the saved arrays go back
+ * slot by slot; moments of inertia, vertex masses, Adam moments and the cell
+ * arrays stay as they are; then the box and updateNeighborList (body list
+ * from the current cell arrays, then the vertex list) */
+void orcb_restore_state(orcb_sys *s) {
+    const size_t B = (size_t)s->nb * sizeof(double), L = (size_t)s->nb * sizeof(int64_t);
+    const size_t VB = (size_t)s->nv * sizeof(double), VL = (size_t)s->nv * sizeof(int64_t);
+    memcpy(s->x, s->s_x, B); memcpy(s->y, s->s_y, B); memcpy(s->vx, s->s_vx, B);
+    memcpy(s->vy, s->s_vy, B); memcpy(s->fx, s->s_fx, B); memcpy(s->fy, s->s_fy, B);
+    memcpy(s->r, s->s_r, B); memcpy(s->m, s->s_m, B); memcpy(s->th, s->s_th, B);
+    memcpy(s->w, s->s_w, B); memcpy(s->tq, s->s_tq, B);
+    memcpy(s->pidx, s->s_pidx, L); memcpy(s->sidx, s->s_sidx, L);
+    memcpy(s->nvb, s->s_nvb, L); memcpy(s->start, s->s_start, L);
+    memcpy(s->px, s->s_px, VB); memcpy(s->py, s->s_py, VB);
+    memcpy(s->vbody, s->s_vbody, VL); memcpy(s->svidx, s->s_svidx, VL);
+    s->box[0] = s->s_box[0]; s->box[1] = s->s_box[1];
+    update_body_list(s, s->method == ORC_NEIGH_CELL);
+}
+
+void orcb_get_box(const orcb_sys *s, double *bx, double *by) {
+    if (bx) *bx = s->box[0];
+    if (by) *by = s->box[1];
 }
 
 /* ---------------- state access -------------------------------------------- */

@@ -429,6 +429,19 @@ _BSIGS = {
     "get_vertices": (None, [P, DP, DP]),
     "get_vertex_neighbors": (I64, [P, LP, LP]),
     "neighbor_info": (None, [P, C.POINTER(C.c_int), DP, DP, DP, LP, LP, LP, LP]),
+    "adam_init": (None, [P]),
+    "adam_step": (None, [P, I64, D, D, D, D]),
+    "adam_steps": (None, [P, D, D, D, D, I64]),
+    "damped_nve_steps": (None, [P, D, D, I64]),
+    "wall_only": (None, [P]),
+    "wall_and_pair_forces": (None, [P]),
+    "nve_wall_steps": (None, [P, D, I64]),
+    "stress": (None, [P, DP]),
+    "count_contacts": (D, [P]),
+    "get_stress": (None, [P, DP, DP, DP, DP]),
+    "get_contacts": (None, [P, LP, LP]),
+    "save_state": (None, [P]),
+    "restore_state": (None, [P]),
 }
 _blibs: dict[str, C.CDLL] = {}
 
@@ -446,6 +459,10 @@ def _bload(kind):
             lib.orcb_minimize_fire.argtypes = [P, D, D, D, D, I64, D, D, C.POINTER(C.c_int)]
             lib.orcb_vertex_radius.restype = D
             lib.orcb_vertex_radius.argtypes = [D, I64, D]
+            lib.orcb_minimize_adam.restype = I64
+            lib.orcb_minimize_adam.argtypes = [P, D, D, D, D, D, D, I64]
+            lib.orcb_damped_forces.restype = None
+            lib.orcb_damped_forces.argtypes = [P, D]
         _blibs[kind] = lib
     return lib, prefix
 
@@ -546,6 +563,65 @@ class BumpyOracle:
                                         float(pe_diff_target), int(num_steps), float(fmax),
                                         float(tmax), C.byref(st))
         return n, st.value
+
+    def adam_init(self):
+        self._f("adam_init")(self.h)
+
+    def adam_step(self, step, alpha=1e-4, beta1=0.9, beta2=0.999, eps=1e-8):
+        self._f("adam_step")(self.h, int(step), float(alpha), float(beta1), float(beta2), float(eps))
+
+    def adam_steps(self, n, alpha=1e-4, beta1=0.9, beta2=0.999, eps=1e-8):
+        """n steps of Adam::minimize from fresh moments (no stop test)."""
+        self._f("adam_steps")(self.h, float(alpha), float(beta1), float(beta2), float(eps), int(n))
+
+    def minimize_adam(self, alpha=1e-4, beta1=0.9, beta2=0.999, eps=1e-8, pe_target=1e-16,
+                      pe_diff_target=1e-16, num_steps=100000):
+        return self.lib.orcb_minimize_adam(self.h, float(alpha), float(beta1), float(beta2),
+                                           float(eps), float(pe_target), float(pe_diff_target),
+                                           int(num_steps))
+
+    def damped_forces(self, gamma):
+        self.lib.orcb_damped_forces(self.h, float(gamma))
+
+    def damped_nve_steps(self, dt, gamma, n):
+        self._f("damped_nve_steps")(self.h, float(dt), float(gamma), int(n))
+
+    def wall_only(self):
+        self._f("wall_only")(self.h)
+
+    def wall_and_pair_forces(self):
+        self._f("wall_and_pair_forces")(self.h)
+
+    def nve_wall_steps(self, dt, n):
+        self._f("nve_wall_steps")(self.h, float(dt), int(n))
+
+    def stress(self):
+        """calculateStressTensor: (component sums [xx, xy, yx, yy], per-body
+        components in static order as a (4, nb) array)."""
+        t = np.zeros(4)
+        self._f("stress")(self.h, _dp(t))
+        per = np.zeros((4, self.nb))
+        self._f("get_stress")(self.h, *[_dp(per[k]) for k in range(4)])
+        return t, per
+
+    def pressure(self):
+        t, _ = self.stress()
+        return (t[0] + t[3]) / 2
+
+    def count_contacts(self):
+        """countContacts: (getContactCount, per-body contacts, per-body vertex
+        contacts), static order."""
+        tot = self._f("count_contacts")(self.h)
+        cc = np.zeros(self.nb, dtype=np.int64)
+        vcc = np.zeros(self.nb, dtype=np.int64)
+        self._f("get_contacts")(self.h, _lp(cc), _lp(vcc))
+        return tot, cc, vcc
+
+    def save_state(self):
+        self._f("save_state")(self.h)
+
+    def restore_state(self):
+        self._f("restore_state")(self.h)
 
     def bodies(self):
         out = {k: np.zeros(self.nb) for k in self.BODY_KEYS}

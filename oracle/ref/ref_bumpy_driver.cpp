@@ -54,6 +54,14 @@ struct refb_sys {
     double f_alpha, f_alpha0, f_dt, f_dtmax, f_dtmin;
     long f_ngood = 0, f_nbad = 0;
     int f_stopped = 0;
+    // Adam moments (first_moment / second_moment and their swap twins, the angular ones)
+    dvec m1x, m1y, m2x, m2y, tm1x, tm1y, tm2x, tm2y, m1a, m2a;
+    dvec sxx, sxy, syx, syy;
+    lvec cc, vcc;
+    // setLastState copies
+    dvec s_x, s_y, s_vx, s_vy, s_fx, s_fy, s_r, s_m, s_th, s_w, s_tq, s_px, s_py;
+    lvec s_pidx, s_sidx, s_nvb, s_start, s_vbody, s_svidx;
+    double s_box[2] = {0, 0};
 };
 
 static void bsync(refb_sys *s) {
@@ -90,10 +98,12 @@ refb_sys *refb_create(int64_t nb, int64_t nv, double bx, double by, double e_c, 
     dvec *bd[] = {&s->x, &s->y, &s->th, &s->vx, &s->vy, &s->w, &s->fx, &s->fy, &s->tq, &s->pe,
                   &s->m, &s->r, &s->I, &s->ke, &s->lpx, &s->lpy, &s->dx, &s->dy, &s->dth, &s->tx,
                   &s->ty, &s->tth, &s->tvx, &s->tvy, &s->tw, &s->tfx, &s->tfy, &s->ttq, &s->tm,
-                  &s->tr, &s->tI, &s->lnx, &s->lny, &s->lcx, &s->lcy, &s->nd2, &s->cd2};
+                  &s->tr, &s->tI, &s->lnx, &s->lny, &s->lcx, &s->lcy, &s->nd2, &s->cd2,
+                  &s->m1x, &s->m1y, &s->m2x, &s->m2y, &s->tm1x, &s->tm1y, &s->tm2x, &s->tm2y,
+                  &s->m1a, &s->m2a, &s->sxx, &s->sxy, &s->syx, &s->syy};
     for (dvec *d : bd) d->assign(nb, 0.0);
     lvec *bl[] = {&s->nvb, &s->start, &s->tnvb, &s->tstart, &s->o2n, &s->cell_index, &s->pidx,
-                  &s->sidx, &s->ncount};
+                  &s->sidx, &s->ncount, &s->cc, &s->vcc};
     for (lvec *l : bl) l->assign(nb, 0);
     dvec *vd[] = {&s->px, &s->py, &s->vfx, &s->vfy, &s->vtq, &s->vpe, &s->vm, &s->tpx, &s->tpy, &s->tvm};
     for (dvec *d : vd) d->assign(nv, 0.0);
@@ -277,6 +287,9 @@ static void update_cell_list(refb_sys *s) {
     std::swap(s->nvb, s->tnvb); std::swap(s->start, s->tstart);
     std::swap(s->px, s->tpx); std::swap(s->py, s->tpy); std::swap(s->vm, s->tvm);
     std::swap(s->vbody, s->tvbody); std::swap(s->svidx, s->tsvidx);
+    // first_moment.swap(); second_moment.swap() (rigid_bumpy.cu:1370-1371), no gather
+    std::swap(s->m1x, s->tm1x); std::swap(s->m1y, s->tm1y);
+    std::swap(s->m2x, s->tm2x); std::swap(s->m2y, s->tm2y);
     bsync(s);
     long width = s->ncells > 0 ? s->nb / s->ncells : 0;
     launchb(s->ncells, [&] { kernelGetFirstParticleIndexForCell(s->cell_index.data(), s->cell_start.data(), 2, width); });
@@ -498,6 +511,162 @@ int64_t refb_get_vertex_neighbors(refb_sys *s, int64_t *list, int64_t *counts) {
         }
     }
     return s->vcap;
+}
+
+// ---- Adam: RigidBumpy::initAdamVariables / updatePositionsAdam (rigid_bumpy.cu:1461-1486)
+void refb_adam_init(refb_sys *s) {
+    dvec *m[] = {&s->m1x, &s->m1y, &s->m2x, &s->m2y, &s->tm1x, &s->tm1y, &s->tm2x, &s->tm2y, &s->m1a, &s->m2a};
+    for (dvec *d : m) std::fill(d->begin(), d->end(), 0.0);
+}
+
+void refb_adam_step(refb_sys *s, int64_t step, double alpha, double b1, double b2, double eps) {
+    double c1 = 1 - std::pow(b1, step + 1), c2 = 1 - std::pow(b2, step + 1);
+    bsync(s);
+    launchb(s->nb, [&] {
+        kernelRigidBumpyAdamStep(s->lpx.data(), s->lpy.data(), s->m1x.data(), s->m1y.data(), s->m1a.data(),
+                                 s->m2x.data(), s->m2y.data(), s->m2a.data(), s->x.data(), s->y.data(),
+                                 s->th.data(), s->dx.data(), s->dy.data(), s->dth.data(), s->fx.data(),
+                                 s->fy.data(), s->tq.data(), alpha, b1, b2, c1, c2, eps, s->lnx.data(),
+                                 s->lny.data(), s->nd2.data(), s->lcx.data(), s->lcy.data(), s->cd2.data(),
+                                 s->rotation);
+    });
+    launchb(s->nv, [&] {
+        kernelTranslateAndRotateVertices1(s->lpx.data(), s->lpy.data(), s->x.data(), s->y.data(),
+                                          s->px.data(), s->py.data(), s->dx.data(), s->dy.data(),
+                                          s->dth.data());
+    });
+}
+
+// Adam::minimize steps (src/integrator/adam.cu:11-17) without the stop test
+void refb_adam_steps(refb_sys *s, double alpha, double b1, double b2, double eps, int64_t n) {
+    refb_adam_init(s);
+    for (int64_t t = 0; t < n; t++) {
+        refb_zero(s);
+        refb_check_for_neighbor_update(s);
+        refb_calculate_forces(s);
+        refb_adam_step(s, t, alpha, b1, b2, eps);
+    }
+}
+
+// ---- DampedNVE::step (src/integrator/damped_nve.cu:15-25) with RigidBumpy::calculateDampedForces
+void refb_damped_nve_steps(refb_sys *s, double dt, double g, int64_t n) {
+    for (int64_t t = 0; t < n; t++) {
+        refb_update_velocities(s, 0.5 * dt);
+        refb_update_positions(s, dt);
+        refb_check_for_neighbor_update(s);
+        refb_zero(s);
+        bsync(s);
+        launchb(s->nb, [&] {
+            kernelCalculateRigidDampedForces(s->fx.data(), s->fy.data(), s->tq.data(), s->vx.data(),
+                                             s->vy.data(), s->w.data(), g);
+        });
+        refb_calculate_forces(s);
+        refb_update_velocities(s, 0.5 * dt);
+    }
+}
+
+// ---- walls: RigidBumpy::calculateWallForces (rigid_bumpy.cu:1488-1493)
+static void wall_kernel(refb_sys *s) {
+    bsync(s);
+    launchb(s->nv, [&] {
+        kernelCalcRigidBumpyWallForces(s->x.data(), s->y.data(), s->px.data(), s->py.data(),
+                                       s->vfx.data(), s->vfy.data(), s->vtq.data(), s->vpe.data());
+    });
+}
+
+// calculateWallForces_onlyWallContacts (rigid_bumpy.cu:1495-1499)
+void refb_wall_only(refb_sys *s) {
+    wall_kernel(s);
+    launchb(s->nb, [&] {
+        kernelCalcRigidBumpyParticleForces1(s->vfx.data(), s->vfy.data(), s->vtq.data(), s->vpe.data(),
+                                            s->fx.data(), s->fy.data(), s->tq.data(), s->pe.data());
+    });
+}
+
+// calculateWallForces then calculateForces, as NVE::wall_step calls them
+void refb_wall_and_pair_forces(refb_sys *s) {
+    wall_kernel(s);
+    refb_calculate_forces(s);
+}
+
+// NVE::wall_step (src/integrator/nve.cu:27-38)
+void refb_nve_wall_steps(refb_sys *s, double dt, int64_t n) {
+    for (int64_t t = 0; t < n; t++) {
+        refb_update_velocities(s, 0.5 * dt);
+        refb_update_positions(s, dt);
+        refb_check_for_neighbor_update(s);
+        refb_zero(s);
+        wall_kernel(s);
+        refb_calculate_forces(s);
+        refb_update_velocities(s, 0.5 * dt);
+    }
+}
+
+// ---- calculateStressTensor + getPressure (rigid_bumpy.cu:1513-1519, particle.cu:1371-1376);
+// the component sums run in body order here (thrust::reduce in the reference)
+void refb_stress(refb_sys *s, double *out) {
+    bsync(s);
+    launchb(s->nb, [&] {
+        kernelCalcRigidBumpyStressTensor(s->x.data(), s->y.data(), s->vx.data(), s->vy.data(), s->w.data(),
+                                         s->px.data(), s->py.data(), s->vm.data(), s->sxx.data(),
+                                         s->sxy.data(), s->syx.data(), s->syy.data());
+    });
+    double t[4] = {0, 0, 0, 0};
+    for (long b = 0; b < s->nb; b++) { t[0] += s->sxx[b]; t[1] += s->sxy[b]; t[2] += s->syx[b]; t[3] += s->syy[b]; }
+    for (int k = 0; k < 4; k++) out[k] = t[k];
+}
+
+// ---- countContacts (rigid_bumpy.cu:1505-1511) + getContactCount
+double refb_count_contacts(refb_sys *s) {
+    std::fill(s->cc.begin(), s->cc.end(), 0L);
+    std::fill(s->vcc.begin(), s->vcc.end(), 0L);
+    bsync(s);
+    launchb(s->nb, [&] {
+        kernelCountRigidBumpyContacts(s->x.data(), s->y.data(), s->px.data(), s->py.data(), s->r.data(),
+                                      s->cc.data(), s->vcc.data());
+    });
+    long tot = 0;
+    for (long v : s->cc) tot += v;
+    return (double)tot;
+}
+
+void refb_get_stress(refb_sys *s, double *sxx, double *sxy, double *syx, double *syy) {
+    for (long b = 0; b < s->nb; b++) {
+        long k = s->sidx[b];
+        if (sxx) sxx[k] = s->sxx[b];
+        if (sxy) sxy[k] = s->sxy[b];
+        if (syx) syx[k] = s->syx[b];
+        if (syy) syy[k] = s->syy[b];
+    }
+}
+
+void refb_get_contacts(refb_sys *s, int64_t *cc, int64_t *vcc) {
+    for (long b = 0; b < s->nb; b++) {
+        long k = s->sidx[b];
+        if (cc) cc[k] = s->cc[b];
+        if (vcc) vcc[k] = s->vcc[b];
+    }
+}
+
+// ---- RigidBumpy::setLastState / revertToLastStateVariables + Particle::revertToLastState
+// (rigid_bumpy.cu:1144-1179, particle.cu:956-991)
+void refb_save_state(refb_sys *s) {
+    s->s_x = s->x; s->s_y = s->y; s->s_vx = s->vx; s->s_vy = s->vy; s->s_fx = s->fx; s->s_fy = s->fy;
+    s->s_r = s->r; s->s_m = s->m; s->s_th = s->th; s->s_w = s->w; s->s_tq = s->tq;
+    s->s_px = s->px; s->s_py = s->py;
+    s->s_pidx = s->pidx; s->s_sidx = s->sidx; s->s_nvb = s->nvb; s->s_start = s->start;
+    s->s_vbody = s->vbody; s->s_svidx = s->svidx;
+    s->s_box[0] = s->box[0]; s->s_box[1] = s->box[1];
+}
+
+void refb_restore_state(refb_sys *s) {
+    s->x = s->s_x; s->y = s->s_y; s->vx = s->s_vx; s->vy = s->s_vy; s->fx = s->s_fx; s->fy = s->s_fy;
+    s->r = s->s_r; s->m = s->s_m; s->th = s->s_th; s->w = s->s_w; s->tq = s->s_tq;
+    s->px = s->s_px; s->py = s->s_py;
+    s->pidx = s->s_pidx; s->sidx = s->s_sidx; s->nvb = s->s_nvb; s->start = s->s_start;
+    s->vbody = s->s_vbody; s->svidx = s->s_svidx;
+    s->box[0] = s->s_box[0]; s->box[1] = s->s_box[1];
+    update_body_list(s, s->method == 0);
 }
 
 void refb_neighbor_info(refb_sys *s, int *method, double *cutoff, double *vcutoff, double *thr2,

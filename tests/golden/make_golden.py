@@ -199,11 +199,12 @@ def padded_sets(sets):
     return out
 
 
-def bumpy_snapshot(b: BumpyOracle, prefix: str, d: dict):
+def bumpy_snapshot(b: BumpyOracle, prefix: str, d: dict, vertices: bool = True):
     bd = b.bodies()
     for k in ("x", "y", "th", "vx", "vy", "w", "fx", "fy", "tq", "pe"):
         d[f"{prefix}_{k}"] = bd[k]
-    d[f"{prefix}_px"], d[f"{prefix}_py"] = b.vertices()
+    if vertices:
+        d[f"{prefix}_px"], d[f"{prefix}_py"] = b.vertices()
 
 
 def make_bumpy(nb, phi, seed, name):
@@ -230,6 +231,76 @@ def make_bumpy(nb, phi, seed, name):
     np.savez_compressed(HERE / name, **d)
 
 
+def make_bumpy_extras():
+    """Rigid bumpy bodies beyond FIRE and NVE, from the reference's own kernels:
+    stress tensor and contact counts (with translational and angular
+    velocities, so the kinetic term's omega x r branch runs), DampedNVE,
+    NVE::wall_step, the wall-only and wall-plus-pair force calls, Adam steps
+    across cell re-sorts, and setLastState / revertToLastState across re-sorts
+    (cell displacement multiplier 0.05 makes the re-sorts frequent)."""
+    nb, seed = 128, 7
+    st = bumpy_packing(nb, 0.80, seed, kind="reference")
+    vx = fill_normal(nb, 0.0, np.sqrt(1e-3), 1, seed)
+    vy = fill_normal(nb, 0.0, np.sqrt(1e-3), 1 + nb, seed)
+    w = fill_normal(nb, 0.0, np.sqrt(1e-3), 1 + 2 * nb, seed)
+    vx -= vx.mean()
+    vy -= vy.mean()
+    d = dict(x0=st["x"], y0=st["y"], th0=st["th"], r=st["r"], nvb=st["nvb"], box=st["box"],
+             rv=st["rv"], e_c=st["e_c"], seg=st["seg"], vx0=vx, vy0=vy, w0=w)
+
+    def fresh(cdm=0.5):
+        b = BumpyOracle(nb, st["nv"], st["box"], st["e_c"], 2.0, st["rv"], st["seg"], True,
+                        kind="reference")
+        b.set_bodies(st["x"], st["y"], st["th"], st["r"], st["nvb"], vx, vy, w)
+        b.init_vertices()
+        b.set_mass(1.0)
+        b.setup_neighbors(0, 1.5, 0.2, 8.0, cdm)
+        return b
+
+    def info(b):
+        i = b.neighbor_info()
+        return np.array([i["n_rebuilds"], i["n_cell_rebuilds"]])
+
+    b = fresh()
+    d["method"] = b.neighbor_info()["method"]
+    bumpy_snapshot(b, "setup", d)
+    d["stress_tot"], d["stress_body"] = b.stress()
+    d["contacts_tot"], d["contacts_body"], d["vcontacts_body"] = b.count_contacts()
+    b.zero()
+    b.wall_only()
+    bumpy_snapshot(b, "wallonly", d, vertices=False)
+    b.zero()
+    b.wall_and_pair_forces()
+    bumpy_snapshot(b, "wallpair", d, vertices=False)
+    b = fresh()
+    b.damped_nve_steps(5e-3, 0.5, 200)
+    bumpy_snapshot(b, "damped", d)
+    d["damped_info"] = info(b)
+    b = fresh()
+    b.nve_wall_steps(5e-3, 200)
+    bumpy_snapshot(b, "walls", d)
+    d["walls_info"] = info(b)
+    b = fresh(0.05)
+    b.adam_steps(150, 1e-2)
+    bumpy_snapshot(b, "adam", d)
+    d["adam_info"] = info(b)
+    assert d["adam_info"][1] > 1, "Adam run should cross a cell re-sort"
+    b = fresh(0.05)
+    b.save_state()
+    b.fire_init(0.1, 1e-2)
+    for _ in range(100):
+        b.fire_step()
+    d["revert_pre_info"] = info(b)
+    assert d["revert_pre_info"][1] > 1, "FIRE run should cross a cell re-sort"
+    b.restore_state()
+    bumpy_snapshot(b, "revert", d)
+    b.zero()
+    b.calculate_forces()
+    bumpy_snapshot(b, "revertf", d, vertices=False)
+    d["revert_info"] = info(b)
+    np.savez_compressed(HERE / "bumpy_n128_extras.npz", **d)
+
+
 if __name__ == "__main__":
     if build_reference() is None:
         sys.exit("reference tree not available; cannot regenerate fixtures")
@@ -246,4 +317,5 @@ if __name__ == "__main__":
     make_pairs()
     make_bumpy(64, 0.80, 3, "bumpy_n64_verlet.npz")
     make_bumpy(256, 0.80, 5, "bumpy_n256_cell.npz")
+    make_bumpy_extras()
     print("fixtures written to", HERE)
