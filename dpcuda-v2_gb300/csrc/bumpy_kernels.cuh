@@ -856,6 +856,45 @@ __global__ void kb_adam(BumpySys *bs, double alpha, double b1, double b2, double
     if (grid_reduce<2>(v, ops, &bs->b)) { bs->b.s.max_nd2 = v[0]; bs->b.s.max_cd2 = v[1]; }
 }
 
+// ---- rigid gradient descent (no reference kernel: the reference's GradDesc on
+// rigid bodies runs the disk kernelGradDescStep, src/particles/base/kernels.cu:
+// 613-637, on the body centres only).  x += alpha F as that kernel, theta +=
+// alpha tau with rotation, vertices translated and rotated with the body as in
+// kernelTranslateAndRotateVertices1; one warp per body.
+__global__ void kb_grad_desc(BumpySys *bs, double alpha) {
+    const int lane = threadIdx.x & 31;
+    const int b = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
+    double v[2] = {0.0, 0.0};
+    if (b < bs->b.p.n) {
+        DevSys &d = bs->b;
+        BumpyExt &x = bs->x;
+        const double2 f = d.v.frc[b], p = d.v.pos[b];
+        const double ang = x.th[b];
+        const double nx = p.x + alpha * f.x, ny = p.y + alpha * f.y;
+        const double dth = x.rotation ? alpha * x.tq[b] : 0.0;
+        __syncwarp();
+        if (lane == 0) {
+            d.v.pos[b] = make_double2(nx, ny);
+            if (x.rotation) x.th[b] = ang + dth;
+            const double2 a = d.w.pos_n[b], c = d.w.pos_c[b];
+            const double a1 = nx - a.x, a2 = ny - a.y, e1 = nx - c.x, e2 = ny - c.y;
+            v[0] = a1 * a1 + a2 * a2;
+            v[1] = e1 * e1 + e2 * e2;
+        }
+        const double ca = cos(dth), sa = sin(dth);
+        const int f0 = x.start[b], nvb = x.nvb[b];
+        for (int k = lane; k < nvb; k += 32) {
+            const double2 q = x.vpos[f0 + k];
+            const double rx = q.x - p.x, ry = q.y - p.y;
+            const double2 nq = make_double2(nx + (rx * ca - ry * sa), ny + (rx * sa + ry * ca));
+            x.vpos[f0 + k] = nq;
+            if (x.mixed) x.vpk[f0 + k] = mixed_pack(d.p, nq, x.rv);
+        }
+    }
+    const int ops[2] = {1, 1};
+    if (grid_reduce<2>(v, ops, &bs->b)) { bs->b.s.max_nd2 = v[0]; bs->b.s.max_cd2 = v[1]; }
+}
+
 // ---- kernelCalcRigidBumpyStressTensor (kernels.cu:705-789): one thread per
 // body in the reference's accumulation order (per vertex: the kinetic term with
 // omega x r through atan2 / sin / cos when omega != 0, then half the virial of
@@ -963,6 +1002,138 @@ __global__ void kb_contacts(BumpySys *bs) {
     if (grid_reduce<2>(v, ops, &bs->b)) {
         bs->b.s.contacts = v[0];
         bs->x.vcontacts = v[1];
+    }
+}
+
+// ---- RigidBumpy::calculateForceDistancePairs (rigid_bumpy.cu:1383-1459) with
+// kernelCalcRigidBumpyForceDistancePairs (kernels.cu:482-703): one thread per
+// body in the reference's order; entry [slot * cap + k] for the k-th listed
+// neighbour body.  Array order: see dpg_bumpy_pair_dump in include/dpg.h.
+constexpr int kBumpyPairArrays = 30;
+constexpr double kPi = 3.14159265358979323846;
+
+struct BumpyPairOut {
+    double *d[kBumpyPairArrays];
+    long long *this_id, *other_id, *vcount;
+};
+
+__global__ void kb_pair_fill(BumpyPairOut o, long long m) {
+    long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= m) return;
+    // the resizeAndFill values of calculateForceDistancePairs
+#pragma unroll
+    for (int k = 0; k < kBumpyPairArrays; k++) {
+        const double f = (k == 0 || (k >= 3 && k <= 10)) ? -1.0 : 0.0;
+        if (o.d[k]) o.d[k][q] = f;
+    }
+    o.this_id[q] = -1;
+    o.other_id[q] = -1;
+    o.vcount[q] = -1;
+}
+
+__global__ void kb_pair_dump(BumpySys *bs, BumpyPairOut o) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    const DevSys &d = bs->b;
+    const BumpyExt &x = bs->x;
+    const int nb = d.p.n, cap = d.p.cap;
+    if (b >= nb) return;
+    const int nn = min(d.w.count[b], cap);
+    if (nn == 0) return;
+    const int nv = x.nv, capv = x.capv;
+    const double bx = d.p.box[0], by = d.p.box[1], e_c = d.p.e_c, n_c = d.p.n_c, rv = x.rv;
+    const double rs = rv * 2.0;
+    const double2 c = d.v.pos[b];
+    const double thi = x.th[b], rad = d.v.rad[b];
+    const int f0 = x.start[b], nvb = x.nvb[b];
+    for (int k = 0; k < nn; k++) {
+        const int ob = d.v.nbr[(size_t)k * nb + b];
+        if (ob == b) continue;
+        const double2 oc = d.v.pos[ob];
+        const double thj = x.th[ob], orad = d.v.rad[ob];
+        const int of = x.start[ob], onvb = x.nvb[ob];
+        double fx = 0.0, fy = 0.0, en = 0.0, vov = 0.0;
+        long long vci = 0;
+        double hij[9], hii[9];
+#pragma unroll
+        for (int e = 0; e < 9; e++) { hij[e] = 0.0; hii[e] = 0.0; }
+        for (int u = 0; u < nvb; u++) {
+            const int v = f0 + u;
+            const double2 q = x.vpos[v];
+            const double phu = (double)(u * 2) * kPi / (double)nvb;
+            const double rdx = q.x - c.x, rdy = q.y - c.y;
+            const double Ri = sqrt(rdx * rdx + rdy * rdy);
+            bool contact = false;
+            const int cnt = min(x.vcount[v], capv);
+            for (int t = 0; t < cnt; t++) {
+                const int w = x.vnbr[(size_t)t * nv + v];
+                if (w == v || x.vbody[w] != ob) continue;
+                const double2 wp = x.vpos[w];
+                const int iv = w - of;
+                const double phv = (double)(iv * 2) * kPi / (double)onvb;
+                const double odx = wp.x - oc.x, ody = wp.y - oc.y;
+                const double Rj = sqrt(odx * odx + ody * ody);
+                double tfx, tfy;
+                const double te = disk_pair(q.x, q.y, rv, wp.x, wp.y, rv, bx, by, e_c, n_c, tfx, tfy);
+                en += te;
+                fx += tfx;
+                fy += tfy;
+                if (te > 0.0) {
+                    contact = true;
+                    const double dx = pbc_dist(q.x, wp.x, bx), dy = pbc_dist(q.y, wp.y, by);
+                    vov += rs - sqrt(dx * dx + dy * dy);
+                    const double dist = sqrt(dx * dx + dy * dy);
+                    const double tij = -e_c / rs * (1 - dist / rs);
+                    const double cij = e_c / (rs * rs);
+                    const double si = sin(thi + phu), ci = cos(thi + phu);
+                    const double sj = sin(thj + phv), cj = cos(thj + phv);
+                    for (int a = 0; a < 3; a++) {
+                        for (int cc = 0; cc < 3; cc++) {
+                            const double dia_x = (double)(a == 0) - Ri * si * (double)(a == 2);
+                            const double dia_y = (double)(a == 1) + Ri * ci * (double)(a == 2);
+                            const double djb_x = -1.0 * ((double)(cc == 0) - Rj * sj * (double)(cc == 2));
+                            const double djb_y = -1.0 * ((double)(cc == 1) + Rj * cj * (double)(cc == 2));
+                            const double qia = dx * dia_x + dy * dia_y;
+                            const double qjb = dx * djb_x + dy * djb_y;
+                            const double dqjb = (dia_x * djb_x + dia_y * djb_y) / dist;
+                            hij[a * 3 + cc] += cij * qia * qjb / (dist * dist) +
+                                               tij * (dqjb - qia * qjb / (dist * dist * dist));
+                            const double dib_x = (double)(cc == 0) - Ri * si * (double)(cc == 2);
+                            const double dib_y = (double)(cc == 1) + Ri * ci * (double)(cc == 2);
+                            const double d2x = -Ri * ci * (double)(a == 2) * (double)(cc == 2);
+                            const double d2y = -Ri * si * (double)(a == 2) * (double)(cc == 2);
+                            const double qib = dx * dib_x + dy * dib_y;
+                            const double dqib = (dia_x * dib_x + dx * d2x + dia_y * dib_y + dy * d2y) / dist;
+                            hii[a * 3 + cc] += cij * qia * qib / (dist * dist) +
+                                               tij * (dqib - qia * qib / (dist * dist * dist));
+                        }
+                    }
+                }
+            }
+            if (contact) vci++;
+        }
+        const long long qi = (long long)b * cap + k;
+        const double xd = pbc_dist(c.x, oc.x, bx), yd = pbc_dist(c.y, oc.y, by);
+        const double dist = sqrt(xd * xd + yd * yd);
+        double fric = 0.0;
+        if (fx != 0.0 || fy != 0.0) {
+            const double nfx = fx * xd / dist, nfy = fy * yd / dist;
+            const double nf = sqrt(nfx * nfx + nfy * nfy);
+            const double tfx = fx - nfx, tfy = fy - nfy;
+            fric = sqrt(tfx * tfx + tfy * tfy) / nf;
+        }
+        const double vals[12] = {en, fx, fy, xd, yd, dist - (rad + orad), rad + orad,
+                                 atan2(yd, xd), thi, thj, fric, vov};
+#pragma unroll
+        for (int e = 0; e < 12; e++)
+            if (o.d[e]) o.d[e][qi] = vals[e];
+#pragma unroll
+        for (int e = 0; e < 9; e++) {
+            if (o.d[12 + e]) o.d[12 + e][qi] += hij[e];
+            if (o.d[21 + e]) o.d[21 + e][qi] += hii[e];
+        }
+        o.this_id[qi] = d.v.sidx[b];
+        o.other_id[qi] = d.v.sidx[ob];
+        o.vcount[qi] = vci;
     }
 }
 

@@ -907,6 +907,24 @@ extern "C" int dpg_bumpy_adam_minimize(dpg_bumpy_handle s, double alpha, double 
     return DPG_OK;
 }
 
+extern "C" int dpg_bumpy_grad_desc_step(dpg_bumpy_handle s, double alpha) {
+    if (!s) return set_err(DPG_ERR_ARG, "null handle");
+    LAUNCH(kb_grad_desc, s->gw(s->nb), kTPB, s->d, alpha);
+    return DPG_OK;
+}
+
+// GradDesc::step (src/integrator/grad_desc.cu:11-17) with the rigid step
+extern "C" int dpg_bumpy_grad_desc_steps(dpg_bumpy_handle s, double alpha, int64_t n_steps) {
+    TRY(need(s));
+    for (int64_t t = 0; t < n_steps; t++) {
+        TRY(dpg_bumpy_zero_forces(s));
+        TRY(dpg_bumpy_check_neighbors(s, nullptr));
+        TRY(dpg_bumpy_compute_forces(s));
+        TRY(dpg_bumpy_grad_desc_step(s, alpha));
+    }
+    return DPG_OK;
+}
+
 extern "C" int dpg_bumpy_damped_forces(dpg_bumpy_handle s, double damping) {
     if (!s) return set_err(DPG_ERR_ARG, "null handle");
     LAUNCH(kb_damp, s->gb(s->nb), kTPB, s->d, damping);
@@ -995,4 +1013,50 @@ extern "C" int dpg_bumpy_restore_state(dpg_bumpy_handle s) {
     CK(cudaMemcpyAsync(&s->d->b.p, &s->h.b.p, sizeof(DevParams), cudaMemcpyHostToDevice, s->stream));
     TRY(rebuild_now(s, 1));
     return vrefresh(s);
+}
+
+extern "C" int dpg_bumpy_pair_dump(dpg_bumpy_handle s, double *const *out, int64_t *this_id,
+                                   int64_t *other_id, int64_t *vertex_contacts, int where) {
+    TRY(need(s));
+    if (!out || !this_id || !other_id || !vertex_contacts)
+        return set_err(DPG_ERR_ARG, "dpg_bumpy_pair_dump: null argument");
+    if (where != DPG_HOST && where != DPG_DEVICE) return set_err(DPG_ERR_ARG, "bad where");
+    const long long m = (long long)s->nb * s->cap;
+    BumpyPairOut o{};
+    std::vector<void *> tmp;
+    auto release = [&]() { for (void *p : tmp) cudaFree(p); };
+    auto dev = [&](void **p) -> int {
+        cudaError_t e = cudaMalloc(p, 8 * (size_t)m);
+        if (e != cudaSuccess) { release(); return set_err(DPG_ERR_CUDA, "pair dump: %s", cudaGetErrorString(e)); }
+        tmp.push_back(*p);
+        return DPG_OK;
+    };
+    for (int k = 0; k < kBumpyPairArrays; k++) {
+        if (!out[k]) continue;
+        if (where == DPG_DEVICE) { o.d[k] = out[k]; continue; }
+        void *p = nullptr;
+        TRY(dev(&p));
+        o.d[k] = (double *)p;
+    }
+    int64_t *ids[3] = {this_id, other_id, vertex_contacts};
+    long long **dst[3] = {&o.this_id, &o.other_id, &o.vcount};
+    for (int k = 0; k < 3; k++) {
+        if (where == DPG_DEVICE) { *dst[k] = (long long *)ids[k]; continue; }
+        void *p = nullptr;
+        TRY(dev(&p));
+        *dst[k] = (long long *)p;
+    }
+    kb_pair_fill<<<(int)((m + kTPB - 1) / kTPB), kTPB, 0, s->stream>>>(o, m);
+    kb_pair_dump<<<s->gb(s->nb), kTPB, 0, s->stream>>>(s->d, o);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess && where == DPG_HOST) {
+        for (int k = 0; k < kBumpyPairArrays && e == cudaSuccess; k++)
+            if (out[k]) e = cudaMemcpyAsync(out[k], o.d[k], 8 * (size_t)m, cudaMemcpyDeviceToHost, s->stream);
+        for (int k = 0; k < 3 && e == cudaSuccess; k++)
+            e = cudaMemcpyAsync(ids[k], *dst[k], 8 * (size_t)m, cudaMemcpyDeviceToHost, s->stream);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    release();
+    if (e != cudaSuccess) return set_err(DPG_ERR_CUDA, "pair dump: %s", cudaGetErrorString(e));
+    return DPG_OK;
 }

@@ -10,7 +10,7 @@ import ctypes as C
 import numpy as np
 
 from .disk import _METHODS
-from .lib import (D, DP, I32P, I64, BumpyParams, FireParams, FireResult, NeighborConfig,
+from .lib import (D, DP, I32P, I64, I64P, BumpyParams, FireParams, FireResult, NeighborConfig,
                   NeighborInfo, check, load_library)
 
 
@@ -197,6 +197,13 @@ class RigidBumpy:
                                                C.byref(steps)))
         return steps.value
 
+    # ---- gradient descent (rigid update; see dpg_bumpy_grad_desc_step) -------------
+    def updatePositionsGradDesc(self, alpha):
+        check(self.lib.dpg_bumpy_grad_desc_step(self.h, float(alpha)))
+
+    def gradDescSteps(self, alpha, n):
+        check(self.lib.dpg_bumpy_grad_desc_steps(self.h, float(alpha), int(n)))
+
     # ---- DampedNVE and walls ------------------------------------------------------
     def calculateDampedForces(self, damping_coefficient):
         check(self.lib.dpg_bumpy_damped_forces(self.h, float(damping_coefficient)))
@@ -244,6 +251,28 @@ class RigidBumpy:
         c = D()
         check(self.lib.dpg_bumpy_contacts(self.h, C.byref(c), None, None, None))
         return c.value
+
+    # ---- pair and Hessian dump -----------------------------------------------------
+    PAIR_KEYS = ("potential", "force_x", "force_y", "distance_x", "distance_y", "overlap",
+                 "radsum", "separation_angle", "angle_i", "angle_j", "friction",
+                 "vertex_overlap",
+                 "hess_xx", "hess_xy", "hess_xt", "hess_yx", "hess_yy", "hess_yt", "hess_tx",
+                 "hess_ty", "hess_tt",
+                 "hess_ii_xx", "hess_ii_xy", "hess_ii_xt", "hess_ii_yx", "hess_ii_yy",
+                 "hess_ii_yt", "hess_ii_tx", "hess_ii_ty", "hess_ii_tt")
+
+    def calculateForceDistancePairs(self):
+        """dict of the 30 per-entry arrays ([slot * cap + k]) plus this_id,
+        other_id, vertex_contacts and cap."""
+        cap = self.neighborInfo()["capacity"]
+        m = self.nb * cap
+        arrs = [np.zeros(m) for _ in self.PAIR_KEYS]
+        ptrs = (DP * 30)(*[a.ctypes.data_as(DP) for a in arrs])
+        ids = [np.zeros(m, dtype=np.int64) for _ in range(3)]
+        check(self.lib.dpg_bumpy_pair_dump(self.h, ptrs, *[a.ctypes.data_as(I64P) for a in ids], 0))
+        out = dict(zip(self.PAIR_KEYS, arrs))
+        out.update(this_id=ids[0], other_id=ids[1], vertex_contacts=ids[2], cap=cap)
+        return out
 
     # ---- setLastState / revertToLastState ----------------------------------------
     def setLastState(self):

@@ -184,11 +184,14 @@ SIGNATURES = {
     "dpg_bumpy_adam_step": [VP, I64, D, D, D, D],
     "dpg_bumpy_adam_minimize": [VP, D, D, D, D, D, D, I64, I64P],
     "dpg_bumpy_damped_forces": [VP, D],
+    "dpg_bumpy_grad_desc_step": [VP, D],
+    "dpg_bumpy_grad_desc_steps": [VP, D, I64],
     "dpg_bumpy_damped_nve_steps": [VP, D, D, I64],
     "dpg_bumpy_wall_forces": [VP, I32],
     "dpg_bumpy_nve_wall_steps": [VP, D, I64],
     "dpg_bumpy_stress": [VP, DP, DP, DP],
     "dpg_bumpy_contacts": [VP, DP, DP, I32P, I32P],
+    "dpg_bumpy_pair_dump": [VP, C.POINTER(DP), I64P, I64P, I64P, I32],
     "dpg_bumpy_save_state": [VP],
     "dpg_bumpy_restore_state": [VP],
 }

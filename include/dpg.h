@@ -407,6 +407,13 @@ int dpg_bumpy_adam_step(dpg_bumpy_handle h, int64_t step, double alpha, double b
 int dpg_bumpy_adam_minimize(dpg_bumpy_handle h, double alpha, double beta1, double beta2,
                             double epsilon, double avg_pe_target, double avg_pe_diff_target,
                             int64_t max_steps, int64_t *steps);
+/* Rigid gradient descent, GradDesc::step (src/integrator/grad_desc.cu:11-17) with
+ * a rigid update the reference lacks (its GradDesc runs the disk
+ * kernelGradDescStep, src/particles/base/kernels.cu:613-637, on the body
+ * centres only): x += alpha F, theta += alpha tau (rotation), vertices move
+ * with their body */
+int dpg_bumpy_grad_desc_step(dpg_bumpy_handle h, double alpha);
+int dpg_bumpy_grad_desc_steps(dpg_bumpy_handle h, double alpha, int64_t n_steps);
 /* RigidBumpy::calculateDampedForces (rigid_bumpy.cu:1501-1503): F -= g v, tau -= g omega */
 int dpg_bumpy_damped_forces(dpg_bumpy_handle h, double damping);
 /* DampedNVE::step (src/integrator/damped_nve.cu:15-25) n times, device-resident */
@@ -426,6 +433,18 @@ int dpg_bumpy_stress(dpg_bumpy_handle h, double *stress, double *pressure, doubl
  * 779-781, kernels.cu:924-997); per-body arrays nullable, host, static order */
 int dpg_bumpy_contacts(dpg_bumpy_handle h, double *contacts, double *vertex_contacts,
                        int32_t *per_body, int32_t *vertex_per_body);
+/* RigidBumpy::calculateForceDistancePairs (rigid_bumpy.cu:1383-1459, kernel
+ * kernels.cu:482-703): arrays of n_bodies * cap (cap from
+ * dpg_bumpy_neighbor_info_get), [slot * cap + k] in the current (cell-sorted)
+ * slot order, the reference's fill values where an entry is unused.  out[30]
+ * (NULL entries skipped): pair energy, force x, force y, separation x, y,
+ * overlap (distance - radius sum), radius sum, separation angle, angle i,
+ * angle j, friction coefficient, summed vertex overlap, pair Hessian xx, xy,
+ * xt, yx, yy, yt, tx, ty, tt, self Hessian xx, xy, xt, yx, yy, yt, tx, ty, tt.
+ * this_id / other_id: static body indices; vertex_contacts: this body's
+ * vertices touching the other body.  where: DPG_HOST or DPG_DEVICE pointers. */
+int dpg_bumpy_pair_dump(dpg_bumpy_handle h, double *const *out, int64_t *this_id,
+                        int64_t *other_id, int64_t *vertex_contacts, int where);
 /* setLastState / revertToLastState (rigid_bumpy.cu:1144-1179, particle.cu:956-991):
  * device-side snapshot; the revert restores the box and rebuilds the body and
  * vertex lists from the cell arrays as they are */

@@ -761,6 +761,49 @@ void orcb_adam_steps(orcb_sys *s, double alpha, double b1, double b2, double eps
     }
 }
 
+/* Rigid gradient descent (no reference counterpart: GradDesc::step on a
+ * RigidBumpy runs the disk kernelGradDescStep, src/particles/base/kernels.cu:
+ * 613-637, which moves the body centres but neither the angles nor the
+ * vertices).  Here x += alpha F as that kernel, theta += alpha tau with
+ * rotation, and the vertices follow as in kernelTranslateAndRotateVertices1. */
+void orcb_grad_desc_step(orcb_sys *s, double alpha) {
+    for (int64_t b = 0; b < s->nb; b++) {
+        double px = s->x[b], py = s->y[b];
+        s->lpx[b] = px; s->lpy[b] = py;
+        px += alpha * s->fx[b];
+        py += alpha * s->fy[b];
+        double dth = 0.0;
+        if (s->rotation) {
+            dth = alpha * s->tq[b];
+            s->th[b] += dth;
+        }
+        s->dx[b] = px - s->lpx[b]; s->dy[b] = py - s->lpy[b];
+        s->x[b] = px; s->y[b] = py;
+        double a1 = px - s->lnx[b], a2 = py - s->lny[b];
+        s->nd2[b] = a1 * a1 + a2 * a2;
+        double e1 = px - s->lcx[b], e2 = py - s->lcy[b];
+        s->cd2[b] = e1 * e1 + e2 * e2;
+        s->ke[b] = dth; /* scratch: this step's angle increment */
+    }
+    for (int64_t v = 0; v < s->nv; v++) {
+        int64_t b = s->vbody[v];
+        double rx = s->px[v] - s->lpx[b], ry = s->py[v] - s->lpy[b];
+        double ca = cos(s->ke[b]), sa = sin(s->ke[b]);
+        s->px[v] = s->x[b] + (rx * ca - ry * sa);
+        s->py[v] = s->y[b] + (rx * sa + ry * ca);
+    }
+}
+
+/* GradDesc::step (src/integrator/grad_desc.cu:11-17) n times with the rigid step */
+void orcb_grad_desc_steps(orcb_sys *s, double alpha, int64_t n) {
+    for (int64_t t = 0; t < n; t++) {
+        orcb_zero(s);
+        orcb_check_for_neighbor_update(s);
+        orcb_calculate_forces(s);
+        orcb_grad_desc_step(s, alpha);
+    }
+}
+
 /* ---------------- damping and walls --------------------------------------- */
 /* kernelCalculateRigidDampedForces: kernels.cu:80-87 */
 void orcb_damped_forces(orcb_sys *s, double g) {
@@ -961,6 +1004,117 @@ void orcb_get_contacts(const orcb_sys *s, int64_t *cc, int64_t *vcc) {
         if (cc) cc[k] = s->cc[b];
         if (vcc) vcc[k] = s->vcc[b];
     }
+}
+
+/* ---------------- pair and Hessian dump ------------------------------------ */
+/* RigidBumpy::calculateForceDistancePairs (rigid_bumpy.cu:1383-1459) with
+ * kernelCalcRigidBumpyForceDistancePairs (kernels.cu:482-703).  Entry
+ * [slot * cap + k] describes the k-th listed neighbour body of the body in
+ * slot `slot`.  out[30] (NULL skipped): pair energy, force x, y, separation x,
+ * y, overlap (distance - radius sum), radius sum, separation angle, angle i,
+ * angle j, friction coefficient, summed vertex overlap, pair Hessian xx, xy,
+ * xt, yx, yy, yt, tx, ty, tt, self Hessian in the same order; ids: static
+ * body indices and the count of this body's vertices touching the other body.
+ * Returns cap (entries = n_bodies * cap). */
+static const double k_pair_fill_b[30] = {-1, 0, 0, -1, -1, -1, -1, -1, -1, -1, -1, 0,
+                                         0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+
+int64_t orcb_pair_dump(orcb_sys *s, double **out, int64_t *this_id, int64_t *other_id,
+                       int64_t *vcount) {
+    const int64_t cap = s->cap, m = s->nb * cap;
+    if (!out) return cap;
+    for (int k = 0; k < 30; k++)
+        if (out[k]) for (int64_t q = 0; q < m; q++) out[k][q] = k_pair_fill_b[k];
+    for (int64_t q = 0; q < m; q++) { this_id[q] = -1; other_id[q] = -1; vcount[q] = -1; }
+    const double rs = s->rv * 2.0;
+#pragma omp parallel for schedule(static) if (s->nb >= PAR_MIN)
+    for (int64_t b = 0; b < s->nb; b++) {
+        if (s->ncount[b] == 0) continue;
+        const double cx = s->x[b], cy = s->y[b], thi = s->th[b], rad = s->r[b];
+        for (int64_t k = 0; k < s->ncount[b]; k++) {
+            int64_t ob = s->nlist[b * cap + k];
+            if (ob == -1 || ob == b) continue;
+            const double ox = s->x[ob], oy = s->y[ob], thj = s->th[ob], orad = s->r[ob];
+            double fx = 0.0, fy = 0.0, en = 0.0, vov = 0.0;
+            int64_t vci = 0;
+            double hij[9] = {0}, hii[9] = {0};
+            for (int64_t u = 0; u < s->nvb[b]; u++) {
+                const int64_t v = s->start[b] + u;
+                const double qx = s->px[v], qy = s->py[v];
+                const double phu = (double)(u * 2) * PI_REF / (double)s->nvb[b];
+                const double rdx = qx - cx, rdy = qy - cy;
+                const double Ri = sqrt(rdx * rdx + rdy * rdy);
+                int contact = 0;
+                for (int64_t t = 0; t < s->vncount[v]; t++) {
+                    const int64_t w = s->vnlist[v * s->vcap + t];
+                    if (w == -1 || w == v || s->vbody[w] != ob) continue;
+                    const double wx = s->px[w], wy = s->py[w];
+                    const int64_t iv = w - s->start[ob];
+                    const double phv = (double)(iv * 2) * PI_REF / (double)s->nvb[ob];
+                    const double odx = wx - ox, ody = wy - oy;
+                    const double Rj = sqrt(odx * odx + ody * ody);
+                    double tfx, tfy;
+                    const double te = vpair(s, qx, qy, wx, wy, &tfx, &tfy);
+                    en += te;
+                    fx += tfx;
+                    fy += tfy;
+                    if (te > 0.0) {
+                        contact = 1;
+                        const double dx = bpbc(qx, wx, s->box[0]), dy = bpbc(qy, wy, s->box[1]);
+                        vov += rs - sqrt(dx * dx + dy * dy);
+                        const double dist = sqrt(dx * dx + dy * dy);
+                        const double tij = -s->e_c / rs * (1 - dist / rs);
+                        const double cij = s->e_c / (rs * rs);
+                        const double si = sin(thi + phu), ci = cos(thi + phu);
+                        const double sj = sin(thj + phv), cj = cos(thj + phv);
+                        for (int a = 0; a < 3; a++) {
+                            for (int c = 0; c < 3; c++) {
+                                const double dia_x = (double)(a == 0) - Ri * si * (double)(a == 2);
+                                const double dia_y = (double)(a == 1) + Ri * ci * (double)(a == 2);
+                                const double djb_x = -1.0 * ((double)(c == 0) - Rj * sj * (double)(c == 2));
+                                const double djb_y = -1.0 * ((double)(c == 1) + Rj * cj * (double)(c == 2));
+                                const double qia = dx * dia_x + dy * dia_y;
+                                const double qjb = dx * djb_x + dy * djb_y;
+                                const double dqjb = (dia_x * djb_x + dia_y * djb_y) / dist;
+                                hij[a * 3 + c] += cij * qia * qjb / (dist * dist) +
+                                                  tij * (dqjb - qia * qjb / (dist * dist * dist));
+                                const double dib_x = (double)(c == 0) - Ri * si * (double)(c == 2);
+                                const double dib_y = (double)(c == 1) + Ri * ci * (double)(c == 2);
+                                const double d2x = -Ri * ci * (double)(a == 2) * (double)(c == 2);
+                                const double d2y = -Ri * si * (double)(a == 2) * (double)(c == 2);
+                                const double qib = dx * dib_x + dy * dib_y;
+                                const double dqib = (dia_x * dib_x + dx * d2x + dia_y * dib_y + dy * d2y) / dist;
+                                hii[a * 3 + c] += cij * qia * qib / (dist * dist) +
+                                                  tij * (dqib - qia * qib / (dist * dist * dist));
+                            }
+                        }
+                    }
+                }
+                if (contact) vci++;
+            }
+            const int64_t q = b * cap + k;
+            const double xd = bpbc(cx, ox, s->box[0]), yd = bpbc(cy, oy, s->box[1]);
+            const double dist = sqrt(xd * xd + yd * yd);
+            double fric = 0.0;
+            if (fx != 0.0 || fy != 0.0) {
+                const double nfx = fx * xd / dist, nfy = fy * yd / dist;
+                const double nf = sqrt(nfx * nfx + nfy * nfy);
+                const double tfx = fx - nfx, tfy = fy - nfy;
+                fric = sqrt(tfx * tfx + tfy * tfy) / nf;
+            }
+            const double vals[12] = {en, fx, fy, xd, yd, dist - (rad + orad), rad + orad,
+                                     atan2(yd, xd), thi, thj, fric, vov};
+            for (int e = 0; e < 12; e++) if (out[e]) out[e][q] = vals[e];
+            for (int e = 0; e < 9; e++) {
+                if (out[12 + e]) out[12 + e][q] += hij[e];
+                if (out[21 + e]) out[21 + e][q] += hii[e];
+            }
+            this_id[q] = s->sidx[b];
+            other_id[q] = s->sidx[ob];
+            vcount[q] = vci;
+        }
+    }
+    return cap;
 }
 
 /* ---------------- setLastState / revertToLastState ------------------------- */

@@ -271,6 +271,11 @@ class DiskOracle:
     def nve_steps(self, dt, n):
         self._f("nve_steps")(self.h, float(dt), int(n))
 
+    def grad_desc_steps(self, alpha, n):
+        """GradDesc::step n times with the rigid step (oracle only: the reference
+        has no rigid gradient-descent kernel)."""
+        self.lib.orcb_grad_desc_steps(self.h, float(alpha), int(n))
+
     def damped_nve_steps(self, dt, gamma, n):
         self._f("damped_nve_steps")(self.h, float(dt), float(gamma), int(n))
 
@@ -442,6 +447,7 @@ _BSIGS = {
     "get_contacts": (None, [P, LP, LP]),
     "save_state": (None, [P]),
     "restore_state": (None, [P]),
+    "pair_dump": (I64, [P, C.POINTER(DP), LP, LP, LP]),
 }
 _blibs: dict[str, C.CDLL] = {}
 
@@ -463,6 +469,8 @@ def _bload(kind):
             lib.orcb_minimize_adam.argtypes = [P, D, D, D, D, D, D, I64]
             lib.orcb_damped_forces.restype = None
             lib.orcb_damped_forces.argtypes = [P, D]
+            lib.orcb_grad_desc_steps.restype = None
+            lib.orcb_grad_desc_steps.argtypes = [P, D, I64]
         _blibs[kind] = lib
     return lib, prefix
 
@@ -583,6 +591,11 @@ class BumpyOracle:
     def damped_forces(self, gamma):
         self.lib.orcb_damped_forces(self.h, float(gamma))
 
+    def grad_desc_steps(self, alpha, n):
+        """GradDesc::step n times with the rigid step (oracle only: the reference
+        has no rigid gradient-descent kernel)."""
+        self.lib.orcb_grad_desc_steps(self.h, float(alpha), int(n))
+
     def damped_nve_steps(self, dt, gamma, n):
         self._f("damped_nve_steps")(self.h, float(dt), float(gamma), int(n))
 
@@ -616,6 +629,27 @@ class BumpyOracle:
         vcc = np.zeros(self.nb, dtype=np.int64)
         self._f("get_contacts")(self.h, _lp(cc), _lp(vcc))
         return tot, cc, vcc
+
+    PAIR_KEYS = ("potential", "force_x", "force_y", "distance_x", "distance_y", "overlap",
+                 "radsum", "separation_angle", "angle_i", "angle_j", "friction",
+                 "vertex_overlap",
+                 "hess_xx", "hess_xy", "hess_xt", "hess_yx", "hess_yy", "hess_yt", "hess_tx",
+                 "hess_ty", "hess_tt",
+                 "hess_ii_xx", "hess_ii_xy", "hess_ii_xt", "hess_ii_yx", "hess_ii_yy",
+                 "hess_ii_yt", "hess_ii_tx", "hess_ii_ty", "hess_ii_tt")
+
+    def pair_dump(self):
+        """calculateForceDistancePairs: dict of the 30 per-entry arrays (n * cap,
+        [slot * cap + k]) plus this_id, other_id, vertex_contacts."""
+        cap = self._f("pair_dump")(self.h, None, None, None, None)
+        m = self.nb * cap
+        arrs = [np.zeros(m) for _ in self.PAIR_KEYS]
+        ptrs = (DP * 30)(*[_dp(a) for a in arrs])
+        ti, oi, vc = (np.zeros(m, dtype=np.int64) for _ in range(3))
+        self._f("pair_dump")(self.h, ptrs, _lp(ti), _lp(oi), _lp(vc))
+        out = dict(zip(self.PAIR_KEYS, arrs))
+        out.update(this_id=ti, other_id=oi, vertex_contacts=vc, cap=cap)
+        return out
 
     def save_state(self):
         self._f("save_state")(self.h)

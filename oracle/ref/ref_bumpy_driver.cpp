@@ -669,6 +669,38 @@ void refb_restore_state(refb_sys *s) {
     update_body_list(s, s->method == 0);
 }
 
+// ---- RigidBumpy::calculateForceDistancePairs (rigid_bumpy.cu:1383-1459): the
+// reference's fills, then its kernel; out[30] in the order of orcb_pair_dump
+int64_t refb_pair_dump(refb_sys *s, double **out, int64_t *this_id, int64_t *other_id,
+                       int64_t *vcount) {
+    const long m = s->nb * s->cap;
+    if (!out) return s->cap;
+    static const double fill[30] = {-1, 0, 0, -1, -1, -1, -1, -1, -1, -1, -1, 0,
+                                    0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    std::vector<dvec> a(30);
+    for (int k = 0; k < 30; k++) a[k].assign(m, fill[k]);
+    lvec ti(m, -1), oi(m, -1), vc(m, -1);
+    bsync(s);
+    // kernel argument order: potential, force x/y, distance x/y, ids, overlap, radsum,
+    // radii, static index, separation angle, angle i/j, vertex contacts, angles,
+    // friction, vertex overlaps, pair Hessian xx xy yx yy xt yt tt tx ty, self Hessian same
+    launchb(s->nb, [&] {
+        kernelCalcRigidBumpyForceDistancePairs(
+            s->x.data(), s->y.data(), s->px.data(), s->py.data(), a[0].data(), a[1].data(),
+            a[2].data(), a[3].data(), a[4].data(), ti.data(), oi.data(), a[5].data(), a[6].data(),
+            s->r.data(), s->sidx.data(), a[7].data(), a[8].data(), a[9].data(), vc.data(),
+            s->th.data(), a[10].data(), a[11].data(),
+            a[12].data(), a[13].data(), a[15].data(), a[16].data(), a[14].data(), a[17].data(),
+            a[20].data(), a[18].data(), a[19].data(),
+            a[21].data(), a[22].data(), a[24].data(), a[25].data(), a[23].data(), a[26].data(),
+            a[29].data(), a[27].data(), a[28].data());
+    });
+    for (int k = 0; k < 30; k++)
+        if (out[k]) std::copy(a[k].begin(), a[k].end(), out[k]);
+    for (long q = 0; q < m; q++) { this_id[q] = ti[q]; other_id[q] = oi[q]; vcount[q] = vc[q]; }
+    return s->cap;
+}
+
 void refb_neighbor_info(refb_sys *s, int *method, double *cutoff, double *vcutoff, double *thr2,
                         int64_t *cap, int64_t *vcap, int64_t *nr, int64_t *ncr) {
     if (method) *method = s->method;

@@ -233,7 +233,7 @@ def make_bumpy(nb, phi, seed, name):
 
 def make_bumpy_extras():
     """Rigid bumpy bodies beyond FIRE and NVE, from the reference's own kernels:
-    stress tensor and contact counts (with translational and angular
+    pair and Hessian dump, stress tensor and contact counts (with translational and angular
     velocities, so the kinetic term's omega x r branch runs), DampedNVE,
     NVE::wall_step, the wall-only and wall-plus-pair force calls, Adam steps
     across cell re-sorts, and setLastState / revertToLastState across re-sorts
@@ -266,6 +266,8 @@ def make_bumpy_extras():
     bumpy_snapshot(b, "setup", d)
     d["stress_tot"], d["stress_body"] = b.stress()
     d["contacts_tot"], d["contacts_body"], d["vcontacts_body"] = b.count_contacts()
+    for k, v in b.pair_dump().items():
+        d[f"pairs_{k}"] = v
     b.zero()
     b.wall_only()
     bumpy_snapshot(b, "wallonly", d, vertices=False)

@@ -216,3 +216,52 @@ def test_revert_needs_a_snapshot(dpg, d):
     with pytest.raises(dpg.DpgError):
         b.revertToLastState()
     b.close()
+
+
+@pytest.mark.parametrize("rotation", [True, False])
+def test_rigid_grad_desc_matches_oracle(dpg, d, rotation):
+    """Rigid gradient descent (the reference has no rigid kernel for it): the
+    GPU step against the oracle's restatement of the same update."""
+    from oracle.oracle import BumpyOracle
+    nb = len(d["r"])
+    o = BumpyOracle(nb, int(d["nvb"].sum()), float(d["box"]), float(d["e_c"]), 2.0,
+                    float(d["rv"]), float(d["seg"]), rotation)
+    o.set_bodies(d["x0"], d["y0"], d["th0"], d["r"], d["nvb"])
+    o.set_vertices(d["setup_px"], d["setup_py"])
+    o.set_mass(1.0)
+    o.setup_neighbors(0, 1.5, 0.2, 8.0, 0.05)
+    pe0 = o.total_pe()
+    o.grad_desc_steps(0.05, 300)
+    b = make(dpg, d, cdm=0.05, rotation=rotation, velocities=False)
+    b.gradDescSteps(0.05, 300)
+    g, w = b.getBodies(), o.bodies()
+    for k in ("x", "y", "th", "fx", "fy", "tq", "pe"):
+        np.testing.assert_allclose(g[k], w[k], rtol=0, atol=TRAJ_ATOL, err_msg=k)
+    px, py = b.getVertexPositions()
+    opx, opy = o.vertices()
+    np.testing.assert_allclose(px, opx, rtol=0, atol=TRAJ_ATOL)
+    assert o.total_pe() < pe0
+    ob = o.neighbor_info()
+    assert counts(b) == [ob["n_rebuilds"], ob["n_cell_rebuilds"]]
+    b.close()
+
+
+def test_pair_and_hessian_dump(dpg, d):
+    """calculateForceDistancePairs: layout, fill values, ids and everything
+    without trigonometry bit for bit; the separation angle (atan2) and the
+    Hessian blocks (sin / cos of the vertex angles) to the last bits."""
+    b = make(dpg, d)
+    got = b.calculateForceDistancePairs()
+    assert got["cap"] == int(d["pairs_cap"])
+    trig = {"separation_angle"} | {k for k in got if k.startswith("hess")}
+    for k, v in got.items():
+        if k == "cap":
+            continue
+        want = d[f"pairs_{k}"]
+        if k in trig:
+            scale = max(1.0, np.abs(want).max())
+            np.testing.assert_allclose(v, want, rtol=0, atol=1e-13 * scale, err_msg=k)
+        else:
+            np.testing.assert_array_equal(v, want, err_msg=k)
+    assert (got["vertex_contacts"] > 0).sum() > 0 and np.abs(got["hess_tt"]).max() > 0
+    b.close()

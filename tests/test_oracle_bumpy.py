@@ -76,7 +76,7 @@ def counts(b):
 
 
 def test_bumpy_oracle_extras_match_reference_kernels():
-    """Stress, contacts, walls, DampedNVE, Adam across re-sorts and
+    """Pair and Hessian dump, stress, contacts, walls, DampedNVE, Adam across re-sorts and
     setLastState / revertToLastState across re-sorts: bit for bit."""
     d = dict(np.load(G / "bumpy_n128_extras.npz"))
     b = extras_system(d)
@@ -88,6 +88,8 @@ def test_bumpy_oracle_extras_match_reference_kernels():
     assert tot == float(d["contacts_tot"])
     np.testing.assert_array_equal(cc, d["contacts_body"])
     np.testing.assert_array_equal(vcc, d["vcontacts_body"])
+    for k, v in b.pair_dump().items():
+        np.testing.assert_array_equal(v, d[f"pairs_{k}"], err_msg=f"pairs_{k}")
     b.zero()
     b.wall_only()
     check_bodies(b, d, "wallonly", vertices=False)
