@@ -52,6 +52,8 @@ FIRE_ALPHA0, FIRE_DT0 = 0.1, 1e-2
 L2_FLUSH_BYTES = 512 << 20
 BATCH = 16                  # systems per step of the batched form
 CUTOFF, SKIN = 1.7, 0.3     # neighbour cutoff d_max + skin, and the skin
+TUNE_ITERS = 300            # FIRE iterations per autotuner candidate
+FORM_CODES = {"grid": 1, "persist": 2}
 SWITCH_FMAX = 1e-6          # mixed systems switch to FP64 pair forces below this max|F|
 PLAIN_SOLVES = 2            # timed solves of the plain FP64 path (after one untimed)
 WARMUP_ITERS = 2000         # FIRE iterations of a warm-up solve
@@ -82,7 +84,8 @@ def workload_config():
             "n_particles": N_PART, "packing_fraction": PHI, "fmax_target": FMAX,
             "fire": {"alpha0": FIRE_ALPHA0, "dt0": FIRE_DT0, "dt_max": 10 * FIRE_DT0,
                      "f_inc": 1.1, "f_dec": 0.5, "f_alpha": 0.99, "n_min": 5},
-            "neighbors": {"method": "cell", "cutoff": 1.7, "skin": 0.3, "particles_per_cell": 8},
+            "neighbors": {"method": "cell", "cutoff": "d_max + skin", "skin": "0.3, or the "
+                          "autotuner's 0.225 / 0.15 (extra.autotune)", "particles_per_cell": 8},
             "form": f"mixed precision (FP32 pairs, FP64 accumulation, FP64 pair refinement "
                     f"below max|F| = {SWITCH_FMAX:g}), {BATCH} systems per step",
             "l2": "flushed between steps (512 MiB write)",
@@ -273,11 +276,23 @@ def run_ours(args):
     # ---- inputs of every timed step, resident in HBM before the timed region --
     # (step k >= warmup uses the seeds of step k, so the reference arm, which
     # solves the first start of each timed step, sees the same starts)
+    # the autotuner picks the execution form, block size and skin on the first
+    # timed step's starts (FIRE iterations from those starts, positions
+    # restored), before anything is timed
+    tune_sts = [packing(sd) for sd in step_seeds(rank, args.warmup)]
+    te = dpg.Ensemble([N_PART] * BATCH, [st["box"] for st in tune_sts], CUTOFF, SKIN,
+                      precision=dpg.MIXED, switch_fmax=SWITCH_FMAX, stream=sptr)
+    te.setState(*[np.concatenate([st[c] for st in tune_sts]) for c in ("x", "y", "r", "m")])
+    tune = te.autotune(TUNE_ITERS)
+    te.close()
+    skin = tune["skin"]
+    form = FORM_CODES[tune["form"]]
     batches = []
     for k in range(args.warmup, args.warmup + args.steps):
         sts = [packing(sd) for sd in step_seeds(rank, k)]
-        e = dpg.Ensemble([N_PART] * BATCH, [st["box"] for st in sts], CUTOFF, SKIN,
+        e = dpg.Ensemble([N_PART] * BATCH, [st["box"] for st in sts], CUTOFF - (SKIN - skin), skin,
                          precision=dpg.MIXED, switch_fmax=SWITCH_FMAX, stream=sptr)
+        e.setForm(form, tune["threads"])
         e.setState(*[np.concatenate([st[c] for st in sts]) for c in ("x", "y", "r", "m")])
         batches.append((e, sts))
     torch.cuda.synchronize()
@@ -305,10 +320,14 @@ def run_ours(args):
         res, ms = timed(lambda: solve_batch(e))
         ev_ms.append(ms)
         results.append(res)
-        # kernels per iteration of the graph loop: move, force, transition,
-        # guard; 5 rebuild kernels on iterations where any system rebuilt
         iters = max(r["fire_steps"] for r in res)
-        launches += 4 * (iters + 1) + 5 * max(r["rebuilds"] for r in res)
+        if form == FORM_CODES["persist"]:
+            # one persistent launch per 2^17 iterations
+            launches += 1 + iters // (1 << 17)
+        else:
+            # kernels per iteration of the graph loop: move, force, transition,
+            # guard; 5 rebuild kernels on iterations where any system rebuilt
+            launches += 4 * (iters + 1) + 5 * max(r["rebuilds"] for r in res)
     torch.cuda.synchronize()
     t_wall = time.perf_counter() - t_wall0
     barrier()
@@ -418,7 +437,11 @@ def run_ours(args):
                           "plain_fp64": plain,
                           "mixed_minima_checked_in_fp64": mixed_check,
                           "mixed_batched_over_plain_fp64": value / plain["value"],
-                          "roofline_large": large, "other_workloads": others}}
+                          "roofline_large": large, "other_workloads": others,
+                          "autotune": {"chosen": {"form": tune["form"], "threads": tune["threads"],
+                                                  "skin": tune["skin"]},
+                                       "iters_per_candidate": TUNE_ITERS,
+                                       "particle_iterations_per_s": tune["candidates"]}}}
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist

