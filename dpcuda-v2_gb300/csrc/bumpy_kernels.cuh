@@ -677,6 +677,31 @@ __global__ void kb_set_mass(BumpySys *bs, double mass) {
     if (lane == 0) x.I[b] = acc;
 }
 
+// radii, masses, vertex counts and vertex masses in static (vertex) order
+__global__ void kb_get_static(BumpySys *bs, double *rad, double *mass, int *nvb, double *vmass) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < bs->b.p.n) {
+        const int k = bs->b.v.sidx[i];
+        if (rad) rad[k] = bs->b.v.rad[i];
+        if (mass) mass[k] = bs->b.v.mass[i];
+        if (nvb) nvb[k] = bs->x.nvb[i];
+    }
+    if (vmass && i < bs->x.nv) vmass[bs->x.svidx[i]] = bs->x.vmass[i];
+}
+
+// body masses, moments of inertia and vertex masses from static-order arrays
+// (the values a state directory holds, as loadDataFromPath sets them)
+__global__ void kb_put_mass(BumpySys *bs, const double *mass, const double *inertia,
+                            const double *vmass) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < bs->b.p.n) {
+        const int k = bs->b.v.sidx[i];
+        bs->b.v.mass[i] = mass[k];
+        bs->x.I[i] = inertia[k];
+    }
+    if (i < bs->x.nv) bs->x.vmass[i] = vmass[bs->x.svidx[i]];
+}
+
 // which: 0 angle, 1 angular velocity, 2 torque ; static order in/out
 __global__ void kb_put_body_scalar(BumpySys *bs, int which, const double *a) {
     int b = blockIdx.x * blockDim.x + threadIdx.x;

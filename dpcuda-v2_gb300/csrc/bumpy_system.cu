@@ -1060,3 +1060,73 @@ extern "C" int dpg_bumpy_pair_dump(dpg_bumpy_handle s, double *const *out, int64
     if (e != cudaSuccess) return set_err(DPG_ERR_CUDA, "pair dump: %s", cudaGetErrorString(e));
     return DPG_OK;
 }
+
+// ---------------------------------------------------------------------------
+// static arrays and the box (state files)
+// ---------------------------------------------------------------------------
+extern "C" int dpg_bumpy_get_static(dpg_bumpy_handle s, double *radii, double *masses,
+                                    int32_t *n_vertices_per_body, double *vertex_masses,
+                                    double *box) {
+    if (!s) return set_err(DPG_ERR_ARG, "null handle");
+    // xfer holds max(4 nb, 2 nv) doubles: radii | masses | counts, then vertex masses
+    double *d0 = s->xfer, *d1 = s->xfer + s->nb;
+    int *c0 = (int *)(s->xfer + 2 * (size_t)s->nb);
+    LAUNCH(kb_get_static, s->gb(std::max(s->nb, s->nv)), kTPB, s->d, radii ? d0 : nullptr,
+           masses ? d1 : nullptr, n_vertices_per_body ? c0 : nullptr, (double *)nullptr);
+    if (radii) CK(cudaMemcpyAsync(radii, d0, 8 * (size_t)s->nb, cudaMemcpyDeviceToHost, s->stream));
+    if (masses) CK(cudaMemcpyAsync(masses, d1, 8 * (size_t)s->nb, cudaMemcpyDeviceToHost, s->stream));
+    if (n_vertices_per_body)
+        CK(cudaMemcpyAsync(n_vertices_per_body, c0, 4 * (size_t)s->nb, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    if (vertex_masses) {
+        LAUNCH(kb_get_static, s->gb(std::max(s->nb, s->nv)), kTPB, s->d, (double *)nullptr,
+               (double *)nullptr, (int *)nullptr, s->xfer);
+        CK(cudaMemcpyAsync(vertex_masses, s->xfer, 8 * (size_t)s->nv, cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+    }
+    if (box) { box[0] = s->h.b.p.box[0]; box[1] = s->h.b.p.box[1]; }
+    return DPG_OK;
+}
+
+extern "C" int dpg_bumpy_set_inertia(dpg_bumpy_handle s, const double *masses, const double *inertia,
+                                     const double *vertex_masses) {
+    if (!s || !masses || !inertia || !vertex_masses) return set_err(DPG_ERR_ARG, "null argument");
+    if (!s->have_state) return set_err(DPG_ERR_STATE, "set the bodies first");
+    const double *dm, *di, *dv;
+    TRY(to_dev(s, masses, s->nb, 0, &dm));
+    TRY(to_dev(s, inertia, s->nb, 1, &di));
+    // vertex masses after the two body arrays: xfer holds 2 max(nb, nv) doubles,
+    // so they go through a temporary
+    double *tmp = nullptr;
+    CK(cudaMalloc((void **)&tmp, 8 * (size_t)s->nv));
+    cudaError_t e = cudaMemcpyAsync(tmp, vertex_masses, 8 * (size_t)s->nv, cudaMemcpyHostToDevice, s->stream);
+    dv = tmp;
+    if (e == cudaSuccess) {
+        kb_put_mass<<<s->gb(std::max(s->nb, s->nv)), kTPB, 0, s->stream>>>(s->d, dm, di, dv);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    cudaFree(tmp);
+    if (e != cudaSuccess) return set_err(DPG_ERR_CUDA, "set_inertia: %s", cudaGetErrorString(e));
+    return DPG_OK;
+}
+
+// Particle::setBoxSize for rigid bodies: the box; the cell size follows the box
+// as updateCellSize does when a cell list is set up
+extern "C" int dpg_bumpy_set_box(dpg_bumpy_handle s, double bx, double by) {
+    if (!s) return set_err(DPG_ERR_ARG, "null handle");
+    if (!(bx > 0) || !(by > 0)) return set_err(DPG_ERR_ARG, "box must be > 0");
+    s->h.b.p.box[0] = bx;
+    s->h.b.p.box[1] = by;
+    if (s->ncd > 0) { s->cs = bx / s->ncd; s->h.b.p.cell_size = s->cs; }
+    mixed_grid_update(s->h.b.p);
+    CK(cudaMemcpyAsync(&s->d->b.p, &s->h.b.p, sizeof(DevParams), cudaMemcpyHostToDevice, s->stream));
+    return DPG_OK;
+}
+
+extern "C" int dpg_bumpy_counts(dpg_bumpy_handle s, int64_t *n_bodies, int64_t *n_vertices) {
+    if (!s) return set_err(DPG_ERR_ARG, "null handle");
+    if (n_bodies) *n_bodies = s->nb;
+    if (n_vertices) *n_vertices = s->nv;
+    return DPG_OK;
+}

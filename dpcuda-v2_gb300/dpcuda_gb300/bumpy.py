@@ -280,3 +280,32 @@ class RigidBumpy:
 
     def revertToLastState(self):
         check(self.lib.dpg_bumpy_restore_state(self.h))
+
+    # ---- static arrays, box and state directories ----------------------------------
+    def getStatic(self):
+        """radii, masses, vertex counts (static body order), vertex masses (static
+        vertex order) and the box."""
+        r, m = np.zeros(self.nb), np.zeros(self.nb)
+        nvb = np.zeros(self.nb, dtype=np.int32)
+        vm, box = np.zeros(self.nv), np.zeros(2)
+        check(self.lib.dpg_bumpy_get_static(self.h, r.ctypes.data_as(DP), m.ctypes.data_as(DP),
+                                            nvb.ctypes.data_as(I32P), vm.ctypes.data_as(DP),
+                                            box.ctypes.data_as(DP)))
+        return dict(radii=r, masses=m, n_vertices_per_body=nvb, vertex_masses=vm, box=box)
+
+    def setBoxSize(self, box_x, box_y=None):
+        check(self.lib.dpg_bumpy_set_box(self.h, float(box_x), float(box_x if box_y is None else box_y)))
+
+    def writeState(self, directory, step=-1):
+        check(self.lib.dpg_bumpy_write_state(self.h, str(directory).encode(), int(step)))
+
+    def readState(self, directory):
+        check(self.lib.dpg_bumpy_read_state(self.h, str(directory).encode()))
+
+
+def bumpyStateCount(directory):
+    """(bodies, vertices) of a rigid-bumpy state directory."""
+    lib = load_library()
+    nb, nv = I64(), I64()
+    check(lib.dpg_bumpy_state_count(str(directory).encode(), C.byref(nb), C.byref(nv)))
+    return nb.value, nv.value

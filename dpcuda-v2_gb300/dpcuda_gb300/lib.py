@@ -200,6 +200,13 @@ SIGNATURES = {
     "dpg_bumpy_stress": [VP, DP, DP, DP],
     "dpg_bumpy_contacts": [VP, DP, DP, I32P, I32P],
     "dpg_bumpy_pair_dump": [VP, C.POINTER(DP), I64P, I64P, I64P, I32],
+    "dpg_bumpy_counts": [VP, I64P, I64P],
+    "dpg_bumpy_get_static": [VP, DP, DP, I32P, DP, DP],
+    "dpg_bumpy_set_inertia": [VP, DP, DP, DP],
+    "dpg_bumpy_set_box": [VP, D, D],
+    "dpg_bumpy_write_state": [VP, C.c_char_p, I64],
+    "dpg_bumpy_read_state": [VP, C.c_char_p],
+    "dpg_bumpy_state_count": [C.c_char_p, I64P, I64P],
     "dpg_bumpy_save_state": [VP],
     "dpg_bumpy_restore_state": [VP],
 }

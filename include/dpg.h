@@ -445,6 +445,31 @@ int dpg_bumpy_contacts(dpg_bumpy_handle h, double *contacts, double *vertex_cont
  * vertices touching the other body.  where: DPG_HOST or DPG_DEVICE pointers. */
 int dpg_bumpy_pair_dump(dpg_bumpy_handle h, double *const *out, int64_t *this_id,
                         int64_t *other_id, int64_t *vertex_contacts, int where);
+/* sizes, static arrays (static body / vertex order) and the box */
+int dpg_bumpy_counts(dpg_bumpy_handle h, int64_t *n_bodies, int64_t *n_vertices);
+int dpg_bumpy_get_static(dpg_bumpy_handle h, double *radii, double *masses,
+                         int32_t *n_vertices_per_body, double *vertex_masses, double *box);
+/* body masses, moments of inertia and vertex masses as given (static order),
+ * as RigidBumpy::loadDataFromPath sets them from a state directory */
+int dpg_bumpy_set_inertia(dpg_bumpy_handle h, const double *masses, const double *inertia,
+                          const double *vertex_masses);
+/* Particle::setBoxSize; the cell size follows the box (updateCellSize) */
+int dpg_bumpy_set_box(dpg_bumpy_handle h, double box_x, double box_y);
+/* State directory in the reference's layout (one "%.17e" text file per array,
+ * static order): the disk files (positions, velocities, forces, radii, masses,
+ * potential_energy, box_size) plus angles, angular_velocities, torques,
+ * moments_of_inertia, num_vertices_in_particle (integers), vertex_positions
+ * and vertex_masses (static vertex order) -- RigidBumpy's fundamental values
+ * (include/particles/rigid_bumpy/rigid_bumpy.h:32); step.dat when step >= 0.
+ * The reader follows RigidBumpy::loadDataFromPath (rigid_bumpy.cu:310-371):
+ * positions, radii, masses, box_size, num_vertices_in_particle and
+ * vertex_positions required; velocities, angles, angular velocities optional
+ * (zero); moments of inertia and vertex masses computed as setMass does when
+ * absent.  The handle's body and vertex counts must match the directory's
+ * (dpg_bumpy_state_count). */
+int dpg_bumpy_write_state(dpg_bumpy_handle h, const char *dir, int64_t step);
+int dpg_bumpy_read_state(dpg_bumpy_handle h, const char *dir);
+int dpg_bumpy_state_count(const char *dir, int64_t *n_bodies, int64_t *n_vertices);
 /* setLastState / revertToLastState (rigid_bumpy.cu:1144-1179, particle.cu:956-991):
  * device-side snapshot; the revert restores the box and rebuilds the body and
  * vertex lists from the cell arrays as they are */

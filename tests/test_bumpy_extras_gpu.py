@@ -265,3 +265,42 @@ def test_pair_and_hessian_dump(dpg, d):
             np.testing.assert_array_equal(v, want, err_msg=k)
     assert (got["vertex_contacts"] > 0).sum() > 0 and np.abs(got["hess_tt"]).max() > 0
     b.close()
+
+
+def test_state_directory_round_trip(dpg, d, tmp_path):
+    """writeState / readState in the reference's layout: a fresh handle read
+    from the directory holds the same bodies, vertices, masses, inertia and box
+    (bit for bit) and computes the same forces."""
+    import re
+    from dpcuda_gb300.bumpy import bumpyStateCount
+    b = make(dpg, d)
+    b.fireInit(0.1, 1e-2)
+    for _ in range(20):
+        b.fireStep()
+    out = tmp_path / "restart"
+    b.writeState(out, step=20)
+    assert (out / "step.dat").read_text() == "20"
+    line = (out / "positions.dat").read_text().splitlines()[0]
+    assert re.fullmatch(r"-?\d\.\d{17}e[+-]\d\d\t-?\d\.\d{17}e[+-]\d\d", line), line
+    assert all(re.fullmatch(r"\d+", t) for t in (out / "num_vertices_in_particle.dat").read_text().split())
+    nb, nv = bumpyStateCount(out)
+    assert (nb, nv) == (len(d["r"]), int(d["nvb"].sum()))
+    c = dpg.RigidBumpy(nb, nv, 1.0, float(d["e_c"]), 2.0, float(d["rv"]), float(d["seg"]), True)
+    c.readState(out)
+    gb, gc = b.getBodies(), c.getBodies()
+    for k in ("x", "y", "th", "vx", "vy", "w", "I"):
+        np.testing.assert_array_equal(gc[k], gb[k], err_msg=k)
+    for u, v in zip(b.getVertexPositions(), c.getVertexPositions()):
+        np.testing.assert_array_equal(u, v)
+    sb, sc = b.getStatic(), c.getStatic()
+    for k in sb:
+        np.testing.assert_array_equal(sc[k], sb[k], err_msg=k)
+    c.setupNeighbors("cell", 1.5, 0.2, 8.0, 0.5)
+    b.zeroForceAndPotentialEnergy()
+    b.calculateForces()
+    gb, gc = b.getBodies(), c.getBodies()
+    for k in ("fx", "fy", "tq", "pe"):
+        scale = max(np.abs(gb[k]).max(), 1e-300)
+        np.testing.assert_allclose(gc[k], gb[k], rtol=0, atol=1e-12 * scale, err_msg=k)
+    b.close()
+    c.close()
