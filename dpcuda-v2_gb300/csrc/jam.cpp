@@ -1,7 +1,8 @@
 // jam.cpp -- jamming drivers over the C ABI: the control flow of the
 // reference's run scripts (scripts/runArthurJamWithFire.cpp,
-// scripts/runJam.cpp), restated as host C++.  Every particle operation goes
-// through the dpg_* entry points, so the drivers run the GPU hot path.
+// scripts/runJam.cpp), restated as host C++, for disks and (the pressure-band
+// driver) rigid bumpy bodies.  Every particle operation goes through the
+// dpg_* / dpg_bumpy_* entry points, so the drivers run the GPU hot path.
 #include <cmath>
 #include <vector>
 
@@ -198,6 +199,140 @@ extern "C" int dpg_jam_phi(dpg_handle h, const dpg_jam_phi_params *p, dpg_jam_re
     r->contacts = contacts;
     r->compression_steps = step;
     r->fire_steps_total = total;
+    r->status = status;
+    return DPG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// rigid bumpy bodies
+// ---------------------------------------------------------------------------
+namespace {
+
+// write_restart_file("last_state") for rigid bodies: RigidBumpy's fundamental
+// values (include/particles/rigid_bumpy/rigid_bumpy.h:32) in static order
+struct SavedBumpy {
+    std::vector<double> x, y, th, vx, vy, w, r, m, I, px, py, vm;
+    std::vector<int32_t> nvb;
+    double box[2] = {0, 0};
+};
+
+int bsave(dpg_bumpy_handle h, SavedBumpy &s) {
+    int64_t nb = 0, nv = 0;
+    DPG_TRY(dpg_bumpy_counts(h, &nb, &nv));
+    for (auto *v : {&s.x, &s.y, &s.th, &s.vx, &s.vy, &s.w, &s.r, &s.m, &s.I}) v->resize(nb);
+    s.nvb.resize(nb);
+    s.px.resize(nv); s.py.resize(nv); s.vm.resize(nv);
+    DPG_TRY(dpg_bumpy_get_bodies(h, s.x.data(), s.y.data(), s.th.data(), s.vx.data(), s.vy.data(),
+                                 s.w.data(), nullptr, nullptr, nullptr, nullptr, s.I.data()));
+    DPG_TRY(dpg_bumpy_get_vertices(h, s.px.data(), s.py.data()));
+    DPG_TRY(dpg_bumpy_get_static(h, s.r.data(), s.m.data(), s.nvb.data(), s.vm.data(), s.box));
+    return DPG_OK;
+}
+
+// RigidBumpy::load("last_state") (loadDataFromPath, rigid_bumpy.cu:310-371),
+// then setupNeighbors
+int bload(dpg_bumpy_handle h, const SavedBumpy &s, const dpg_neighbor_config &cfg) {
+    DPG_TRY(dpg_bumpy_set_box(h, s.box[0], s.box[1]));
+    DPG_TRY(dpg_bumpy_set_bodies(h, s.x.data(), s.y.data(), s.th.data(), s.vx.data(), s.vy.data(),
+                                 s.w.data(), s.r.data(), s.nvb.data()));
+    DPG_TRY(dpg_bumpy_set_vertices(h, s.px.data(), s.py.data()));
+    DPG_TRY(dpg_bumpy_set_inertia(h, s.m.data(), s.I.data(), s.vm.data()));
+    DPG_TRY(dpg_bumpy_zero_forces(h));
+    DPG_TRY(dpg_bumpy_setup_neighbors(h, &cfg, nullptr));
+    return DPG_OK;
+}
+
+double bbox_length(dpg_bumpy_handle h) {
+    double box[2] = {1, 1};
+    dpg_bumpy_get_static(h, nullptr, nullptr, nullptr, nullptr, box);
+    return std::pow(1.0 * box[0] * box[1], 1.0 / 2);
+}
+
+}  // namespace
+
+// RigidBumpy::getParticleArea (rigid_bumpy.cu:1026-1030: pi sum R^2 of the body
+// radii) over the box area: Particle::getPackingFraction (particle.cu:1011-1015)
+extern "C" int dpg_bumpy_packing_fraction(dpg_bumpy_handle h, double *phi) {
+    if (!h || !phi) return set_error(DPG_ERR_ARG, "null argument");
+    int64_t nb = 0, nv = 0;
+    DPG_TRY(dpg_bumpy_counts(h, &nb, &nv));
+    std::vector<double> r(nb);
+    double box[2];
+    DPG_TRY(dpg_bumpy_get_static(h, r.data(), nullptr, nullptr, nullptr, box));
+    double a = 0.0;
+    for (double v : r) a += v * v;
+    *phi = a * 3.141592653589793238462643383279502884197 / (1.0 * box[0] * box[1]);
+    return DPG_OK;
+}
+
+// scripts/runArthurJamWithFire.cpp:36-106 on rigid bumpy bodies
+extern "C" int dpg_bumpy_jam_pressure(dpg_bumpy_handle h, const dpg_jam_params *p, double tmax_target,
+                                      dpg_jam_result *r) {
+    if (!h || !p || !r) return set_error(DPG_ERR_ARG, "dpg_bumpy_jam_pressure: null argument");
+    int64_t nb = 0, nv = 0;
+    DPG_TRY(dpg_bumpy_counts(h, &nb, &nv));
+    dpg_fire_result fr;
+    int64_t fire_total = 0;
+    dpg_fire_params dec = p->fire;
+    dec.avg_pe_target = 1e-16;
+    dec.avg_pe_diff_target = 0.0;
+    double P = 0.0, contacts = 0.0;
+    for (int guard = 0;; guard++) {
+        if (guard > 10000) return set_error(DPG_ERR_NOT_CONVERGED, "decompression did not end");
+        DPG_TRY(dpg_bumpy_fire_minimize(h, &dec, tmax_target, &fr));
+        fire_total += fr.steps + 1;
+        DPG_TRY(dpg_bumpy_stress(h, nullptr, &P, nullptr));
+        if (P < p->pressure_low) break;
+        DPG_TRY(dpg_bumpy_scale_box(h, p->decompress_factor));
+    }
+    SavedBumpy last;
+    double L_low = -1, L_high = -1, L_last = -1;
+    int64_t step = 0;
+    int status = 2;
+    while (step < p->max_compression_steps) {
+        DPG_TRY(dpg_bumpy_fire_minimize(h, &p->fire, tmax_target, &fr));
+        fire_total += fr.steps + 1;
+        DPG_TRY(dpg_bumpy_stress(h, nullptr, &P, nullptr));
+        DPG_TRY(dpg_bumpy_contacts(h, &contacts, nullptr, nullptr, nullptr));
+        double L = bbox_length(h);
+        double L_prior = L;
+        if (P < p->pressure_low) {
+            L_low = L;
+            DPG_TRY(bsave(h, last));
+            L_last = L;
+            if (L_high != -1) {
+                L = (L_high + L_low) / 2;
+                L_high = -1;
+            } else {
+                L = L * p->compression_rate;
+            }
+        } else {
+            if (P > p->pressure_high) {
+                L_high = L;
+                if (L_last < 0) return set_error(DPG_ERR_STATE, "jammed before any unjammed state was saved");
+                DPG_TRY(bload(h, last, p->neighbors));
+                L_prior = L_last;
+                L = (L_high + L_low) / 2;
+            } else if (contacts > 2 * nb) {
+                status = 0;
+                break;
+            }
+        }
+        if (L_low > 0 && L_high > 0 && std::abs(L_low / L_high - 1) < p->length_tolerance) {
+            status = 1;
+            break;
+        }
+        DPG_TRY(dpg_bumpy_scale_box(h, L / L_prior));
+        step++;
+    }
+    DPG_TRY(dpg_bumpy_stress(h, nullptr, &P, nullptr));
+    DPG_TRY(dpg_bumpy_contacts(h, &contacts, nullptr, nullptr, nullptr));
+    DPG_TRY(dpg_bumpy_packing_fraction(h, &r->packing_fraction));
+    r->pressure = P;
+    r->box_length = bbox_length(h);
+    r->contacts = contacts;
+    r->compression_steps = step;
+    r->fire_steps_total = fire_total;
     r->status = status;
     return DPG_OK;
 }

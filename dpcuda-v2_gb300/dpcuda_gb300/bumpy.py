@@ -293,6 +293,11 @@ class RigidBumpy:
                                             box.ctypes.data_as(DP)))
         return dict(radii=r, masses=m, n_vertices_per_body=nvb, vertex_masses=vm, box=box)
 
+    def getPackingFraction(self):
+        phi = D()
+        check(self.lib.dpg_bumpy_packing_fraction(self.h, C.byref(phi)))
+        return phi.value
+
     def setBoxSize(self, box_x, box_y=None):
         check(self.lib.dpg_bumpy_set_box(self.h, float(box_x), float(box_x if box_y is None else box_y)))
 
@@ -301,6 +306,27 @@ class RigidBumpy:
 
     def readState(self, directory):
         check(self.lib.dpg_bumpy_read_state(self.h, str(directory).encode()))
+
+
+def bumpyJamPressure(particle: RigidBumpy, pressure_low, pressure_high, compression_rate=0.99,
+                     length_tolerance=1e-10, decompress_factor=1.01, max_compression_steps=1000,
+                     fire=(0.1, 1e-2, 1e-16, 1e-16, 100000), tmax_target=0.0,
+                     neighbors=("cell", 1.5, 0.2, 8.0, 0.5)):
+    """Pressure-band jamming (scripts/runArthurJamWithFire.cpp) of rigid bumpy
+    bodies through the C ABI."""
+    from .lib import JamParams, JamResult
+    m = _METHODS.get(neighbors[0], neighbors[0])
+    prm = JamParams(float(pressure_low), float(pressure_high), float(compression_rate),
+                    float(length_tolerance), float(decompress_factor), int(max_compression_steps),
+                    FireParams(float(fire[0]), float(fire[1]), float(fire[2]), float(fire[3]),
+                               int(fire[4]), float(fire[5]) if len(fire) > 5 else 0.0),
+                    NeighborConfig(int(m), *[float(v) for v in neighbors[1:]]))
+    r = JamResult()
+    check(particle.lib.dpg_bumpy_jam_pressure(particle.h, C.byref(prm), float(tmax_target),
+                                              C.byref(r)))
+    return dict(packing_fraction=r.packing_fraction, pressure=r.pressure, box_length=r.box_length,
+                contacts=r.contacts, compression_steps=r.compression_steps,
+                fire_steps_total=r.fire_steps_total, status=r.status)
 
 
 def bumpyStateCount(directory):

@@ -201,6 +201,8 @@ SIGNATURES = {
     "dpg_bumpy_contacts": [VP, DP, DP, I32P, I32P],
     "dpg_bumpy_pair_dump": [VP, C.POINTER(DP), I64P, I64P, I64P, I32],
     "dpg_bumpy_counts": [VP, I64P, I64P],
+    "dpg_bumpy_packing_fraction": [VP, DP],
+    "dpg_bumpy_jam_pressure": [VP, C.POINTER(JamParams), D, C.POINTER(JamResult)],
     "dpg_bumpy_get_static": [VP, DP, DP, I32P, DP, DP],
     "dpg_bumpy_set_inertia": [VP, DP, DP, DP],
     "dpg_bumpy_set_box": [VP, D, D],

@@ -470,6 +470,15 @@ int dpg_bumpy_set_box(dpg_bumpy_handle h, double box_x, double box_y);
 int dpg_bumpy_write_state(dpg_bumpy_handle h, const char *dir, int64_t step);
 int dpg_bumpy_read_state(dpg_bumpy_handle h, const char *dir);
 int dpg_bumpy_state_count(const char *dir, int64_t *n_bodies, int64_t *n_vertices);
+/* getPackingFraction for rigid bodies: pi sum R^2 of the body radii over the
+ * box area (RigidBumpy::getParticleArea, rigid_bumpy.cu:1026-1030) */
+int dpg_bumpy_packing_fraction(dpg_bumpy_handle h, double *phi);
+/* scripts/runArthurJamWithFire.cpp:36-106 on rigid bodies (dpg_jam_pressure's
+ * control flow with the rigid calls); minimisations stop on p->fire's tests
+ * plus max|tau| <= tmax_target when p->fire.fmax_target > 0; the saved
+ * unjammed state is reloaded as RigidBumpy::load does, then setupNeighbors */
+int dpg_bumpy_jam_pressure(dpg_bumpy_handle h, const dpg_jam_params *p, double tmax_target,
+                           dpg_jam_result *r);
 /* setLastState / revertToLastState (rigid_bumpy.cu:1144-1179, particle.cu:956-991):
  * device-side snapshot; the revert restores the box and rebuilds the body and
  * vertex lists from the cell arrays as they are */

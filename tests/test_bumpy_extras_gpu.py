@@ -304,3 +304,31 @@ def test_state_directory_round_trip(dpg, d, tmp_path):
         np.testing.assert_allclose(gc[k], gb[k], rtol=0, atol=1e-12 * scale, err_msg=k)
     b.close()
     c.close()
+
+
+def test_packing_fraction_and_pressure_band_jamming(dpg):
+    """runArthurJamWithFire on rigid bodies: pi sum R^2 / A as the packing
+    fraction, and a short run of the jamming driver (bounded minimisations and
+    compression steps) whose result is consistent with the system it leaves.
+    (From random starts, interlocked bumpy bodies can keep a finite pressure
+    at any density, so the run starts dilute.)"""
+    from dpcuda_gb300.bumpy import bumpyJamPressure
+    from oracle.oracle import bumpy_packing
+    st = bumpy_packing(32, 0.30, 21)
+    b = dpg.RigidBumpy(32, st["nv"], st["box"], st["e_c"], 2.0, st["rv"], st["seg"], True)
+    b.setBodies(st["x"], st["y"], st["th"], st["r"], st["nvb"])
+    b.setMass(1.0)
+    b.setupNeighbors("cell", 1.5, 0.2, 8.0, 0.5)
+    np.testing.assert_allclose(b.getPackingFraction(), 0.30, rtol=1e-12)
+    band = (1e-3 * 0.9, 1e-3 * 1.1)
+    r = bumpyJamPressure(b, *band, compression_rate=0.95, max_compression_steps=20,
+                         fire=(0.1, 1e-2, 1e-16, 1e-8, 2000))
+    assert r["status"] in (0, 1, 2) and 0 < r["compression_steps"] <= 20
+    if r["status"] == 0:
+        assert band[0] <= r["pressure"] <= band[1] and r["contacts"] > 2 * 32
+    phi = np.pi * np.sum(st["r"] ** 2) / r["box_length"] ** 2
+    np.testing.assert_allclose(r["packing_fraction"], phi, rtol=1e-12)
+    np.testing.assert_allclose(b.getPackingFraction(), phi, rtol=1e-12)
+    np.testing.assert_allclose(b.getPressure(), r["pressure"], rtol=1e-12)
+    assert b.getContactCount() == r["contacts"]
+    b.close()
