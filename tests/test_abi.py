@@ -80,3 +80,47 @@ def test_bad_arguments_rejected_before_any_device_work():
                EnsembleParams(1, 1.0, 2.0, -1.0, 0.3, 0, 0, 0.0),
                EnsembleParams(1, 1.0, 2.0, 1.7, 0.3, 5, 0, 0.0)):
         assert lib.dpg_ensemble_create(C.byref(ep), n, box, None, C.byref(h)) == DPG_ERR_ARG
+
+
+def test_null_handles_rejected_for_rigid_and_ensemble_calls():
+    """Every rigid-body and ensemble entry point added for the workflow pieces
+    checks its handle first and returns DPG_ERR_ARG without device work."""
+    import ctypes as C
+    from dpcuda_gb300.lib import load_library
+    DPG_ERR_ARG = 1
+    lib = load_library()
+    calls = [
+        ("dpg_bumpy_adam_init", ()), ("dpg_bumpy_adam_step", (C.c_int64(0), C.c_double(1e-3),
+                                      C.c_double(0.9), C.c_double(0.999), C.c_double(1e-8))),
+        ("dpg_bumpy_damped_forces", (C.c_double(0.1),)),
+        ("dpg_bumpy_damped_nve_steps", (C.c_double(1e-3), C.c_double(0.1), C.c_int64(1))),
+        ("dpg_bumpy_wall_forces", (C.c_int(0),)),
+        ("dpg_bumpy_nve_wall_steps", (C.c_double(1e-3), C.c_int64(1))),
+        ("dpg_bumpy_grad_desc_step", (C.c_double(1e-3),)),
+        ("dpg_bumpy_grad_desc_steps", (C.c_double(1e-3), C.c_int64(1))),
+        ("dpg_bumpy_stress", (None, None, None)),
+        ("dpg_bumpy_contacts", (None, None, None, None)),
+        ("dpg_bumpy_save_state", ()), ("dpg_bumpy_restore_state", ()),
+        ("dpg_bumpy_pair_dump", (None, None, None, None, C.c_int(0))),
+        ("dpg_bumpy_counts", (None, None)),
+        ("dpg_bumpy_get_static", (None, None, None, None, None)),
+        ("dpg_bumpy_set_box", (C.c_double(10.0), C.c_double(10.0))),
+        ("dpg_bumpy_packing_fraction", (None,)),
+        ("dpg_bumpy_write_state", (b"/nonexistent", C.c_int64(-1))),
+        ("dpg_bumpy_read_state", (b"/nonexistent",)),
+        ("dpg_ensemble_set_form", (C.c_int(1), C.c_int(0))),
+        ("dpg_ensemble_autotune", (None, C.c_int(10), None)),
+    ]
+    for name, args in calls:
+        assert getattr(lib, name)(None, *args) == DPG_ERR_ARG, name
+
+
+def test_bumpy_state_count_reads_the_reference_layout(tmp_path):
+    """dpg_bumpy_state_count is host-only: bodies from radii.dat, vertices from
+    the "x<TAB>y" lines of vertex_positions.dat."""
+    import numpy as np
+    from dpcuda_gb300.bumpy import bumpyStateCount
+    (tmp_path / "radii.dat").write_text("".join(f"{v:.17e}\n" for v in np.full(5, 0.5)))
+    (tmp_path / "vertex_positions.dat").write_text(
+        "".join(f"{a:.17e}\t{b:.17e}\n" for a, b in np.random.default_rng(1).random((83, 2))))
+    assert bumpyStateCount(tmp_path) == (5, 83)
