@@ -271,11 +271,6 @@ class DiskOracle:
     def nve_steps(self, dt, n):
         self._f("nve_steps")(self.h, float(dt), int(n))
 
-    def grad_desc_steps(self, alpha, n):
-        """GradDesc::step n times with the rigid step (oracle only: the reference
-        has no rigid gradient-descent kernel)."""
-        self.lib.orcb_grad_desc_steps(self.h, float(alpha), int(n))
-
     def damped_nve_steps(self, dt, gamma, n):
         self._f("damped_nve_steps")(self.h, float(dt), float(gamma), int(n))
 
