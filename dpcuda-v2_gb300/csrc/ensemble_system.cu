@@ -677,7 +677,10 @@ extern "C" int dpg_ensemble_autotune(dpg_ensemble s, const dpg_fire_params *p, i
     cudaMemcpyAsync(s->h.pos, saved, 16 * (size_t)s->T, cudaMemcpyDeviceToDevice, s->stream);
     cudaStreamSynchronize(s->stream);
     cudaFree(saved);
-    if (rc != DPG_OK) return rc;
+    if (rc != DPG_OK) {
+        set_skin(s, s->prm.skin);  // a failed trial leaves the given skin in place
+        return rc;
+    }
     size_t best = 0;
     for (size_t k = 1; k < cands.size(); k++)
         if (cands[k].rate > cands[best].rate) best = k;
