@@ -263,7 +263,9 @@ extern "C" int dpg_create(const dpg_params *p, void *cuda_stream, dpg_handle *ou
     A((void **)&w.pos_n, n * 16); A((void **)&w.pos_c, n * 16); A((void **)&w.pe, n * 8);
     A((void **)&w.count, n * 4); A((void **)&w.cell_raw, n * 4); A((void **)&w.cell_of, n * 4);
     A((void **)&w.perm, n * 4);
-    w.max_blocks = std::max(std::max(s->grid(s->n), s->grid_full(s->n)), s->fgrid());
+    // partials for the widest force group (8 lanes), so the group can change later
+    const int fg8 = std::max(1, (int)(((long long)s->n * 8 + s->ftpb - 1) / s->ftpb));
+    w.max_blocks = std::max(std::max(s->grid(s->n), s->grid_full(s->n)), std::max(s->fgrid(), fg8));
     A((void **)&w.partials, (size_t)w.max_blocks * 8 * 8);
     A((void **)&w.s_pos, n * 16); A((void **)&w.s_vel, n * 16); A((void **)&w.s_frc, n * 16);
     A((void **)&w.s_rad, n * 8); A((void **)&w.s_mass, n * 8); A((void **)&w.s_sidx, n * 4);
@@ -1363,5 +1365,74 @@ extern "C" int dpg_profile_loop(dpg_handle s, int kind, int iters, double dt, do
         counts[2] = s->hs->n_cell_rebuilds - nc0;
     }
     TRY(put_field(s, &s->d->s.flags, 0));
+    return DPG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// threads per particle of the FP64 force kernels
+// ---------------------------------------------------------------------------
+extern "C" int dpg_set_force_group(dpg_handle s, int lanes) {
+    if (!s) return set_err(DPG_ERR_ARG, "null handle");
+    if (lanes != 1 && lanes != 2 && lanes != 4 && lanes != 8)
+        return set_err(DPG_ERR_ARG, "lanes per particle must be 1, 2, 4 or 8");
+    if (s->mixed && lanes != 1) return set_err(DPG_ERR_ARG, "DPG_MIXED systems use one lane per particle");
+    if (s->fg != lanes) {
+        s->fg = lanes;
+        free_graphs(s);  // the graphs hold the kernels and grids of the old group
+    }
+    return DPG_OK;
+}
+
+// Autotuner for the threads per particle of the FP64 force kernels (every
+// group gives bit-identical sums): times `iters` force passes with 1, 2, 4 and
+// 8 lanes per particle on the current positions and lists (CUDA events on the
+// system's stream), keeps the fastest, and restores the forces and energies.
+extern "C" int dpg_autotune_force_group(dpg_handle s, int iters, int *chosen, double *us_per_pass) {
+    TRY(need_neighbors(s));
+    if (iters <= 0) return set_err(DPG_ERR_ARG, "iters must be > 0");
+    if (s->mixed) {
+        if (chosen) *chosen = 1;
+        return DPG_OK;
+    }
+    DevView v;
+    CK(cudaMemcpyAsync(&v, &s->d->v, sizeof(DevView), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    double2 *f_save = nullptr;
+    double *pe_save = nullptr;
+    CK(cudaMalloc((void **)&f_save, 16 * (size_t)s->n));
+    cudaError_t e = cudaMalloc((void **)&pe_save, 8 * (size_t)s->n);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(f_save, v.frc, 16 * (size_t)s->n, cudaMemcpyDeviceToDevice, s->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(pe_save, s->h.w.pe, 8 * (size_t)s->n, cudaMemcpyDeviceToDevice, s->stream);
+    cudaEvent_t a = nullptr, b = nullptr;
+    if (e == cudaSuccess) e = cudaEventCreate(&a);
+    if (e == cudaSuccess) e = cudaEventCreate(&b);
+    const int groups[4] = {1, 2, 4, 8};
+    double best_us = INFINITY;
+    int best = s->fg, rc = DPG_OK;
+    for (int k = 0; k < 4 && e == cudaSuccess && rc == DPG_OK; k++) {
+        s->fg = groups[k];
+        rc = launch_force_acc(s);  // untimed first pass
+        e = cudaEventRecord(a, s->stream);
+        for (int t = 0; t < iters && rc == DPG_OK; t++) rc = launch_force_acc(s);
+        if (e == cudaSuccess) e = cudaEventRecord(b, s->stream);
+        if (e == cudaSuccess) e = cudaEventSynchronize(b);
+        float ms = 0.f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+        const double us = 1e3 * ms / iters;
+        if (us_per_pass) us_per_pass[k] = us;
+        if (us < best_us) { best_us = us; best = groups[k]; }
+    }
+    s->fg = best;
+    free_graphs(s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(v.frc, f_save, 16 * (size_t)s->n, cudaMemcpyDeviceToDevice, s->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(s->h.w.pe, pe_save, 8 * (size_t)s->n, cudaMemcpyDeviceToDevice, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+    cudaFree(f_save);
+    cudaFree(pe_save);
+    if (rc != DPG_OK) return rc;
+    if (e != cudaSuccess) return set_err(DPG_ERR_CUDA, "autotune: %s", cudaGetErrorString(e));
+    if (chosen) *chosen = best;
     return DPG_OK;
 }

@@ -260,6 +260,18 @@ class Disk:
         """DPG_MIXED systems: max|F| below which FIRE continues in FP64."""
         check(self.lib.dpg_set_mixed_switch(self.h, float(switch_fmax)))
 
+    def setForceGroup(self, lanes):
+        """Threads per particle (1, 2, 4, 8) of the FP64 force kernels (identical sums)."""
+        check(self.lib.dpg_set_force_group(self.h, int(lanes)))
+
+    def autotuneForceGroup(self, iters=50):
+        """Times force passes with 1, 2, 4, 8 lanes per particle, keeps the fastest;
+        returns (lanes, microseconds per pass for each group)."""
+        chosen = I32()
+        us = (C.c_double * 4)()
+        check(self.lib.dpg_autotune_force_group(self.h, int(iters), C.byref(chosen), us))
+        return chosen.value, dict(zip((1, 2, 4, 8), list(us)))
+
     def writeState(self, directory, step=-1):
         """State files in the reference's layout (positions.dat, radii.dat, ...)."""
         check(self.lib.dpg_write_state(self.h, str(directory).encode(), int(step)))

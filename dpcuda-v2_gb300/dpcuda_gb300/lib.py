@@ -153,6 +153,8 @@ SIGNATURES = {
     "dpg_save_state": [VP],
     "dpg_restore_state": [VP],
     "dpg_profile_loop": [VP, I32, I32, D, DP, I64P],
+    "dpg_set_force_group": [VP, I32],
+    "dpg_autotune_force_group": [VP, I32, C.POINTER(I32), DP],
     "dpg_disk_forces_noalloc": [VP, VP, VP, I64, D, D, D, D, D, VP, VP, VP, VP],
     "dpg_ensemble_create": [C.POINTER(EnsembleParams), I64P, DP, VP, C.POINTER(VP)],
     "dpg_ensemble_destroy": [VP],

@@ -572,6 +572,18 @@ typedef struct {
  * trial, and keeps the fastest by particle-iterations per second. */
 int dpg_ensemble_autotune(dpg_ensemble e, const dpg_fire_params *p, int iters, dpg_ensemble_tuning *out);
 
+/* ---- threads per particle of the FP64 force kernels ------------------- */
+/* Lanes per particle (1, 2, 4, 8) of the FP64 force kernels: lane g sums
+ * neighbour slots g, g + G, ... and the pair terms are added in slot order
+ * through shuffles, so every group gives bit-identical forces.  The default
+ * is chosen from the particle count; DPG_MIXED systems use one lane. */
+int dpg_set_force_group(dpg_handle h, int lanes);
+/* Autotuner (no reference counterpart): times `iters` force passes for each
+ * group on the current positions and lists, keeps the fastest (*chosen) and
+ * restores the forces and energies; us_per_pass[4] (nullable): mean device
+ * time per pass for 1, 2, 4, 8 lanes. */
+int dpg_autotune_force_group(dpg_handle h, int iters, int *chosen, double *us_per_pass);
+
 /* ---- measurement ------------------------------------------------------ */
 /* Runs `iters` iterations of a device loop (kind 0 = FIRE from the current
  * state, as dpg_fire_minimize's body; kind 1 = NVE with step dt) as plain

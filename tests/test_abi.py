@@ -109,6 +109,8 @@ def test_null_handles_rejected_for_rigid_and_ensemble_calls():
         ("dpg_bumpy_write_state", (b"/nonexistent", C.c_int64(-1))),
         ("dpg_bumpy_read_state", (b"/nonexistent",)),
         ("dpg_ensemble_set_form", (C.c_int(1), C.c_int(0))),
+        ("dpg_set_force_group", (C.c_int(2),)),
+        ("dpg_autotune_force_group", (C.c_int(10), None, None)),
         ("dpg_ensemble_autotune", (None, C.c_int(10), None)),
     ]
     for name, args in calls:

@@ -466,3 +466,31 @@ def test_mixed_fire_refines_to_fp64_residual(dpg):
     assert r64["max_force"] <= 1e-12
     assert r["converged"] and r["max_force"] <= 1e-12
     np.testing.assert_allclose(m.totalPotentialEnergy(), pe64, rtol=1e-10)
+
+
+def test_force_groups_give_identical_forces_and_autotune_restores_state():
+    """1, 2, 4 and 8 lanes per particle: bit-identical forces and energies; the
+    autotuner picks one of them and leaves the forces as they were."""
+    import dpcuda_gb300 as dpg
+    from oracle.oracle import disk_packing
+    st = disk_packing(3000, 0.86, 31)
+    s = dpg.Disk(3000, st["box"])
+    s.setState(st["x"], st["y"], None, None, st["r"], st["m"])
+    s.setupNeighbors("cell", 1.7 / 1.4, 0.2, 8.0, 0.5)
+    ref = None
+    for g in (1, 2, 4, 8):
+        s.setForceGroup(g)
+        s.zeroForceAndPotentialEnergy()
+        s.calculateForces()
+        got = s.getState()
+        if ref is None:
+            ref = got
+        for k in ("fx", "fy", "pe"):
+            np.testing.assert_array_equal(got[k], ref[k], err_msg=f"{k} lanes={g}")
+    lanes, us = s.autotuneForceGroup(20)
+    assert lanes in (1, 2, 4, 8) and all(v > 0 for v in us.values())
+    after = s.getState()
+    for k in ("fx", "fy", "pe", "x", "y"):
+        np.testing.assert_array_equal(after[k], ref[k], err_msg=k)
+    s.nveSteps(1e-2, 20)  # the loops run with the chosen group
+    s.close()
