@@ -13,6 +13,23 @@ from .lib import (DP, EnsembleParams, EnsembleResult, EnsembleTuning, FireParams
                   NeighborConfig, check, load_library)
 
 FP64, MIXED, DWORD = 0, 1, 2
+
+
+def partition_systems(n_particles, world):
+    """Independent systems over `world` ranks (one GPU each): greedy N-balanced
+    bin packing, largest system first to the least-loaded rank (ties: lowest
+    rank), deterministic on every rank.  Returns each rank's system indices in
+    ascending order; the ranks need no exchange while they solve their share."""
+    n = [int(v) for v in n_particles]
+    if world < 1:
+        raise ValueError("world must be >= 1")
+    loads = [0] * world
+    parts = [[] for _ in range(world)]
+    for k in sorted(range(len(n)), key=lambda j: (-n[j], j)):
+        r = min(range(world), key=lambda q: (loads[q], q))
+        parts[r].append(k)
+        loads[r] += n[k]
+    return [sorted(p) for p in parts]
 FORM_AUTO, FORM_GRID, FORM_PERSIST = 0, 1, 2
 _FORM_NAMES = {FORM_GRID: "grid", FORM_PERSIST: "persist"}
 
