@@ -636,9 +636,25 @@ def ncu_case(which):
     """Small fixed workloads for ncu captures (plain stream launches, a few
     hundred kernels): 'fire' = 64 FIRE iterations of the 16384-disk system,
     'nve_large' = 8 NVE steps of the 2^20-disk system, 'ensemble' = 64 FIRE
-    iterations of the batched mixed form on 8 x 16384 disks."""
+    iterations of the batched mixed form on 8 x 16384 disks, 'bumpy_nve' = 192
+    NVE steps of 4096 rigid bumpy bodies."""
     os.environ["DPG_LOOP_MODE"] = "stream"
     import dpcuda_gb300 as dpg
+    if which == "bumpy_nve":
+        # NVE of 4096 rigid bumpy bodies (FP64): 64 steps, then 128 steps
+        from dpcuda_gb300.init import bumpy_packing
+        b = bumpy_packing(4096, 0.80, 3)
+        bv = np.random.default_rng(1).normal(0, 1e-2, (2, 4096))
+        bv -= bv.mean(axis=1, keepdims=True)
+        r = dpg.RigidBumpy(4096, b["nv"], b["box"], b["e_c"], 2.0, b["rv"], b["seg"], True,
+                           precision=0)
+        r.setBodies(b["x"], b["y"], b["th"], b["r"], b["nvb"], bv[0], bv[1])
+        r.setMass(1.0)
+        r.setupNeighbors("cell", 1.5, 0.2, 8.0, 0.5)
+        r.nveSteps(5e-3, 64)
+        r.nveSteps(5e-3, 128)
+        print(json.dumps({"ncu_case": which, "n_rebuilds": r.neighborInfo()["n_rebuilds"]}))
+        return
     if which == "ensemble_forces":
         # one force pass per arithmetic (FP32, double-word, FP64) on 8 x 16384 disks
         from dpcuda_gb300.ensemble import DWORD
@@ -686,7 +702,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--ncu-case", choices=["fire", "nve_large", "ensemble", "ensemble_forces"],
+    ap.add_argument("--ncu-case", choices=["fire", "nve_large", "ensemble", "ensemble_forces",
+                                           "bumpy_nve"],
                     default=None,
                     help="run a small fixed workload for ncu captures and exit")
     ap.add_argument("--batch", type=int, default=BATCH, help="systems per step of the batched form")
