@@ -124,6 +124,8 @@ orc_sys *orc_create(int64_t n, double box_x, double box_y, double e_c, double n_
     lfill(s->nlist, n * s->cap, -1);
     s->cell_start = lalloc(1);
     s->method = -1;
+    /* the reference's member defaults (include/particles/base/particle.h:173-187) */
+    s->cutoff = -1; s->nthr2 = -1; s->cs = -1; s->cthr2 = -1; s->ncd = -1; s->ncells = -1;
     return s;
 }
 
