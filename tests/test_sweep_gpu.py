@@ -62,3 +62,55 @@ def test_fp64_path_matches_oracle_across_sizes_and_methods(dpg, n, phi, seed, me
     o.damped_nve_steps(1e-2, 0.3, 20)
     same(s, o, "damped")
     s.close()
+
+
+@pytest.mark.parametrize("nb,phi,seed", [(8, 0.6, 11), (40, 0.85, 12), (150, 0.75, 13)])
+@pytest.mark.parametrize("rotation", [True, False])
+def test_rigid_path_matches_oracle_across_sizes(dpg, nb, phi, seed, rotation):
+    """Rigid bodies: setup forces bit for bit (same vertex positions); NVE,
+    FIRE, DampedNVE and Adam trajectories to 1e-9 (vertex rotations use
+    cos / sin, whose CUDA and host-libm results may differ in the last bit)."""
+    from oracle.oracle import BumpyOracle, bumpy_packing, fill_normal
+    st = bumpy_packing(nb, phi, seed)
+    vx = fill_normal(nb, 0.0, 1e-2, 1, seed)
+    vy = fill_normal(nb, 0.0, 1e-2, 1 + nb, seed)
+    w = fill_normal(nb, 0.0, 1e-2, 1 + 2 * nb, seed)
+    o = BumpyOracle(nb, st["nv"], st["box"], st["e_c"], 2.0, st["rv"], st["seg"], rotation)
+    o.set_bodies(st["x"], st["y"], st["th"], st["r"], st["nvb"], vx, vy, w)
+    o.init_vertices()
+    o.set_mass(1.0)
+    code = o.setup_neighbors(0, 1.5, 0.2, 8.0, 0.3)
+    px, py = o.vertices()
+    b = dpg.RigidBumpy(nb, st["nv"], st["box"], st["e_c"], 2.0, st["rv"], st["seg"], rotation)
+    b.setBodies(st["x"], st["y"], st["th"], st["r"], st["nvb"], vx, vy, w)
+    b.setVertexPositions(px, py)
+    b.setMass(1.0)
+    assert b.setupNeighbors("cell", 1.5, 0.2, 8.0, 0.3)["method"] == code
+
+    def check(tag, exact=False):
+        g, r = b.getBodies(), o.bodies()
+        for k in ("x", "y", "th", "vx", "vy", "w", "fx", "fy", "tq", "pe"):
+            if exact:
+                np.testing.assert_array_equal(g[k], r[k], err_msg=f"{tag} {k}")
+            else:
+                np.testing.assert_allclose(g[k], r[k], rtol=0, atol=1e-9, err_msg=f"{tag} {k}")
+
+    check("setup", exact=True)
+    b.nveSteps(5e-3, 30)
+    o.nve_steps(5e-3, 30)
+    check("nve")
+    b.fireInit(0.1, 1e-2)
+    o.fire_init(0.1, 1e-2)
+    for _ in range(25):
+        b.fireStep()
+        o.fire_step()
+    check("fire")
+    b.dampedNveSteps(5e-3, 0.4, 20)
+    o.damped_nve_steps(5e-3, 0.4, 20)
+    check("damped")
+    b.initAdamVariables()
+    for t in range(20):
+        b.adamMinimizeStep(t, 2e-3)
+    o.adam_steps(20, 2e-3)
+    check("adam")
+    b.close()
