@@ -126,3 +126,28 @@ def test_bumpy_state_count_reads_the_reference_layout(tmp_path):
     (tmp_path / "vertex_positions.dat").write_text(
         "".join(f"{a:.17e}\t{b:.17e}\n" for a, b in np.random.default_rng(1).random((83, 2))))
     assert bumpyStateCount(tmp_path) == (5, 83)
+
+
+def test_header_is_plain_c_and_links_every_symbol(tmp_path):
+    """include/dpg.h compiles as C99 (no C++ types in the signatures), and a C
+    program that takes the address of every declared entry point links
+    against the built library (the C linkage a cgo / ctypes / JNI stub binds)."""
+    import shutil
+    import subprocess
+    gcc = shutil.which("gcc")
+    if not gcc:
+        pytest.skip("no C compiler")
+    from dpcuda_gb300 import build
+    lib = build.build()
+    names = declared_symbols()
+    src = ['#include "dpg.h"', "#include <stdio.h>", "int main(void) {", "    void *p[] = {"]
+    src += [f"        (void *)&{n}," for n in names]
+    src += ["    };", '    printf("%d\\n", (int)(sizeof p / sizeof p[0]));', "    return 0;", "}"]
+    c = tmp_path / "abi_check.c"
+    c.write_text("\n".join(src) + "\n")
+    exe = tmp_path / "abi_check"
+    subprocess.run([gcc, "-std=c99", "-Wall", "-Werror", "-pedantic-errors", "-Wno-pedantic",
+                    "-I", str(ROOT / "include"), str(c), "-o", str(exe),
+                    "-L", str(lib.parent), "-ldpg", f"-Wl,-rpath,{lib.parent}"],
+                   check=True, capture_output=True)
+    assert exe.exists()
