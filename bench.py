@@ -632,6 +632,37 @@ def jam_ensemble(args):
     print(json.dumps(line), flush=True)
 
 
+def fire_ensemble(args):
+    """Batched FIRE on an uneven ensemble (not the default line): S bidisperse
+    systems with N drawn log-uniformly in [64, 4096] from a seed, phi 0.86,
+    seeded random starts, minimised to max|F| <= 1e-13 in the mixed and the
+    FP64 batched forms (one untimed 50-iteration call first builds the graph).
+    Prints one JSON line per form."""
+    import dpcuda_gb300 as dpg
+    from dpcuda_gb300.init import disk_packing
+    S = args.fire_systems
+    rng = np.random.default_rng(2024)
+    sizes = np.floor(np.exp(rng.uniform(np.log(64), np.log(4096), S))).astype(int)
+    sts = [disk_packing(int(n), PHI, 9000 + k) for k, n in enumerate(sizes)]
+    cat = [np.concatenate([st[c] for st in sts]) for c in ("x", "y", "r", "m")]
+    for name, prec in (("mixed", dpg.MIXED), ("fp64", dpg.FP64)):
+        e = dpg.Ensemble(sizes, [st["box"] for st in sts], CUTOFF, SKIN, precision=prec,
+                         switch_fmax=SWITCH_FMAX)
+        e.setState(*cat)
+        e.minimizeFire(FIRE_ALPHA0, FIRE_DT0, 0.0, 0.0, 50, fmax_target=FMAX)
+        e.setState(*cat)
+        t0 = time.perf_counter()
+        r = e.minimizeFire(FIRE_ALPHA0, FIRE_DT0, 0.0, 0.0, 10**6, fmax_target=FMAX)
+        dt = time.perf_counter() - t0
+        print(json.dumps({"metric": "batched FIRE solves/s, uneven ensemble", "form": name,
+                          "systems": S, "particles": int(sizes.sum()), "s": dt,
+                          "systems_per_s": S / dt,
+                          "converged": int(sum(x["converged"] for x in r)),
+                          "max_force": max(x["max_force"] for x in r),
+                          "fire_steps_max": int(max(x["fire_steps"] for x in r))}), flush=True)
+        e.close()
+
+
 def ncu_case(which):
     """Small fixed workloads for ncu captures (plain stream launches, a few
     hundred kernels): 'fire' = 64 FIRE iterations of the 16384-disk system,
@@ -713,10 +744,16 @@ def main():
     ap.add_argument("--jam-max-compressions", type=int, default=2000)
     ap.add_argument("--jam-pressure", type=float, default=1e-7,
                     help="target pressure of the batched jamming leg (band +-1%%)")
+    ap.add_argument("--fire-ensemble", action="store_true",
+                    help="run batched FIRE on an uneven ensemble instead of the default line")
+    ap.add_argument("--fire-systems", type=int, default=256)
     args = ap.parse_args()
     BATCH = args.batch
     if args.jam_ensemble:
         jam_ensemble(args)
+        return
+    if args.fire_ensemble:
+        fire_ensemble(args)
         return
     if args.ncu_case:
         ncu_case(args.ncu_case)
