@@ -70,6 +70,12 @@ struct ESys {
     unsigned ticket_a, ticket_b;
     int resume;              // persistent form: the last launch stopped after a list overflow
                              // (move done, lists to rebuild, then the force pass)
+    int res_valid;           // resident form: pk / pkl hold the exact double-word offsets
+                             // written back by its last launch
+    int verify;              // resident form: the next pass is an FP64 force pass at the
+                             // current positions, 1 = check max|F| (back to double words if
+                             // it fails), 2 = final measurement of a finished minimisation
+    double dw_scale;         // resident form: double-word exit at dw_scale * fmax_target
 };
 
 struct EParams {
@@ -86,6 +92,7 @@ struct EParams {
     int jam;                 // 0: plain minimisation, 1: jamming protocol
     double p_low, p_high, compression_rate, length_tol, decompress;
     long long max_compressions;
+    int res;                 // resident form: FP64 passes only verify double-word states
 };
 
 struct EDev {
@@ -640,6 +647,8 @@ __device__ __forceinline__ void pair_f32(const float4 a, const float4 b, int ncd
 // Per-system epilogue of a force pass (thread 0 of the system's last block):
 // minimizeFire tests, the mixed-precision switch, the next FIRE decision and
 // the jamming state machine (scripts/runArthurJamWithFire.cpp:36-106).
+__device__ void e_finish(EDev *e, ESys &s);
+
 __device__ void e_force_epilogue(EDev *e, ESys &s, const double (&v)[5], bool setup) {
     const EParams &p = e->p;
     // ---- per-system epilogue: minimizeFire tests and the next FIRE decision ----
@@ -673,7 +682,9 @@ __device__ void e_force_epilogue(EDev *e, ESys &s, const double (&v)[5], bool se
             s.best_f2 = s.fmax2;
             s.best_it = s.iter;
         }
-        const double exit_f = s.prec == 0 ? p.switch_fmax : (p.fmax_target > 0 ? p.fmax_target : 1e-10);
+        const double exit_f = s.prec == 0 ? p.switch_fmax
+                                          : (p.fmax_target > 0 ? p.fmax_target * (p.res ? s.dw_scale : 1.0)
+                                                               : 1e-10);
         const bool stalled = fmax < 100.0 * exit_f && s.iter - s.best_it > kStallIters;
         // a PE-change stop (pe_diff_target > 0) is only decided in FP64: once
         // the double-word energy has stopped changing at its own precision
@@ -685,6 +696,8 @@ __device__ void e_force_epilogue(EDev *e, ESys &s, const double (&v)[5], bool se
                 s.prec = 2;
                 s.best_f2 = s.fmax2;
                 s.best_it = s.iter;
+            } else if (p.res && s.prec == 2 && fmax <= exit_f && p.fmax_target > 0 && !pe_flat) {
+                s.verify = 1;  // resident form: an FP64 pass checks this state next
             } else {
                 s.prec = 1;
                 s.vel_f32 = 1;  // the next move takes the FP32 velocities over
@@ -706,6 +719,19 @@ __device__ void e_force_epilogue(EDev *e, ESys &s, const double (&v)[5], bool se
         if (s.stopped) finished = true;
     }
     if (!finished) return;
+    if (p.res && pass_prec != 1) {
+        // resident form: every finished minimisation ends with an FP64 pass at
+        // its final positions, whose totals are the reported ones
+        s.verify = 2;
+        return;
+    }
+    e_finish(e, s);
+}
+
+// A minimisation finished (the last force pass's totals are in s): the
+// jamming state machine decides the next transition.
+__device__ void e_finish(EDev *e, ESys &s) {
+    const EParams &p = e->p;
     s.converged = 1;
     s.minimizations++;
     if (!p.jam) { s.phase = kIdle; s.done = 1; atomicSub(&e->active, 1); return; }
@@ -1000,6 +1026,8 @@ __device__ __forceinline__ void e_transition_sys(const EParams &p, ESys &s, int 
     s.iter = 0;
     s.prec = (p.switch_fmax > 0 && s.ncd >= 3) ? 0 : 1;
     s.vel_f32 = 0;
+    s.verify = 0;
+    s.dw_scale = 0.9;
 }
 
 __global__ void __launch_bounds__(kEB) e_transition(EDev *e) {
