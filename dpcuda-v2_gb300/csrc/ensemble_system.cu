@@ -11,8 +11,8 @@
 #include <cstring>
 #include <vector>
 
-#include "ensemble_kernels.cuh"
 #include "host_common.h"
+#include "resident_kernels.cuh"
 
 using namespace dpg;
 
@@ -41,6 +41,10 @@ struct dpg_ensemble_system {
     int mode = 2;
     int form = DPG_FORM_AUTO, pthreads = 0;  // execution form and persistent block size
     int max_n = 0;
+    // resident form: one stream per size class, the block -> system lists
+    cudaStream_t rs_stream[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t rs_fork = nullptr, rs_join[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    int *d_rs_blocks = nullptr;
 };
 
 typedef dpg_ensemble_system ES;
@@ -61,6 +65,11 @@ static int ealloc(ES *s, void **p, size_t bytes) {
 extern "C" int dpg_ensemble_destroy(dpg_ensemble s) {
     if (!s) return DPG_OK;
     if (s->stream) cudaStreamSynchronize(s->stream);
+    for (int c = 0; c < 5; c++) {
+        if (s->rs_stream[c]) cudaStreamDestroy(s->rs_stream[c]);
+        if (s->rs_join[c]) cudaEventDestroy(s->rs_join[c]);
+    }
+    if (s->rs_fork) cudaEventDestroy(s->rs_fork);
     if (s->exec) cudaGraphExecDestroy(s->exec);
     for (void *p : s->allocs) cudaFree(p);
     if (s->h.nbr) cudaFree(s->h.nbr);
@@ -98,6 +107,7 @@ extern "C" int dpg_ensemble_create(const dpg_ensemble_params *p, const int64_t *
     const char *f = getenv("DPG_ENSEMBLE_FORM");
     if (f && !strcmp(f, "grid")) s->form = DPG_FORM_GRID;
     if (f && !strcmp(f, "persist")) s->form = DPG_FORM_PERSIST;
+    if (f && !strcmp(f, "resident")) s->form = DPG_FORM_RESIDENT;
     // layout: each system padded to whole blocks; its own cell grid
     s->sys.assign(s->S, ESys{});
     int slot = 0, blk = 0, cell = 0, item = 0;
@@ -154,6 +164,7 @@ extern "C" int dpg_ensemble_create(const dpg_ensemble_params *p, const int64_t *
     A((void **)&h.cell_items, 4 * T);
     A((void **)&h.part, 8 * 8 * (size_t)s->nblocks);
     A((void **)&s->xfer, 8 * 4 * std::max<size_t>(s->n_total, 1));
+    A((void **)&s->d_rs_blocks, 4 * (size_t)s->S);
     if (rc == DPG_OK) rc = alloc_nbr(s, s->cap);
     if (rc != DPG_OK) { dpg_ensemble_destroy(s); return rc; }
     h.sys = s->d_sys;
@@ -370,15 +381,166 @@ static int run(ES *s, long long guard_limit) {
     return set_err(DPG_ERR_STATE, "ensemble loop did not finish");
 }
 
+// ---- the resident form --------------------------------------------------------
+// Size classes (threads per block x particles per thread): a system goes to the
+// first class that holds it.
+struct RClass {
+    int nt, ppt;
+};
+static const RClass kRClasses[5] = {{64, 4}, {128, 4}, {256, 4}, {512, 4}, {512, 8}};
+
+static int res_class_of(int n) {
+    for (int c = 0; c < 5; c++)
+        if (n <= kRClasses[c].nt * kRClasses[c].ppt) return c;
+    return -1;
+}
+
+// largest cell count of the systems of class c
+static int res_ncmax(const ES *s, int c) {
+    int m = 1;
+    for (const auto &y : s->sys)
+        if (res_class_of(y.n) == c) m = std::max(m, y.ncd * y.ncd);
+    return m;
+}
+
+static int res_smem_limit() {
+    int dev = 0, v = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return 0;
+    return v;
+}
+
+// the resident form holds every system: sizes and shared memory within limits
+static bool res_fits(const ES *s) {
+    if (s->max_n > kResMaxN) return false;
+    const size_t lim = (size_t)res_smem_limit();
+    for (int c = 0; c < 5; c++) {
+        const size_t b = res_smem_bytes(kRClasses[c].nt * kRClasses[c].ppt, res_ncmax(s, c));
+        if (b + 4096 > lim) return false;  // room for the kernel's static shared memory
+    }
+    return true;
+}
+
+typedef void (*res_kernel_t)(EDev *, const int *, int, long long, unsigned long long);
+static res_kernel_t res_kernel(int c) {
+    switch (c) {
+    case 0: return e_res<64, 4>;
+    case 1: return e_res<128, 4>;
+    case 2: return e_res<256, 4>;
+    case 3: return e_res<512, 4>;
+    default: return e_res<512, 8>;
+    }
+}
+
+// Launch every class that has live systems, each on its own stream (forked
+// from and joined back into the ensemble's stream).  slice_ns bounds a launch.
+static int launch_resident(ES *s, long long budget, unsigned long long slice_ns, int *launched) {
+    *launched = 0;
+    std::vector<int> order[5];
+    for (int k = 0; k < s->S; k++) {
+        const ESys &y = s->sys[k];
+        if (y.phase == kIdle) continue;
+        order[res_class_of(y.n)].push_back(k);
+    }
+    std::vector<int> flat;
+    int first[5];
+    for (int c = 0; c < 5; c++) {
+        // largest systems first: they start before the small ones fill the SMs
+        std::sort(order[c].begin(), order[c].end(), [&](int a, int b) {
+            return s->sys[a].n != s->sys[b].n ? s->sys[a].n > s->sys[b].n : a < b;
+        });
+        first[c] = (int)flat.size();
+        flat.insert(flat.end(), order[c].begin(), order[c].end());
+    }
+    if (flat.empty()) return DPG_OK;
+    CK(cudaMemcpyAsync(s->d_rs_blocks, flat.data(), 4 * flat.size(), cudaMemcpyHostToDevice, s->stream));
+    if (!s->rs_fork) CK(cudaEventCreateWithFlags(&s->rs_fork, cudaEventDisableTiming));
+    CK(cudaEventRecord(s->rs_fork, s->stream));
+    for (int c = 0; c < 5; c++) {
+        const int nb = (int)order[c].size();
+        if (!nb) continue;
+        if (!s->rs_stream[c]) {
+            CK(cudaStreamCreateWithFlags(&s->rs_stream[c], cudaStreamNonBlocking));
+            CK(cudaEventCreateWithFlags(&s->rs_join[c], cudaEventDisableTiming));
+        }
+        const int ncmax = res_ncmax(s, c);
+        const size_t smem = res_smem_bytes(kRClasses[c].nt * kRClasses[c].ppt, ncmax);
+        res_kernel_t kern = res_kernel(c);
+        CK(cudaFuncSetAttribute((const void *)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        CK(cudaStreamWaitEvent(s->rs_stream[c], s->rs_fork, 0));
+        kern<<<nb, kRClasses[c].nt, smem, s->rs_stream[c]>>>(s->d, s->d_rs_blocks + first[c], ncmax, budget,
+                                                            slice_ns);
+        CK(cudaGetLastError());
+        CK(cudaEventRecord(s->rs_join[c], s->rs_stream[c]));
+        CK(cudaStreamWaitEvent(s->stream, s->rs_join[c], 0));
+        (*launched)++;
+    }
+    return DPG_OK;
+}
+
+static int grow_lists(ES *s, const EDev &cur) {
+    int ncap = 1;
+    while (ncap < cur.max_count) ncap <<= 1;
+    if ((size_t)ncap * s->T > ((size_t)1 << 31)) return set_err(DPG_ERR_OVERFLOW, "ensemble neighbour list too large");
+    TRY(alloc_nbr(s, ncap));
+    if (s->exec) { cudaGraphExecDestroy(s->exec); s->exec = nullptr; }
+    TRY(put(s, &s->d->nbr, s->h.nbr));
+    TRY(put(s, &s->d->p.cap, ncap));
+    TRY(put(s, &s->d->overflow, 0));
+    TRY(pull_sys(s));
+    for (auto &y : s->sys) if (y.phase != kIdle) y.rebuild = 1;
+    CK(cudaMemcpyAsync(s->d_sys, s->sys.data(), sizeof(ESys) * s->S, cudaMemcpyHostToDevice, s->stream));
+    return DPG_OK;
+}
+
+// Relaunch the resident kernels until every system is done.  Each launch runs
+// for at most kSlice of device time per block (so the classes' launches end
+// together and the host sees progress); termination is the device state
+// machine's (every minimisation has a step cap, jamming a compression cap);
+// the host stops with an error when some system's FIRE passes in this run
+// exceed guard_limit or a launch makes no progress.
+static int run_resident(ES *s, long long guard_limit) {
+    const unsigned long long kSlice = 200ull * 1000 * 1000;  // 0.2 s
+    const long long kChunk = 1LL << 24;
+    std::vector<long long> base(s->S, -1);
+    long long last_sum = -1;
+    for (int launches = 0; launches < (1 << 22); launches++) {
+        EDev cur;
+        TRY(pull_dev(s, &cur));
+        if (cur.overflow) {
+            TRY(grow_lists(s, cur));
+            last_sum = -1;
+            continue;
+        }
+        if (cur.active <= 0) return DPG_OK;
+        TRY(pull_sys(s));
+        long long most = 0, sum = 0;
+        for (int k = 0; k < s->S; k++) {
+            const long long f = s->sys[k].fire_total;
+            if (base[k] < 0) base[k] = f;
+            most = std::max(most, f - base[k]);
+            sum += f;
+        }
+        if (most > guard_limit) return set_err(DPG_ERR_NOT_CONVERGED, "ensemble loop budget spent");
+        if (sum == last_sum) return set_err(DPG_ERR_STATE, "resident launch made no progress");
+        last_sum = sum;
+        int nl = 0;
+        TRY(launch_resident(s, kChunk, kSlice, &nl));
+        if (!nl) return DPG_OK;
+    }
+    return set_err(DPG_ERR_STATE, "ensemble loop did not finish");
+}
+
 // ---- the persistent form ----------------------------------------------------
-// AUTO runs the grid form: on one GB300 it measured faster than the persistent
-// form both for 16 x 16384 disks (1.62 vs 0.34 FIRE solves/s) and for 32
-// systems of 64-4096 disks (3.5e8 vs 3.0e8 particle-iterations/s, 512-thread
-// blocks): one block per system keeps too few loads in flight per system.
-// dpg_ensemble_autotune measures and may choose either.
+// AUTO runs the resident form when it holds every system (at most 4096
+// particles each, shared memory within the device limit), else the grid form:
+// on one GB300 the grid form measured faster than the persistent form both for
+// 16 x 16384 disks (1.62 vs 0.34 FIRE solves/s) and for 32 systems of 64-4096
+// disks (3.5e8 vs 3.0e8 particle-iterations/s, 512-thread blocks).
+// dpg_ensemble_autotune measures and may choose any of them.
 static int form_of(const ES *s) {
     if (s->form != DPG_FORM_AUTO) return s->form;
-    return DPG_FORM_GRID;
+    return res_fits(s) ? DPG_FORM_RESIDENT : DPG_FORM_GRID;
 }
 
 static int threads_of(const ES *s) {
@@ -431,8 +593,12 @@ static int run_persist(ES *s, long long guard_limit) {
 
 extern "C" int dpg_ensemble_set_form(dpg_ensemble s, int form, int threads) {
     if (!s) return set_err(DPG_ERR_ARG, "null handle");
-    if (form != DPG_FORM_AUTO && form != DPG_FORM_GRID && form != DPG_FORM_PERSIST)
+    if (form != DPG_FORM_AUTO && form != DPG_FORM_GRID && form != DPG_FORM_PERSIST &&
+        form != DPG_FORM_RESIDENT)
         return set_err(DPG_ERR_ARG, "bad form");
+    if (form == DPG_FORM_RESIDENT && !res_fits(s))
+        return set_err(DPG_ERR_ARG, "resident form: systems of at most %d particles whose cell lists fit "
+                                    "shared memory", kResMaxN);
     if (threads != 0 && threads != 128 && threads != 256 && threads != 512)
         return set_err(DPG_ERR_ARG, "threads must be 0, 128, 256 or 512");
     s->form = form;
@@ -441,7 +607,7 @@ extern "C" int dpg_ensemble_set_form(dpg_ensemble s, int form, int threads) {
 }
 
 // per-system FIRE / jamming state reset and parameters upload (no launches)
-static int prepare(ES *s, const dpg_fire_params *fp, int jam, const dpg_jam_params *jp) {
+static int prepare(ES *s, const dpg_fire_params *fp, int jam, const dpg_jam_params *jp, int res = 0) {
     if (!s->have_state) return set_err(DPG_ERR_STATE, "set the state first");
     TRY(pull_sys(s));
     EParams &p = s->h.p;
@@ -449,6 +615,7 @@ static int prepare(ES *s, const dpg_fire_params *fp, int jam, const dpg_jam_para
     p.pe_target = fp->avg_pe_target; p.pe_diff_target = fp->avg_pe_diff_target;
     p.fmax_target = fp->fmax_target; p.max_steps = fp->max_steps;
     p.jam = jam;
+    p.res = res;
     if (jp) {
         p.p_low = jp->pressure_low; p.p_high = jp->pressure_high;
         p.compression_rate = jp->compression_rate; p.length_tol = jp->length_tolerance;
@@ -464,6 +631,9 @@ static int prepare(ES *s, const dpg_fire_params *fp, int jam, const dpg_jam_para
         y.ticket_a = y.ticket_b = 0;
         y.best_f2 = INFINITY; y.best_it = 0; y.vel_f32 = 0; y.fp64_total = 0; y.dw_total = 0;
         y.resume = 0;
+        y.res_valid = 0;
+        y.verify = 0;
+        y.dw_scale = 0.9;
     }
     CK(cudaMemcpyAsync(s->d_sys, s->sys.data(), sizeof(ESys) * s->S, cudaMemcpyHostToDevice, s->stream));
     CK(cudaMemcpyAsync(&s->d->p, &p, sizeof(EParams), cudaMemcpyHostToDevice, s->stream));
@@ -480,9 +650,11 @@ static int prepare(ES *s, const dpg_fire_params *fp, int jam, const dpg_jam_para
 }
 
 static int start(ES *s, const dpg_fire_params *fp, int jam, const dpg_jam_params *jp) {
-    TRY(prepare(s, fp, jam, jp));
+    const int form = form_of(s);
+    TRY(prepare(s, fp, jam, jp, form == DPG_FORM_RESIDENT));
     long long budget = jam ? (long long)4e9 : fp->max_steps * 2 + 16;
-    if (form_of(s) == DPG_FORM_PERSIST) TRY(run_persist(s, budget));
+    if (form == DPG_FORM_PERSIST) TRY(run_persist(s, budget));
+    else if (form == DPG_FORM_RESIDENT) TRY(run_resident(s, budget));
     else TRY(run(s, budget));
     TRY(pull_sys(s));
     return DPG_OK;
@@ -626,13 +798,14 @@ static int trial(ES *s, const double2 *saved, const dpg_fire_params *p, int iter
     const int f0 = s->form, t0 = s->pthreads;
     s->form = form;
     s->pthreads = nt;
-    TRY(prepare(s, &q, 0, nullptr));
+    TRY(prepare(s, &q, 0, nullptr, form == DPG_FORM_RESIDENT));
     cudaEvent_t a, b;
     CK(cudaEventCreate(&a));
     CK(cudaEventCreate(&b));
     CK(cudaEventRecord(a, s->stream));
-    int rc = form == DPG_FORM_PERSIST ? run_persist(s, (long long)iters * 2 + 16)
-                                      : run(s, (long long)iters * 2 + 16);
+    const long long g = (long long)iters * 2 + 16;
+    int rc = form == DPG_FORM_PERSIST ? run_persist(s, g)
+             : (form == DPG_FORM_RESIDENT ? run_resident(s, g) : run(s, g));
     cudaEventRecord(b, s->stream);
     cudaEventSynchronize(b);
     float ms = 0.f;
@@ -663,12 +836,14 @@ extern "C" int dpg_ensemble_autotune(dpg_ensemble s, const dpg_fire_params *p, i
     for (double f : skins) {
         cands.push_back({DPG_FORM_GRID, 0, s->prm.skin * f, 0.0});
         for (int nt : {128, 256, 512}) cands.push_back({DPG_FORM_PERSIST, nt, s->prm.skin * f, 0.0});
+        if (res_fits(s)) cands.push_back({DPG_FORM_RESIDENT, 0, s->prm.skin * f, 0.0});
     }
     int rc = DPG_OK;
     double warm = 0.0;
     // untimed first pass of each form (graph instantiation, module loading)
     rc = trial(s, saved, p, 4, DPG_FORM_GRID, 0, s->prm.skin, &warm);
     if (rc == DPG_OK) rc = trial(s, saved, p, 4, DPG_FORM_PERSIST, 256, s->prm.skin, &warm);
+    if (rc == DPG_OK && res_fits(s)) rc = trial(s, saved, p, 4, DPG_FORM_RESIDENT, 0, s->prm.skin, &warm);
     for (auto &c : cands) {
         if (rc != DPG_OK) break;
         rc = trial(s, saved, p, iters, c.form, c.nt, c.skin, &c.rate);

@@ -30,8 +30,8 @@ def partition_systems(n_particles, world):
         parts[r].append(k)
         loads[r] += n[k]
     return [sorted(p) for p in parts]
-FORM_AUTO, FORM_GRID, FORM_PERSIST = 0, 1, 2
-_FORM_NAMES = {FORM_GRID: "grid", FORM_PERSIST: "persist"}
+FORM_AUTO, FORM_GRID, FORM_PERSIST, FORM_RESIDENT = 0, 1, 2, 3
+_FORM_NAMES = {FORM_GRID: "grid", FORM_PERSIST: "persist", FORM_RESIDENT: "resident"}
 
 
 class Ensemble:
@@ -127,9 +127,11 @@ class Ensemble:
 
     def setForm(self, form=FORM_AUTO, threads=0):
         """FORM_GRID (one launch per stage over all systems, a CUDA graph loop),
-        FORM_PERSIST (one persistent block per system), FORM_AUTO (the grid
-        form, or the autotuner's choice); threads: the persistent block size
-        (128, 256, 512; 0 = by system size)."""
+        FORM_PERSIST (one persistent block per system), FORM_RESIDENT (one
+        block per system holding it on chip, systems of at most 4096
+        particles), FORM_AUTO (resident when it holds every system, else grid,
+        or the autotuner's choice); threads: the persistent block size (128,
+        256, 512; 0 = by system size)."""
         check(self.lib.dpg_ensemble_set_form(self.h, int(form), int(threads)))
 
     def autotune(self, iters=300, alpha_init=0.1, dt=1e-2):

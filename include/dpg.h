@@ -541,22 +541,32 @@ int dpg_ensemble_compute_forces(dpg_ensemble e, int precision, dpg_ensemble_resu
 /* pressure-band jamming of every system (the dpg_jam_pressure control flow) */
 int dpg_ensemble_jam(dpg_ensemble e, const dpg_jam_params *p, dpg_ensemble_result *per_system);
 
-/* Execution forms of an ensemble run (the same per-slot arithmetic; totals
- * round differently):
- *  DPG_FORM_GRID    every stage is one launch over all systems, the loop a
- *                   CUDA graph (best for few large systems);
- *  DPG_FORM_PERSIST one persistent block per system runs its whole
- *                   minimisation / jamming protocol with no further launches
- *                   (no grid-wide synchronisation; each system at its own pace);
- *  DPG_FORM_AUTO    the grid form, or the form dpg_ensemble_autotune chose. */
+/* Execution forms of an ensemble run (the same FIRE / jamming algorithm; the
+ * grid and persistent forms share the per-slot arithmetic, the resident form
+ * keeps positions as FP64 cell centres plus double-word FP32 offsets; totals
+ * round differently in each):
+ *  DPG_FORM_GRID     every stage is one launch over all systems, the loop a
+ *                    CUDA graph (best for few large systems);
+ *  DPG_FORM_PERSIST  one persistent block per system runs its whole
+ *                    minimisation / jamming protocol with no further launches
+ *                    (no grid-wide synchronisation; each system at its own pace);
+ *  DPG_FORM_RESIDENT one block per system holds the system on chip (packed
+ *                    offsets and cell lists in shared memory, per-particle
+ *                    dynamics in registers) for time-sliced persistent launches;
+ *                    FP64 pair arithmetic only verifies double-word states and
+ *                    measures finished minimisations; systems of at most 4096
+ *                    particles, in size classes that run side by side;
+ *  DPG_FORM_AUTO     the resident form when it holds every system, else the
+ *                    grid form, or the form dpg_ensemble_autotune chose. */
 #define DPG_FORM_AUTO 0
 #define DPG_FORM_GRID 1
 #define DPG_FORM_PERSIST 2
+#define DPG_FORM_RESIDENT 3
 /* threads: persistent form's threads per system block (128, 256 or 512; 0 = by size) */
 int dpg_ensemble_set_form(dpg_ensemble e, int form, int threads);
 
 typedef struct {
-    int form;                  /* chosen form (DPG_FORM_GRID / DPG_FORM_PERSIST) */
+    int form;                  /* chosen form (DPG_FORM_GRID / _PERSIST / _RESIDENT) */
     int threads;               /* chosen threads per system block (persistent form) */
     double skin;               /* chosen Verlet skin (the cutoff moves with it) */
     int n_candidates;
