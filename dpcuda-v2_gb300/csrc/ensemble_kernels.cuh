@@ -685,13 +685,17 @@ __device__ void e_force_epilogue(EDev *e, ESys &s, const double (&v)[5], bool se
         const double exit_f = s.prec == 0 ? p.switch_fmax
                                           : (p.fmax_target > 0 ? p.fmax_target * (p.res ? s.dw_scale : 1.0)
                                                                : 1e-10);
-        const bool stalled = fmax < 100.0 * exit_f && s.iter - s.best_it > kStallIters;
+        // (in the resident form a double-word system leaves only through its FP64
+        // check: its noise floor, ~1e-14 of the contact force, is far below any
+        // plateau of FIRE near jamming, and uphill runs there are FIRE's own)
+        const bool dw_res = p.res && s.prec == 2;
+        const bool stalled = !dw_res && fmax < 100.0 * exit_f && s.iter - s.best_it > kStallIters;
         // a PE-change stop (pe_diff_target > 0) is only decided in FP64: once
         // the double-word energy has stopped changing at its own precision
         // (1e-12 relative), hand over so the FP64 test can fire
         const bool pe_flat = s.prec == 2 && p.pe_diff_target > 0 &&
                              fabs(s.pe / (double)s.n / s.last_avg_pe - 1) < 1e-12;
-        if (fmax <= exit_f || s.nbad > 5 || stalled || pe_flat) {
+        if (fmax <= exit_f || (s.nbad > 5 && !dw_res) || stalled || pe_flat) {
             if (s.prec == 0 && p.dw_ok) {
                 s.prec = 2;
                 s.best_f2 = s.fmax2;
