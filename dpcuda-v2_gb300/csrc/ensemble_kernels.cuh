@@ -647,9 +647,12 @@ __device__ __forceinline__ void pair_f32(const float4 a, const float4 b, int ncd
 // Per-system epilogue of a force pass (thread 0 of the system's last block):
 // minimizeFire tests, the mixed-precision switch, the next FIRE decision and
 // the jamming state machine (scripts/runArthurJamWithFire.cpp:36-106).
-__device__ void e_finish(EDev *e, ESys &s);
+__device__ void e_finish(EDev *e, ESys &s, bool primary = true);
 
-__device__ void e_force_epilogue(EDev *e, ESys &s, const double (&v)[5], bool setup) {
+// primary: this copy of the system state performs the global side effects
+// (a cluster of the resident form keeps one identical copy per block)
+__device__ void e_force_epilogue(EDev *e, ESys &s, const double (&v)[5], bool setup,
+                                 bool primary = true) {
     const EParams &p = e->p;
     // ---- per-system epilogue: minimizeFire tests and the next FIRE decision ----
     s.pe = v[0];
@@ -729,16 +732,21 @@ __device__ void e_force_epilogue(EDev *e, ESys &s, const double (&v)[5], bool se
         s.verify = 2;
         return;
     }
-    e_finish(e, s);
+    e_finish(e, s, primary);
 }
 
 // A minimisation finished (the last force pass's totals are in s): the
 // jamming state machine decides the next transition.
-__device__ void e_finish(EDev *e, ESys &s) {
+__device__ void e_finish(EDev *e, ESys &s, bool primary) {
     const EParams &p = e->p;
     s.converged = 1;
     s.minimizations++;
-    if (!p.jam) { s.phase = kIdle; s.done = 1; atomicSub(&e->active, 1); return; }
+    if (!p.jam) {
+        s.phase = kIdle;
+        s.done = 1;
+        if (primary) atomicSub(&e->active, 1);
+        return;
+    }
     // ---- jamming state machine (scripts/runArthurJamWithFire.cpp:36-106) ----
     // pressure with v = 0: sum_ij r_ij . f_ij / (4 A)
     double A = s.L * s.L;
@@ -782,7 +790,7 @@ __device__ void e_finish(EDev *e, ESys &s) {
         s.pending = kActNone;
         s.phase = kIdle;
         s.done = 1;
-        atomicSub(&e->active, 1);
+        if (primary) atomicSub(&e->active, 1);
         return;
     }
     s.scale = Lnew / L_prior;

@@ -382,16 +382,18 @@ static int run(ES *s, long long guard_limit) {
 }
 
 // ---- the resident form --------------------------------------------------------
-// Size classes (threads per block x particles per thread): a system goes to the
-// first class that holds it.
+// Size classes (threads per block x particles per thread x blocks per
+// cluster): a system goes to the first class that holds it.
 struct RClass {
-    int nt, ppt;
+    int nt, ppt, c;
+    int per_block() const { return nt * ppt; }
+    int capacity() const { return nt * ppt * c; }
 };
-static const RClass kRClasses[5] = {{64, 4}, {128, 4}, {256, 4}, {512, 4}, {512, 8}};
+static const RClass kRClasses[5] = {{64, 4, 1}, {128, 4, 1}, {256, 4, 1}, {256, 4, 2}, {256, 4, 4}};
 
 static int res_class_of(int n) {
     for (int c = 0; c < 5; c++)
-        if (n <= kRClasses[c].nt * kRClasses[c].ppt) return c;
+        if (n <= kRClasses[c].capacity()) return c;
     return -1;
 }
 
@@ -415,7 +417,7 @@ static bool res_fits(const ES *s) {
     if (s->max_n > kResMaxN) return false;
     const size_t lim = (size_t)res_smem_limit();
     for (int c = 0; c < 5; c++) {
-        const size_t b = res_smem_bytes(kRClasses[c].nt * kRClasses[c].ppt, res_ncmax(s, c));
+        const size_t b = res_smem_bytes(kRClasses[c].per_block(), kRClasses[c].capacity(), res_ncmax(s, c));
         if (b + 4096 > lim) return false;  // room for the kernel's static shared memory
     }
     return true;
@@ -424,11 +426,11 @@ static bool res_fits(const ES *s) {
 typedef void (*res_kernel_t)(EDev *, const int *, int, long long, unsigned long long);
 static res_kernel_t res_kernel(int c) {
     switch (c) {
-    case 0: return e_res<64, 4>;
-    case 1: return e_res<128, 4>;
-    case 2: return e_res<256, 4>;
-    case 3: return e_res<512, 4>;
-    default: return e_res<512, 8>;
+    case 0: return e_res<64, 4, 1>;
+    case 1: return e_res<128, 4, 1>;
+    case 2: return e_res<256, 4, 1>;
+    case 3: return e_res<256, 4, 2>;
+    default: return e_res<256, 4, 4>;
     }
 }
 
@@ -463,14 +465,28 @@ static int launch_resident(ES *s, long long budget, unsigned long long slice_ns,
             CK(cudaStreamCreateWithFlags(&s->rs_stream[c], cudaStreamNonBlocking));
             CK(cudaEventCreateWithFlags(&s->rs_join[c], cudaEventDisableTiming));
         }
+        const RClass &K = kRClasses[c];
         const int ncmax = res_ncmax(s, c);
-        const size_t smem = res_smem_bytes(kRClasses[c].nt * kRClasses[c].ppt, ncmax);
+        const size_t smem = res_smem_bytes(K.per_block(), K.capacity(), ncmax);
         res_kernel_t kern = res_kernel(c);
         CK(cudaFuncSetAttribute((const void *)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         CK(cudaStreamWaitEvent(s->rs_stream[c], s->rs_fork, 0));
-        kern<<<nb, kRClasses[c].nt, smem, s->rs_stream[c]>>>(s->d, s->d_rs_blocks + first[c], ncmax, budget,
-                                                            slice_ns);
-        CK(cudaGetLastError());
+        // one cluster of K.c blocks per system
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(nb * K.c);
+        cfg.blockDim = dim3(K.nt);
+        cfg.dynamicSmemBytes = smem;
+        cfg.stream = s->rs_stream[c];
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = K.c;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        const int *blocks = s->d_rs_blocks + first[c];
+        EDev *dev = s->d;
+        CK(cudaLaunchKernelEx(&cfg, kern, dev, blocks, ncmax, budget, slice_ns));
         CK(cudaEventRecord(s->rs_join[c], s->rs_stream[c]));
         CK(cudaStreamWaitEvent(s->stream, s->rs_join[c], 0));
         (*launched)++;

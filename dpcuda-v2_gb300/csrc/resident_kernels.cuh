@@ -34,10 +34,19 @@
 // so where a launch ends does not change any result.  Blocks never wait on one
 // another.
 //
-// Size classes: NT threads x PPT particles per thread cover systems of at most
-// NT * PPT particles; the host launches each class on its own stream so the
-// classes run side by side.
+// Size classes: a system of a class runs on a thread-block cluster of C
+// blocks of NT threads, each thread owning PPT particles; block r of the
+// cluster owns the particles [r M, (r + 1) M), M = NT * PPT, and holds their
+// packed offsets in its shared memory.  Neighbours owned by another block of
+// the cluster are read from its shared memory (distributed shared memory);
+// every block keeps an identical copy of the system state and of the cell
+// list, per-system totals are exchanged between the blocks and summed in
+// block order, so every copy takes the same decisions (only block 0 performs
+// the global side effects).  The host launches each class on its own stream
+// so the classes run side by side.
 #pragma once
+#include <cooperative_groups.h>
+
 #include "ensemble_kernels.cuh"
 
 namespace dpg {
@@ -68,32 +77,55 @@ __device__ __forceinline__ float2 split_lo(double ox, double oy, float hx, float
     return make_float2((float)(ox - (double)hx), (float)(oy - (double)hy));
 }
 
-// shared-memory layout of one resident system (dynamic shared memory)
+// shared-memory layout of one block of a resident system (dynamic shared memory)
 struct RLayout {
-    float4 *pk;               // [nmax] {offset hi x, offset hi y, radius hi, cell code}
-    float4 *pkl;              // [nmax] {offset lo x, offset lo y, radius lo, 0}
-    int *cstart;              // [ncmax + 1] first item of each cell
+    float4 *pk;               // [m] own particles {offset hi x, offset hi y, radius hi, cell code}
+    float4 *pkl;              // [m] own particles {offset lo x, offset lo y, radius lo, 0}
+    int *cstart;              // [ncmax + 1] first item of each cell (the whole system)
     int *ccur;                // [ncmax] counts, then fill cursors
-    unsigned short *citem;    // [nmax] particle (local index) of each cell item
+    unsigned short *citem;    // [nsys] particle (system index) of each cell item
 };
 
-__host__ __device__ inline size_t res_smem_bytes(int nmax, int ncmax) {
-    return (size_t)32 * nmax + (size_t)4 * (2 * (size_t)ncmax + 1) + (size_t)2 * nmax + 16;
+// m: particles per block, nsys: particles per system (C m)
+__host__ __device__ inline size_t res_smem_bytes(int m, int nsys, int ncmax) {
+    return (size_t)32 * m + (size_t)4 * (2 * (size_t)ncmax + 1) + (size_t)2 * nsys + 16;
 }
 
-__device__ __forceinline__ RLayout res_layout(float4 *base, int nmax, int ncmax) {
+__device__ __forceinline__ RLayout res_layout(float4 *base, int m, int ncmax) {
     RLayout L;
     L.pk = base;
-    L.pkl = base + nmax;
-    L.cstart = reinterpret_cast<int *>(base + 2 * nmax);
+    L.pkl = base + m;
+    L.cstart = reinterpret_cast<int *>(base + 2 * m);
     L.ccur = L.cstart + ncmax + 1;
     L.citem = reinterpret_cast<unsigned short *>(L.ccur + ncmax);
     return L;
 }
 
-// FP64 position of local particle l from its cell centre and double-word offset
-__device__ __forceinline__ double2 res_position(const RLayout &L, const double2 c, int l) {
-    const float4 a = L.pk[l], b = L.pkl[l];
+// packed offsets of particle j (system index) of a cluster of C blocks of M
+// particles each: block j / M holds them
+template <int C, int M>
+__device__ __forceinline__ const float4 *res_pk_of(const RLayout &L, int j) {
+    if constexpr (C == 1) {
+        return L.pk + j;
+    } else {
+        const int q = j / M;
+        return cooperative_groups::this_cluster().map_shared_rank(L.pk, q) + (j - q * M);
+    }
+}
+template <int C, int M>
+__device__ __forceinline__ const float4 *res_pkl_of(const RLayout &L, int j) {
+    if constexpr (C == 1) {
+        return L.pkl + j;
+    } else {
+        const int q = j / M;
+        return cooperative_groups::this_cluster().map_shared_rank(L.pkl, q) + (j - q * M);
+    }
+}
+
+// FP64 position of own particle lo (block-local index) from its cell centre
+// and double-word offset
+__device__ __forceinline__ double2 res_position(const RLayout &L, const double2 c, int lo) {
+    const float4 a = L.pk[lo], b = L.pkl[lo];
     return make_double2(c.x + ((double)a.x + (double)b.x), c.y + ((double)a.y + (double)b.y));
 }
 
@@ -143,25 +175,26 @@ __device__ __forceinline__ void res_dcell(int ca, int cb, int ncd, int &dcx, int
     if (dcy > ncd / 2) dcy -= ncd; else if (dcy < -(ncd / 2)) dcy += ncd;
 }
 
-// ---- FP32 pair terms of local particle l from the shared offsets --------------
-__device__ __forceinline__ void res_forces_f32(const EDev *e, const ESys &s, const RLayout &L, int l,
+// ---- FP32 pair terms of own particle lo (slot i) from the shared offsets -------
+// (neighbour lists are written by the running launch: plain, coherent loads)
+template <int C, int M>
+__device__ __forceinline__ void res_forces_f32(const EDev *e, const ESys &s, const RLayout &L, int lo,
                                                int i, float &ax, float &ay, float &en, float &wv,
                                                int &ncount) {
     const int T = e->p.T, cnt = min(e->cnt[i], e->p.cap), off = s.off;
     const float ecf = (float)e->p.e_c, ncf = (float)e->p.n_c;
-    const float4 a = L.pk[l];
+    const float4 a = L.pk[lo];
     ax = 0.f; ay = 0.f; en = 0.f; wv = 0.f; ncount = 0;
     for (int k0 = 0; k0 < cnt; k0 += 8) {
         int jj[8];
-        // lists written by this launch: plain (coherent) loads
 #pragma unroll
-        for (int u = 0; u < 8; u++) jj[u] = k0 + u < cnt ? e->nbr[(size_t)(k0 + u) * T + i] - off : l;
+        for (int u = 0; u < 8; u++) jj[u] = k0 + u < cnt ? e->nbr[(size_t)(k0 + u) * T + i] - off : 0;
 #pragma unroll
         for (int u = 0; u < 8; u++) {
             if (k0 + u >= cnt) break;
             float fx, fy, ef, wf;
             int ct;
-            pair_f32(a, L.pk[jj[u]], s.ncd, s.cs_f, ecf, ncf, fx, fy, ef, wf, ct);
+            pair_f32(a, *res_pk_of<C, M>(L, jj[u]), s.ncd, s.cs_f, ecf, ncf, fx, fy, ef, wf, ct);
             ax += fx;
             ay += fy;
             en += ef;
@@ -171,14 +204,15 @@ __device__ __forceinline__ void res_forces_f32(const EDev *e, const ESys &s, con
     }
 }
 
-// ---- double-word pair terms of local particle l (full double-word path) -------
+// ---- double-word pair terms of own particle lo (full double-word path) --------
 // Pairs the hi offsets rule out (a 1e-4 relative margin on the contact
 // distance) are skipped; the rest run in double-word arithmetic.  The energy is
 // a double word (the energy-change stop test needs it).
-__device__ __forceinline__ void res_forces_dw(const EDev *e, const ESys &s, const RLayout &L, int l,
+template <int C, int M>
+__device__ __forceinline__ void res_forces_dw(const EDev *e, const ESys &s, const RLayout &L, int lo,
                                               int i, dw &sx, dw &sy, dw &se, float &sw, int &ncount) {
     const int T = e->p.T, cnt = min(e->cnt[i], e->p.cap), off = s.off;
-    const float4 a = L.pk[l], al = L.pkl[l];
+    const float4 a = L.pk[lo], al = L.pkl[lo];
     const dw xi = {a.x, al.x}, yi = {a.y, al.y}, ri = {a.z, al.z};
     const dw csd = {s.cs_f, s.cs_lo}, ec = {e->p.ec_hi, e->p.ec_lo};
     const int ca = __float_as_int(a.w), ncd = s.ncd;
@@ -186,18 +220,18 @@ __device__ __forceinline__ void res_forces_dw(const EDev *e, const ESys &s, cons
     for (int k0 = 0; k0 < cnt; k0 += 4) {
         int jj[4];
 #pragma unroll
-        for (int u = 0; u < 4; u++) jj[u] = k0 + u < cnt ? e->nbr[(size_t)(k0 + u) * T + i] - off : l;
+        for (int u = 0; u < 4; u++) jj[u] = k0 + u < cnt ? e->nbr[(size_t)(k0 + u) * T + i] - off : 0;
 #pragma unroll
         for (int u = 0; u < 4; u++) {
             if (k0 + u >= cnt) break;
-            const float4 b = L.pk[jj[u]];
+            const float4 b = *res_pk_of<C, M>(L, jj[u]);
             int dcx, dcy;
             res_dcell(ca, __float_as_int(b.w), ncd, dcx, dcy);
             const float dxf = (a.x - b.x) + (float)dcx * s.cs_f;
             const float dyf = (a.y - b.y) + (float)dcy * s.cs_f;
             const float rsf = a.z + b.z;
             if (dxf * dxf + dyf * dyf >= rsf * rsf * 1.0001f) continue;
-            const float4 bl = L.pkl[jj[u]];
+            const float4 bl = *res_pkl_of<C, M>(L, jj[u]);
             dw dx = dw_add(dw_add(xi, dw_neg(dw{b.x, bl.x})), dw_mul_f(csd, (float)dcx));
             dw dy = dw_add(dw_add(yi, dw_neg(dw{b.y, bl.y})), dw_mul_f(csd, (float)dcy));
             dw rs = dw_add(ri, dw{b.z, bl.z});
@@ -225,11 +259,12 @@ __device__ __forceinline__ void res_forces_dw(const EDev *e, const ESys &s, cons
 // step).  Forces are accumulated with compensated sums; the energy
 // e_c / 4 ((sigma^2 - d^2) / (sigma (sigma + d)))^2 and the virial in FP32
 // (relative 1e-7; the energy-change stop test uses the full double-word path).
-__device__ __forceinline__ void res_forces_dwf(const EDev *e, const ESys &s, const RLayout &L, int l,
+template <int C, int M>
+__device__ __forceinline__ void res_forces_dwf(const EDev *e, const ESys &s, const RLayout &L, int lo,
                                                int i, dw &sx, dw &sy, float &se, float &sw,
                                                int &ncount) {
     const int T = e->p.T, cnt = min(e->cnt[i], e->p.cap), off = s.off;
-    const float4 a = L.pk[l], al = L.pkl[l];
+    const float4 a = L.pk[lo], al = L.pkl[lo];
     const float csh = s.cs_f, csl = s.cs_lo, ech = e->p.ec_hi, ecl = e->p.ec_lo;
     const int ca = __float_as_int(a.w), ncd = s.ncd;
     float fxh = 0.f, fxl = 0.f, fyh = 0.f, fyl = 0.f;
@@ -237,11 +272,11 @@ __device__ __forceinline__ void res_forces_dwf(const EDev *e, const ESys &s, con
     for (int k0 = 0; k0 < cnt; k0 += 4) {
         int jj[4];
 #pragma unroll
-        for (int u = 0; u < 4; u++) jj[u] = k0 + u < cnt ? e->nbr[(size_t)(k0 + u) * T + i] - off : l;
+        for (int u = 0; u < 4; u++) jj[u] = k0 + u < cnt ? e->nbr[(size_t)(k0 + u) * T + i] - off : 0;
 #pragma unroll
         for (int u = 0; u < 4; u++) {
             if (k0 + u >= cnt) break;
-            const float4 b = L.pk[jj[u]];
+            const float4 b = *res_pk_of<C, M>(L, jj[u]);
             int dcx, dcy;
             res_dcell(ca, __float_as_int(b.w), ncd, dcx, dcy);
             const float cx = (float)dcx, cy = (float)dcy;
@@ -249,7 +284,7 @@ __device__ __forceinline__ void res_forces_dwf(const EDev *e, const ESys &s, con
             const float dyf = (a.y - b.y) + cy * csh;
             const float rsf = a.z + b.z;
             if (dxf * dxf + dyf * dyf >= rsf * rsf * 1.0001f) continue;
-            const float4 bl = L.pkl[jj[u]];
+            const float4 bl = *res_pkl_of<C, M>(L, jj[u]);
             // displacement as double words
             const dw tx = two_sum(a.x, -b.x), px = two_prod(cx, csh), ux = two_sum(tx.hi, px.hi);
             const dw dx = two_sum(ux.hi, tx.lo + px.lo + ux.lo + (al.x - bl.x) + cx * csl);
@@ -300,21 +335,23 @@ __device__ __forceinline__ void res_forces_dwf(const EDev *e, const ESys &s, con
     sy = two_sum(fyh, fyl);
 }
 
-// ---- FP64 pair terms of local particle l (the reference arithmetic on FP64
-// positions; 1/d and 1/rs by Newton steps as in the grid form) -----------------
-__device__ __forceinline__ void res_forces_f64(const EDev *e, const ESys &s, const RLayout &L, int l,
+// ---- FP64 pair terms of own particle lo (the reference arithmetic on FP64
+// positions; 1/d and 1/rs by Newton steps as in the grid form).  Neighbour
+// positions may have been written by another block of the cluster: L2 loads.
+template <int C, int M>
+__device__ __forceinline__ void res_forces_f64(const EDev *e, const ESys &s, const RLayout &L, int lo,
                                                int i, double &ax, double &ay, double &en, double &wv,
                                                double &nc) {
     const EParams &p = e->p;
     const int T = p.T, cnt = min(e->cnt[i], p.cap), off = s.off, ncd = s.ncd;
-    const float4 a = L.pk[l];
+    const float4 a = L.pk[lo];
     const double2 xi = e->pos[i];
     const double ri = e->rad[i];
     ax = 0.0; ay = 0.0; en = 0.0; wv = 0.0; nc = 0.0;
     for (int k = 0; k < cnt; k++) {
         const int j = e->nbr[(size_t)k * T + i];
         if (ncd >= 3) {
-            const float4 b = L.pk[j - off];
+            const float4 b = *res_pk_of<C, M>(L, j - off);
             int dcx, dcy;
             res_dcell(__float_as_int(a.w), __float_as_int(b.w), ncd, dcx, dcy);
             const float dxf = (a.x - b.x) + (float)dcx * s.cs_f;
@@ -322,7 +359,7 @@ __device__ __forceinline__ void res_forces_f64(const EDev *e, const ESys &s, con
             const float rsf = a.z + b.z;
             if (dxf * dxf + dyf * dyf >= rsf * rsf * 1.0001f) continue;
         }
-        const double2 xj = e->pos[j];
+        const double2 xj = __ldcg(&e->pos[j]);
         const double dx = pbc_dist(xi.x, xj.x, s.L), dy = pbc_dist(xi.y, xj.y, s.L);
         const double rs = ri + e->rad[j];
         const double d2 = dx * dx + dy * dy;
@@ -341,12 +378,13 @@ __device__ __forceinline__ void res_forces_f64(const EDev *e, const ESys &s, con
     }
 }
 
-// ---- neighbour list of local particle l from the shared cell list -------------
-__device__ __forceinline__ int res_nlist(EDev *e, const ESys &s, const RLayout &L, int l, int i) {
+// ---- neighbour list of own particle lo (system index l, slot i) ---------------
+template <int C, int M>
+__device__ __forceinline__ int res_nlist(EDev *e, const ESys &s, const RLayout &L, int lo, int l, int i) {
     const int T = e->p.T, cap = e->p.cap, ncd = s.ncd, off = s.off;
     int cnt = 0;
     if (ncd >= 3 && s.cs * s.cs >= e->p.cutoff2) {
-        const float4 a = L.pk[l];
+        const float4 a = L.pk[lo];
         const int c = __float_as_int(a.w), cx = code_x(c), cy = code_y(c);
         // FP32 distances with a 1e-4 relative margin: a superset of the list
         const float c2f = e->p.cutoff2_f * 1.0001f, cs = s.cs_f;
@@ -359,7 +397,7 @@ __device__ __forceinline__ int res_nlist(EDev *e, const ESys &s, const RLayout &
                 for (int k = b0; k < b1; k++) {
                     const int j = L.citem[k];
                     if (j == l) continue;
-                    const float4 b = L.pk[j];
+                    const float4 b = *res_pk_of<C, M>(L, j);
                     const float dx = (a.x - b.x) - sx, dy = (a.y - b.y) - sy;
                     if (dx * dx + dy * dy < c2f) {
                         if (cnt < cap) e->nbr[(size_t)cnt * T + i] = off + j;
@@ -373,7 +411,7 @@ __device__ __forceinline__ int res_nlist(EDev *e, const ESys &s, const RLayout &
         const double c2 = e->p.cutoff2;
         for (int j = off; j < off + s.n; j++) {
             if (j == i) continue;
-            const double2 xj = e->pos[j];
+            const double2 xj = __ldcg(&e->pos[j]);
             const double dx = pbc_dist(xi.x, xj.x, s.L), dy = pbc_dist(xi.y, xj.y, s.L);
             if (dx * dx + dy * dy < c2) {
                 if (cnt < cap) e->nbr[(size_t)cnt * T + i] = j;
@@ -429,7 +467,7 @@ __device__ __forceinline__ void res_scan(const RLayout &L, int nc, int *wsum, in
 // target finishes with these FP64 totals; otherwise the double-word loop goes
 // on with its exit threshold halved.  FIRE's state is not touched: the pass is
 // a measurement, not an iteration.
-__device__ void res_verify_epilogue(EDev *e, ESys &s, const double (&v)[5], int kind) {
+__device__ void res_verify_epilogue(EDev *e, ESys &s, const double (&v)[5], int kind, bool primary) {
     const EParams &p = e->p;
     s.verify = 0;
     s.fire_total++;
@@ -442,25 +480,60 @@ __device__ void res_verify_epilogue(EDev *e, ESys &s, const double (&v)[5], int 
         s.fmax2 = v[2];
         s.virial = v[3];
         s.contacts = v[4];
-        e_finish(e, s);
+        e_finish(e, s, primary);
     } else {
         s.dw_scale *= 0.5;
     }
 }
 
+// per-block totals exchanged between the blocks of a cluster
+struct RPart {
+    dw pe;
+    float v[4];
+    int req;          // block 0: leave the loop after this iteration (time slice, overflow)
+};
+struct RPartD {
+    double v[5];
+    int req;
+};
+
 struct RCtl {
-    int stop;         // leave the loop (uniform decision of thread 0)
+    int stop;         // leave the loop (uniform decision)
+    int req;          // block 0's request, seen by every block after an exchange
     int wsum[32];
     int carry;
     int imax[32];
+    int rb_in[8];     // rebuild requests of the cluster's blocks
+    int mx_in[8];     // longest neighbour list of each block
+    RPart part_in[8];
+    RPartD partd_in[8];
 };
 
-// The resident kernel.  sys_of_block[b]: the system of block b (one class);
-// nmax = NT * PPT and ncmax (cells) size the dynamic shared memory;
-// iter_budget: most iterations per system in this launch; slice_ns: the
-// launch's time slice per block (0 = none).
-template <int NT, int PPT>
-__global__ void __launch_bounds__(NT) e_res(EDev *e, const int *sys_of_block, int ncmax,
+// cluster-wide barrier (release / acquire; a block barrier for one block)
+template <int C>
+__device__ __forceinline__ void res_csync() {
+    if constexpr (C == 1) __syncthreads();
+    else cooperative_groups::this_cluster().sync();
+}
+
+// thread 0 writes x into slot r of field f of every block of the cluster
+template <int C, typename Tv>
+__device__ __forceinline__ void res_bcast(Tv *field, int r, const Tv &x) {
+    if constexpr (C == 1) {
+        field[r] = x;
+    } else {
+        auto cl = cooperative_groups::this_cluster();
+#pragma unroll
+        for (int q = 0; q < C; q++) cl.map_shared_rank(field, q)[r] = x;
+    }
+}
+
+// The resident kernel: one system per cluster of C blocks (C = 1: one block).
+// sys_of_cluster[b]: the system of cluster b (one class); ncmax (cells) sizes
+// the dynamic shared memory; iter_budget: most iterations per system in this
+// launch; slice_ns: the launch's time slice (0 = none).
+template <int NT, int PPT, int C>
+__global__ void __launch_bounds__(NT) e_res(EDev *e, const int *sys_of_cluster, int ncmax,
                                           long long iter_budget, unsigned long long slice_ns) {
     extern __shared__ float4 res_smem[];
     __shared__ ESys s;
@@ -468,47 +541,50 @@ __global__ void __launch_bounds__(NT) e_res(EDev *e, const int *sys_of_block, in
     __shared__ dw smw[NT / 32];
     __shared__ float smv[NT / 32 * 4];
     __shared__ double smd[32 * 5];
-    constexpr int NMAX = NT * PPT;
-    const RLayout L = res_layout(res_smem, NMAX, ncmax);
+    constexpr int M = NT * PPT;
+    const RLayout L = res_layout(res_smem, M, ncmax);
     const int t = threadIdx.x;
-    const int sid = sys_of_block[blockIdx.x];
+    const int r = C == 1 ? 0 : (int)cooperative_groups::this_cluster().block_rank();
+    const bool primary = r == 0;
+    const int sid = sys_of_cluster[blockIdx.x / C];
     unsigned long long t_end = 0;
     if (t == 0) {
         s = e->sys[sid];
+        ctl.req = 0;
         t_end = slice_ns ? global_ns() + slice_ns : 0ull;
     }
     __syncthreads();
     const EParams &p = e->p;
-    const int n = s.n, off = s.off;
+    const int n = s.n, off = s.off, base = r * M;
 
-    // ---- load: offsets (exact double words, or split from the FP64 positions),
-    // velocity, force, last-build offsets
+    // ---- load own particles: offsets (exact double words, or split from the FP64
+    // positions), velocity, force, last-build offsets
     float2 u[PPT], fr[PPT], frl[PPT], orf[PPT];
     float im[PPT];
 #pragma unroll
     for (int k = 0; k < PPT; k++) {
-        const int l = t + k * NT;
+        const int lo = t + k * NT, l = base + lo;
         u[k] = make_float2(0.f, 0.f); fr[k] = u[k]; frl[k] = u[k]; orf[k] = u[k]; im[k] = 1.f;
         if (l >= n) continue;
         const int i = off + l;
         if (s.res_valid) {
-            L.pk[l] = e->pk[i];
-            L.pkl[l] = e->pkl[i];
+            L.pk[lo] = e->pk[i];
+            L.pkl[lo] = e->pkl[i];
         } else {
             const double2 x = e->pos[i], c = e->ctr[i];
-            const double r = e->rad[i];
+            const double rad = e->rad[i];
             const double ox = x.x - c.x, oy = x.y - c.y;
-            const float hx = (float)ox, hy = (float)oy, hr = (float)r;
-            L.pk[l] = make_float4(hx, hy, hr, __int_as_float(e->cellc[i]));
-            const float2 lo = split_lo(ox, oy, hx, hy);
-            L.pkl[l] = make_float4(lo.x, lo.y, (float)(r - (double)hr), 0.f);
+            const float hx = (float)ox, hy = (float)oy, hr = (float)rad;
+            L.pk[lo] = make_float4(hx, hy, hr, __int_as_float(e->cellc[i]));
+            const float2 lw = split_lo(ox, oy, hx, hy);
+            L.pkl[lo] = make_float4(lw.x, lw.y, (float)(rad - (double)hr), 0.f);
         }
         u[k] = e->vel32[i];
         fr[k] = e->frc32[i];
         orf[k] = e->oref[i];
         im[k] = e->invm[i];
     }
-    __syncthreads();
+    res_csync<C>();
 
     // e->pos lags the offsets (an FP32 / double-word move since the last
     // materialisation); every thread tracks it identically
@@ -516,9 +592,11 @@ __global__ void __launch_bounds__(NT) e_res(EDev *e, const int *sys_of_block, in
     long long it = 0;
     const float half_skin2_f = (float)p.half_skin2;
     for (;;) {
+        // ---- uniform loop exit: every block holds the same copy of s and the
+        // same request of block 0 (exchanged with the last totals)
         if (t == 0) {
-            int st = (s.phase == kIdle) || (it >= iter_budget);
-            if (!st && (it & 31) == 0) {
+            int st = (s.phase == kIdle) || (it >= iter_budget) || ctl.req;
+            if (C == 1 && !st && (it & 31) == 0) {
                 if (*(volatile int *)&e->overflow) st = 1;
                 else if (t_end && global_ns() > t_end) st = 1;
             }
@@ -526,27 +604,32 @@ __global__ void __launch_bounds__(NT) e_res(EDev *e, const int *sys_of_block, in
         }
         __syncthreads();
         if (ctl.stop) break;
+        // block 0's request to leave after this iteration (multi-block clusters)
+        int req = 0;
+        if (C > 1 && primary && t == 0 && (it & 31) == 31)
+            req = (*(volatile int *)&e->overflow) || (t_end && global_ns() > t_end);
 
         if (s.verify) {
             // ---- FP64 pass at the current positions (no move, no kick)
             const int kind = s.verify;
 #pragma unroll
             for (int k = 0; k < PPT; k++) {
-                const int l = t + k * NT;
+                const int lo = t + k * NT, l = base + lo;
                 if (!pstale || l >= n) break;
                 const int i = off + l;
-                e->pos[i] = res_position(L, e->ctr[i], l);
+                e->pos[i] = res_position(L, e->ctr[i], lo);
             }
             pstale = false;
-            __syncthreads();
+            if (C > 1) __threadfence();
+            res_csync<C>();
             double a[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
 #pragma unroll
             for (int k = 0; k < PPT; k++) {
-                const int l = t + k * NT;
+                const int lo = t + k * NT, l = base + lo;
                 if (l >= n) break;
                 const int i = off + l;
                 double ax, ay, en, wv, nc;
-                res_forces_f64(e, s, L, l, i, ax, ay, en, wv, nc);
+                res_forces_f64<C, M>(e, s, L, lo, i, ax, ay, en, wv, nc);
                 e->frc[i] = make_double2(ax, ay);
                 fr[k] = make_float2((float)ax, (float)ay);
                 frl[k] = make_float2((float)(ax - (double)fr[k].x), (float)(ay - (double)fr[k].y));
@@ -558,7 +641,28 @@ __global__ void __launch_bounds__(NT) e_res(EDev *e, const int *sys_of_block, in
             }
             const int ops[5] = {0, 0, 1, 0, 0};
             block_reduce<5, double>(a, ops, smd);
-            if (t == 0) res_verify_epilogue(e, s, a, kind);
+            if (t == 0) {
+                RPartD pd;
+#pragma unroll
+                for (int q = 0; q < 5; q++) pd.v[q] = a[q];
+                pd.req = req;
+                res_bcast<C>(ctl.partd_in, r, pd);
+            }
+            res_csync<C>();
+            if (t == 0) {
+                double tot[5];
+#pragma unroll
+                for (int q = 0; q < 5; q++) tot[q] = ctl.partd_in[0].v[q];
+                for (int b = 1; b < C; b++) {
+                    tot[0] += ctl.partd_in[b].v[0];
+                    tot[1] += ctl.partd_in[b].v[1];
+                    tot[2] = fmax(tot[2], ctl.partd_in[b].v[2]);
+                    tot[3] += ctl.partd_in[b].v[3];
+                    tot[4] += ctl.partd_in[b].v[4];
+                }
+                ctl.req = ctl.partd_in[0].req;
+                res_verify_epilogue(e, s, tot, kind, primary);
+            }
             __syncthreads();
         } else {
             // ---- move (src/integrator/fire.cu:29-40)
@@ -570,9 +674,9 @@ __global__ void __launch_bounds__(NT) e_res(EDev *e, const int *sys_of_block, in
                     const bool uphill = s.uphill;
 #pragma unroll
                     for (int k = 0; k < PPT; k++) {
-                        const int l = t + k * NT;
+                        const int lo = t + k * NT, l = base + lo;
                         if (l >= n) break;
-                        const float4 a = L.pk[l], al = L.pkl[l];
+                        const float4 a = L.pk[lo], al = L.pkl[lo];
                         dw ox = {a.x, al.x}, oy = {a.y, al.y};
                         float2 v = u[k];
                         const float2 f = fr[k];
@@ -589,8 +693,8 @@ __global__ void __launch_bounds__(NT) e_res(EDev *e, const int *sys_of_block, in
                         u[k] = v;
                         ox = dw_add_f(ox, v.x * dt);
                         oy = dw_add_f(oy, v.y * dt);
-                        L.pk[l] = make_float4(ox.hi, oy.hi, a.z, a.w);
-                        L.pkl[l] = make_float4(ox.lo, oy.lo, al.z, al.w);
+                        L.pk[lo] = make_float4(ox.hi, oy.hi, a.z, a.w);
+                        L.pkl[lo] = make_float4(ox.lo, oy.lo, al.z, al.w);
                         const float ddx = ox.hi - orf[k].x, ddy = oy.hi - orf[k].y;
                         need |= (ddx * ddx + ddy * ddy > half_skin2_f);
                     }
@@ -599,11 +703,11 @@ __global__ void __launch_bounds__(NT) e_res(EDev *e, const int *sys_of_block, in
                     const bool from32 = s.vel_f32, stale = pstale;
 #pragma unroll
                     for (int k = 0; k < PPT; k++) {
-                        const int l = t + k * NT;
+                        const int lo = t + k * NT, l = base + lo;
                         if (l >= n) break;
                         const int i = off + l;
                         const double2 c = e->ctr[i];
-                        double2 x = stale ? res_position(L, c, l) : e->pos[i];
+                        double2 x = stale ? res_position(L, c, lo) : e->pos[i];
                         double2 v = from32 ? make_double2(u[k].x, u[k].y) : e->vel[i];
                         // the last pass was a double-word one: its force is in registers
                         const double2 f = from32 ? make_double2((double)fr[k].x + (double)frl[k].x,
@@ -623,32 +727,37 @@ __global__ void __launch_bounds__(NT) e_res(EDev *e, const int *sys_of_block, in
                         x.y = x.y + v.y * dt;
                         e->vel[i] = v;
                         e->pos[i] = x;
-                        const float4 a = L.pk[l];
-                        L.pk[l] = make_float4((float)(x.x - c.x), (float)(x.y - c.y), a.z, a.w);
-                        const double2 r = e->pos_ref[i];
-                        const double ddx = x.x - r.x, ddy = x.y - r.y;
+                        const float4 a = L.pk[lo];
+                        L.pk[lo] = make_float4((float)(x.x - c.x), (float)(x.y - c.y), a.z, a.w);
+                        const double2 rf = e->pos_ref[i];
+                        const double ddx = x.x - rf.x, ddy = x.y - rf.y;
                         need |= (ddx * ddx + ddy * ddy > p.half_skin2);
                     }
+                    if (C > 1) __threadfence();
                 }
                 pstale = s.prec != 1;
                 moved_rb = __syncthreads_or(need);
+                if (C > 1) {
+                    if (t == 0) res_bcast<C>(ctl.rb_in, r, moved_rb);
+                    res_csync<C>();
+                    moved_rb = 0;
+#pragma unroll
+                    for (int b = 0; b < C; b++) moved_rb |= ctl.rb_in[b];
+                }
                 if (t == 0 && s.prec == 1) s.vel_f32 = 0;
             }
 
-            // ---- cell list and neighbour list of this system
+            // ---- cell list (the whole system, in every block) and neighbour lists
             if (s.rebuild || moved_rb) {
                 const bool stale = pstale;
                 const int ncd = s.ncd, nc = ncd * ncd;
                 for (int c = t; c < nc; c += NT) L.ccur[c] = 0;
-                __syncthreads();
-                int gc[PPT];
 #pragma unroll
                 for (int k = 0; k < PPT; k++) {
-                    const int l = t + k * NT;
-                    gc[k] = 0;
+                    const int lo = t + k * NT, l = base + lo;
                     if (l >= n) break;
                     const int i = off + l;
-                    const double2 x = stale ? res_position(L, e->ctr[i], l) : e->pos[i];
+                    const double2 x = stale ? res_position(L, e->ctr[i], lo) : e->pos[i];
                     const double fx = floor(x.x * s.inv_cs), fy = floor(x.y * s.inv_cs);
                     const int cx = wrap_int((long long)fx, ncd), cy = wrap_int((long long)fy, ncd);
                     const int code = code_of(cx, cy);
@@ -659,22 +768,26 @@ __global__ void __launch_bounds__(NT) e_res(EDev *e, const int *sys_of_block, in
                     e->cellc[i] = code;
                     const double ox = x.x - c.x, oy = x.y - c.y;
                     const float hx = (float)ox, hy = (float)oy;
-                    const float4 a = L.pk[l], al = L.pkl[l];
-                    L.pk[l] = make_float4(hx, hy, a.z, __int_as_float(code));
-                    const float2 lo = split_lo(ox, oy, hx, hy);
-                    L.pkl[l] = make_float4(lo.x, lo.y, al.z, 0.f);
+                    const float4 a = L.pk[lo], al = L.pkl[lo];
+                    L.pk[lo] = make_float4(hx, hy, a.z, __int_as_float(code));
+                    const float2 lw = split_lo(ox, oy, hx, hy);
+                    L.pkl[lo] = make_float4(lw.x, lw.y, al.z, 0.f);
                     orf[k] = make_float2(hx, hy);
-                    gc[k] = cx + cy * ncd;
-                    atomicAdd(&L.ccur[gc[k]], 1);
+                }
+                if (C > 1) __threadfence();
+                res_csync<C>();
+                // count every particle of the system into its cell
+                for (int j = t; j < n; j += NT) {
+                    const int c = __float_as_int(res_pk_of<C, M>(L, j)->w);
+                    atomicAdd(&L.ccur[code_x(c) + code_y(c) * ncd], 1);
                 }
                 __syncthreads();
                 res_scan<NT>(L, nc, ctl.wsum, &ctl.carry);
                 __syncthreads();
-#pragma unroll
-                for (int k = 0; k < PPT; k++) {
-                    const int l = t + k * NT;
-                    if (l >= n) break;
-                    L.citem[L.cstart[gc[k]] + atomicAdd(&L.ccur[gc[k]], 1)] = (unsigned short)l;
+                for (int j = t; j < n; j += NT) {
+                    const int c = __float_as_int(res_pk_of<C, M>(L, j)->w);
+                    const int g = code_x(c) + code_y(c) * ncd;
+                    L.citem[L.cstart[g] + atomicAdd(&L.ccur[g], 1)] = (unsigned short)j;
                 }
                 __syncthreads();
                 // ascending particle order inside each cell: reproducible lists
@@ -691,9 +804,9 @@ __global__ void __launch_bounds__(NT) e_res(EDev *e, const int *sys_of_block, in
                 int mx = 0;
 #pragma unroll
                 for (int k = 0; k < PPT; k++) {
-                    const int l = t + k * NT;
+                    const int lo = t + k * NT, l = base + lo;
                     if (l >= n) break;
-                    mx = max(mx, res_nlist(e, s, L, l, off + l));
+                    mx = max(mx, res_nlist<C, M>(e, s, L, lo, l, off + l));
                 }
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_down_sync(0xffffffffu, mx, o));
@@ -701,6 +814,12 @@ __global__ void __launch_bounds__(NT) e_res(EDev *e, const int *sys_of_block, in
                 __syncthreads();
                 if (t == 0) {
                     for (int w = 1; w < NT / 32; w++) mx = max(mx, ctl.imax[w]);
+                    res_bcast<C>(ctl.mx_in, r, mx);
+                }
+                res_csync<C>();
+                if (t == 0) {
+                    mx = ctl.mx_in[0];
+                    for (int b = 1; b < C; b++) mx = max(mx, ctl.mx_in[b]);
                     s.resume = e_nlist_sys(e, s, mx) ? 0 : 1;
                 }
                 pstale = false;
@@ -711,7 +830,6 @@ __global__ void __launch_bounds__(NT) e_res(EDev *e, const int *sys_of_block, in
             // ---- force pass (+ kick unless setup) and the per-system epilogue
             {
                 const bool setup = s.phase == kSetup;
-                double tot[5];
                 if (s.prec != 1) {
                     dw pe = {0.f, 0.f};
                     float v[4] = {0.f, 0.f, 0.f, 0.f};  // power, max|F|^2, virial, contacts
@@ -721,7 +839,7 @@ __global__ void __launch_bounds__(NT) e_res(EDev *e, const int *sys_of_block, in
                     const bool short_dw = p.pe_diff_target <= 0.0;
 #pragma unroll
                     for (int k = 0; k < PPT; k++) {
-                        const int l = t + k * NT;
+                        const int lo = t + k * NT, l = base + lo;
                         if (l >= n) break;
                         const int i = off + l;
                         float2 f, flo;
@@ -729,19 +847,19 @@ __global__ void __launch_bounds__(NT) e_res(EDev *e, const int *sys_of_block, in
                         int ncount;
                         if (!dwp) {
                             float en;
-                            res_forces_f32(e, s, L, l, i, f.x, f.y, en, wv, ncount);
+                            res_forces_f32<C, M>(e, s, L, lo, i, f.x, f.y, en, wv, ncount);
                             flo = make_float2(0.f, 0.f);
                             pe = dw_add_f(pe, en);
                         } else if (short_dw) {
                             dw sx, sy;
                             float en;
-                            res_forces_dwf(e, s, L, l, i, sx, sy, en, wv, ncount);
+                            res_forces_dwf<C, M>(e, s, L, lo, i, sx, sy, en, wv, ncount);
                             f = make_float2(sx.hi, sy.hi);
                             flo = make_float2(sx.lo, sy.lo);
                             pe = dw_add_f(pe, en);
                         } else {
                             dw sx, sy, se;
-                            res_forces_dw(e, s, L, l, i, sx, sy, se, wv, ncount);
+                            res_forces_dw<C, M>(e, s, L, lo, i, sx, sy, se, wv, ncount);
                             f = make_float2(sx.hi, sy.hi);
                             flo = make_float2(sx.lo, sy.lo);
                             pe = dw_add(pe, se);
@@ -762,21 +880,39 @@ __global__ void __launch_bounds__(NT) e_res(EDev *e, const int *sys_of_block, in
                     }
                     res_reduce<NT>(pe, v, smw, smv);
                     if (t == 0) {
-                        tot[0] = (double)pe.hi + (double)pe.lo;
-                        tot[1] = v[0];
-                        tot[2] = v[1];
-                        tot[3] = v[2];
-                        tot[4] = v[3];
+                        RPart pp;
+                        pp.pe = pe;
+#pragma unroll
+                        for (int q = 0; q < 4; q++) pp.v[q] = v[q];
+                        pp.req = req;
+                        res_bcast<C>(ctl.part_in, r, pp);
+                    }
+                    res_csync<C>();
+                    if (t == 0) {
+                        dw tp = ctl.part_in[0].pe;
+                        float tv[4];
+#pragma unroll
+                        for (int q = 0; q < 4; q++) tv[q] = ctl.part_in[0].v[q];
+                        for (int b = 1; b < C; b++) {
+                            tp = dw_add(tp, ctl.part_in[b].pe);
+                            tv[0] += ctl.part_in[b].v[0];
+                            tv[1] = fmaxf(tv[1], ctl.part_in[b].v[1]);
+                            tv[2] += ctl.part_in[b].v[2];
+                            tv[3] += ctl.part_in[b].v[3];
+                        }
+                        ctl.req = ctl.part_in[0].req;
+                        const double tot[5] = {(double)tp.hi + (double)tp.lo, tv[0], tv[1], tv[2], tv[3]};
+                        e_force_epilogue(e, s, tot, setup, primary);
                     }
                 } else {
                     double a[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
 #pragma unroll
                     for (int k = 0; k < PPT; k++) {
-                        const int l = t + k * NT;
+                        const int lo = t + k * NT, l = base + lo;
                         if (l >= n) break;
                         const int i = off + l;
                         double ax, ay, en, wv, nc;
-                        res_forces_f64(e, s, L, l, i, ax, ay, en, wv, nc);
+                        res_forces_f64<C, M>(e, s, L, lo, i, ax, ay, en, wv, nc);
                         const double2 f = make_double2(ax, ay);
                         e->frc[i] = f;
                         fr[k] = make_float2((float)ax, (float)ay);
@@ -796,11 +932,29 @@ __global__ void __launch_bounds__(NT) e_res(EDev *e, const int *sys_of_block, in
                     }
                     const int ops[5] = {0, 0, 1, 0, 0};
                     block_reduce<5, double>(a, ops, smd);
-                    if (t == 0)
+                    if (t == 0) {
+                        RPartD pd;
 #pragma unroll
-                        for (int q = 0; q < 5; q++) tot[q] = a[q];
+                        for (int q = 0; q < 5; q++) pd.v[q] = a[q];
+                        pd.req = req;
+                        res_bcast<C>(ctl.partd_in, r, pd);
+                    }
+                    res_csync<C>();
+                    if (t == 0) {
+                        double tot[5];
+#pragma unroll
+                        for (int q = 0; q < 5; q++) tot[q] = ctl.partd_in[0].v[q];
+                        for (int b = 1; b < C; b++) {
+                            tot[0] += ctl.partd_in[b].v[0];
+                            tot[1] += ctl.partd_in[b].v[1];
+                            tot[2] = fmax(tot[2], ctl.partd_in[b].v[2]);
+                            tot[3] += ctl.partd_in[b].v[3];
+                            tot[4] += ctl.partd_in[b].v[4];
+                        }
+                        ctl.req = ctl.partd_in[0].req;
+                        e_force_epilogue(e, s, tot, setup, primary);
+                    }
                 }
-                if (t == 0) e_force_epilogue(e, s, tot, setup);
                 __syncthreads();
             }
         }
@@ -811,10 +965,10 @@ __global__ void __launch_bounds__(NT) e_res(EDev *e, const int *sys_of_block, in
             const bool stale = pstale;
 #pragma unroll
             for (int k = 0; k < PPT; k++) {
-                const int l = t + k * NT;
+                const int lo = t + k * NT, l = base + lo;
                 if (l >= n) break;
                 const int i = off + l;
-                double2 x = stale ? res_position(L, e->ctr[i], l) : e->pos[i];
+                double2 x = stale ? res_position(L, e->ctr[i], lo) : e->pos[i];
                 if (act == kActCompress && s.pressure < p.p_low && s.jam_stage == 1 && s.L_saved == s.L)
                     e->pos_save[i] = x;  // write_restart_file("last_state")
                 if (act == kActRevertScale) x = e->pos_save[i];  // load("last_state")
@@ -832,28 +986,30 @@ __global__ void __launch_bounds__(NT) e_res(EDev *e, const int *sys_of_block, in
         it++;
     }
 
-    // ---- write back (exact double-word offsets, registers, FP64 positions)
-    __syncthreads();
+    // ---- write back own particles (exact double-word offsets, registers, FP64
+    // positions); block 0 writes the system state
     const bool stale = pstale;
     const bool f64_last = s.prec == 1;
 #pragma unroll
     for (int k = 0; k < PPT; k++) {
-        const int l = t + k * NT;
+        const int lo = t + k * NT, l = base + lo;
         if (l >= n) break;
         const int i = off + l;
-        if (stale) e->pos[i] = res_position(L, e->ctr[i], l);
-        e->pk[i] = L.pk[l];
-        e->pkl[i] = L.pkl[l];
+        if (stale) e->pos[i] = res_position(L, e->ctr[i], lo);
+        e->pk[i] = L.pk[lo];
+        e->pkl[i] = L.pkl[lo];
         e->vel32[i] = u[k];
         e->frc32[i] = fr[k];
         e->oref[i] = orf[k];
         if (!f64_last)
             e->frc[i] = make_double2((double)fr[k].x + (double)frl[k].x, (double)fr[k].y + (double)frl[k].y);
     }
-    if (t == 0) {
+    if (t == 0 && primary) {
         s.res_valid = 1;
         e->sys[sid] = s;
     }
+    // no block leaves while another may still read its shared memory
+    res_csync<C>();
 }
 
 }  // namespace
