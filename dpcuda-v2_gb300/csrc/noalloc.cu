@@ -1,22 +1,26 @@
 // noalloc.cu -- disk forces and energies from positions and radii without any
 // device allocation.
 //
-// Some callers cannot call cudaMalloc: code running while a CUDA graph is
-// being captured, allocators with a fixed device budget (an embedding
-// application that hands out all memory up front), or real-time loops that
-// must not take the allocator's locks.  For them this file offers one entry
-// point, dpg_disk_forces_noalloc, that computes the same harmonic forces as
-// dpg_setup_neighbors + dpg_compute_forces but keeps its cell-list scratch in
-// the file-scope array below, sized for at most kMaxParticles particles and
-// kMaxCells cells.  Every GPU that loads the library holds that array (about
-// 1 MiB) until the process exits.
+// Some callers cannot call cudaMalloc: an application that hands all device
+// memory to its own fixed pool up front has none left for a library to take,
+// and a real-time loop cannot afford the allocator's locks and the device
+// synchronisation that cudaMalloc and cudaFree may imply.  For them this file
+// offers one entry point, dpg_disk_forces_noalloc, that computes the same
+// harmonic forces as dpg_setup_neighbors + dpg_compute_forces but keeps its
+// cell-list scratch in the file-scope array below, sized for at most
+// kMaxParticles particles and kMaxCells cells.  Every GPU that loads the
+// library holds that array (about 1 MiB) until the process exits.
 //
 // Host code must not pass the array's name to a kernel (in host code it is a
 // host-side stand-in, not a device address); the device address is looked up
-// once per device with cudaGetSymbolAddress, on that device's first call.
-// Make that first call before any stream capture.  All calls share the one
-// array, so calls whose kernels overlap on the GPU (two streams at once) race;
-// serialise them.  Each call clears the counters it needs before use.
+// with cudaGetSymbolAddress, with the device current, on a device's first
+// call, and again whenever the device's context has changed since (after
+// cudaDeviceReset the module is loaded anew and the array may move).  Make the
+// first call on each device before any stream capture.  All calls share the
+// one array, so calls whose kernels overlap on the GPU (two streams at once)
+// race; serialise them.  Each call clears the counters it needs before use.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -139,19 +143,48 @@ __global__ void na_force(NaArgs a) {
 
 std::mutex g_lock;
 int *g_scratch_addr[kMaxDevices] = {nullptr};
+unsigned long long g_scratch_ctx[kMaxDevices] = {0};  // context the address belongs to
 
-// device address of the scratch array on the current device, looked up once
+// Unique id of the calling thread's current context (driver entry points
+// fetched through the runtime, so the library needs no link to libcuda);
+// 0 when there is none or it cannot be read.
+unsigned long long current_context_id() {
+    static PFN_cuCtxGetCurrent_v4000 get_current = nullptr;
+    static PFN_cuCtxGetId_v12000 get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 4000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = (PFN_cuCtxGetCurrent_v4000)f;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = (PFN_cuCtxGetId_v12000)f;
+    });
+    CUcontext c = nullptr;
+    unsigned long long id = 0;
+    if (!get_current || !get_id || get_current(&c) != CUDA_SUCCESS || !c) return 0;
+    if (get_id(c, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
+
+// Device address of the scratch array on the current device: looked up on the
+// device's first call and again when its context changed (a reset reloads the
+// module); the lookup itself makes the device's context current.
 int scratch_for_current_device(int **out) {
     int dev = 0;
     DPG_CK(cudaGetDevice(&dev));
     if (dev < 0 || dev >= kMaxDevices) return dpg::set_error(DPG_ERR_ARG, "device index out of range");
     std::lock_guard<std::mutex> g(g_lock);
-    if (!g_scratch_addr[dev]) {
+    const unsigned long long ctx = current_context_id();
+    if (!g_scratch_addr[dev] || ctx == 0 || ctx != g_scratch_ctx[dev]) {
         void *p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess)
             return dpg::set_error(DPG_ERR_CUDA, "cudaGetSymbolAddress(scratch): %s", cudaGetErrorString(e));
         g_scratch_addr[dev] = (int *)p;
+        g_scratch_ctx[dev] = current_context_id();
     }
     *out = g_scratch_addr[dev];
     return DPG_OK;
@@ -192,11 +225,13 @@ extern "C" int dpg_disk_forces_noalloc(const double *x, const double *y, const d
     a.cell = a.items + kMaxParticles;
     cudaStream_t st = (cudaStream_t)cuda_stream;
     const int nb = (int)((n + 255) / 256), cb = (int)((ncd * ncd + 1 + 255) / 256);
-    na_clear<<<cb, 256, 0, st>>>(a);
-    na_count<<<nb, 256, 0, st>>>(a);
-    na_scan<<<1, 1024, 0, st>>>(a);
-    na_fill<<<nb, 256, 0, st>>>(a);
-    na_sort<<<cb, 256, 0, st>>>(a);
+    if (ncd >= 3) {  // the all-pairs case (fewer than 3 cells a side) needs no cell list
+        na_clear<<<cb, 256, 0, st>>>(a);
+        na_count<<<nb, 256, 0, st>>>(a);
+        na_scan<<<1, 1024, 0, st>>>(a);
+        na_fill<<<nb, 256, 0, st>>>(a);
+        na_sort<<<cb, 256, 0, st>>>(a);
+    }
     na_force<<<nb, 256, 0, st>>>(a);
     DPG_CK(cudaGetLastError());
     return DPG_OK;

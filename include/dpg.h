@@ -618,16 +618,18 @@ int dpg_ensemble_profile_loop(dpg_ensemble e, const dpg_fire_params *p, int iter
 /* No counterpart in the reference.  Harmonic forces fx, fy and per-particle
  * energies pe of n disks (device arrays, any order, square box of side
  * box_x == box_y), the same values as dpg_setup_neighbors + dpg_compute_forces
- * up to summation order, for callers that cannot call cudaMalloc while they
- * run (inside a stream capture, under a host's fixed device-memory pool, in a
- * real-time loop).  The cell list lives in one fixed array inside the library
- * (about 1 MiB on every GPU that loads it, held until exit), so n is at most
- * 65536 and box_x / max_diameter below 257; larger inputs return
- * DPG_ERR_ARG.  max_diameter must be at least the largest 2 * radius.  The
- * first call on a device looks the array's address up and should come before
- * any stream capture.  Calls share the array: calls that overlap on the GPU
- * race, so serialise them on one stream.  Work is queued on cuda_stream
- * (NULL = legacy default stream); the function does not synchronise. */
+ * up to summation order, for callers that cannot call cudaMalloc: hosts that
+ * give all device memory to their own fixed pool up front, and real-time
+ * loops that cannot wait on the allocator's locks and synchronisation.  The
+ * cell list lives in one fixed array inside the library (about 1 MiB on every
+ * GPU that loads it, held until exit), so n is at most 65536 and
+ * box_x / max_diameter below 257; larger inputs return DPG_ERR_ARG.
+ * max_diameter must be at least the largest 2 * radius.  The first call on a
+ * device (and the first after its context was reset) looks the array's
+ * address up; make that first call before any stream capture.  Calls share
+ * the array: calls that overlap on the GPU race, so serialise them on one
+ * stream.  Work is queued on cuda_stream (NULL = legacy default stream); the
+ * function does not synchronise. */
 int dpg_disk_forces_noalloc(const double *x, const double *y, const double *radii, int64_t n,
                             double box_x, double box_y, double e_c, double n_c,
                             double max_diameter, double *fx, double *fy, double *pe,

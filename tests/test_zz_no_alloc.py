@@ -1,16 +1,18 @@
 """GPU: dpg_disk_forces_noalloc, the one entry point that allocates no device
-memory, against the allocating path (dpg_setup_neighbors + dpg_compute_forces).
+memory, against the allocating path (dpg_setup_neighbors + dpg_compute_forces)
+and against the CPU oracle of the reference's force kernel.
 
-It exists for callers that cannot call cudaMalloc while they run: code inside a
-CUDA stream capture, hosts that hand all device memory to their own fixed pool,
-and real-time loops that must not block on the allocator.  Its cell-list
-scratch is a fixed array inside the library that every call shares, so the
-test makes several calls in a row with different sizes: a call that found the
-previous call's counters still in place would give wrong forces.
+It exists for callers that cannot call cudaMalloc: hosts that hand all device
+memory to their own fixed pool up front, and real-time loops that cannot wait
+on the allocator.  Its cell-list scratch is a fixed array inside the library
+that every call shares, so the test makes several calls in a row with
+different sizes: a call that found the previous call's counters still in place
+would give wrong forces.
 
-Summation order over a particle's contacts differs between the two paths
-(cell stencil order here, neighbour-list order there), so forces and energies
-agree to 1e-12 of the largest value rather than bit for bit.
+Summation order over a particle's contacts differs between the paths (cell
+stencil order here, neighbour-list order in the library and the oracle), so
+forces and energies agree to 1e-12 of the largest value rather than bit for
+bit.
 """
 import ctypes as C
 
@@ -46,6 +48,18 @@ def allocating_path(dpg, x, y, r, box):
     return st["fx"], st["fy"], st["pe"]
 
 
+def oracle_path(x, y, r, box):
+    from oracle.oracle import DiskOracle
+    o = DiskOracle(len(x), box)
+    o.set_arrays(x=x, y=y, r=r, m=np.ones_like(r))
+    o.setup_neighbors(0, 1.5, 0.2, 8.0, 0.5)
+    o.zero_force_and_pe()
+    o.calculate_forces()
+    a = o.get_arrays()
+    o.close()
+    return a["fx"], a["fy"], a["pe"]
+
+
 def noalloc_path(lib, torch, x, y, r, box):
     dev = torch.device("cuda:0")
     tx, ty, tr = (torch.as_tensor(a, dtype=torch.float64, device=dev) for a in (x, y, r))
@@ -75,11 +89,14 @@ def test_noalloc_matches_allocating_path_on_calls_in_a_row(env):
     for n, phi, seed in [(4096, 0.86, 11), (16, 0.8, 12), (4096, 0.86, 11), (20000, 0.9, 13)]:
         x, y, r, box = packing(n, phi, seed)
         want = allocating_path(dpg, x, y, r, box)
+        oracle = oracle_path(x, y, r, box)
         got = noalloc_path(lib, torch, x, y, r, box)
-        for name, g, w in zip(("fx", "fy", "pe"), got, want):
-            assert np.all(np.isfinite(g)), name
-            scale = max(np.abs(w).max(), 1e-300)
-            np.testing.assert_allclose(g, w, rtol=0, atol=TOL * scale, err_msg=f"{name} n={n}")
+        for ref_name, ref in (("allocating path", want), ("oracle", oracle)):
+            for name, g, w in zip(("fx", "fy", "pe"), got, ref):
+                assert np.all(np.isfinite(g)), name
+                scale = max(np.abs(w).max(), 1e-300)
+                np.testing.assert_allclose(g, w, rtol=0, atol=TOL * scale,
+                                           err_msg=f"{name} n={n} against the {ref_name}")
         assert np.abs(want[0]).max() > 0  # the packing has contacts
 
 
