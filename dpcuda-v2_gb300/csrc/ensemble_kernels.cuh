@@ -76,6 +76,7 @@ struct ESys {
                              // current positions, 1 = check max|F| (back to double words if
                              // it fails), 2 = final measurement of a finished minimisation
     double dw_scale;         // resident form: double-word exit at dw_scale * fmax_target
+    double inv_n;            // 1 / n (the epilogue multiplies; FP64 division is slow)
 };
 
 struct EParams {
@@ -660,7 +661,10 @@ __device__ void e_force_epilogue(EDev *e, ESys &s, const double (&v)[5], bool se
     s.fmax2 = v[2];
     s.virial = v[3];
     s.contacts = v[4];
-    double avg = s.pe / (double)s.n;
+    // no FP64 division or square root on this per-iteration path (both are long
+    // instruction sequences on GB300's FP64 pipe): averages by 1/n, max|F|
+    // tests on squares, relative energy changes by cross-multiplication
+    const double avg = s.pe * s.inv_n;
     s.fire_total++;
     if (s.prec == 1) s.fp64_total++;
     else if (s.prec == 2) s.dw_total++;
@@ -674,7 +678,7 @@ __device__ void e_force_epilogue(EDev *e, ESys &s, const double (&v)[5], bool se
         e_fire_decide(p, s, s.power);
         return;
     }
-    double fmax = sqrt(s.fmax2);
+    const double f2 = s.fmax2;
     const int pass_prec = s.prec;  // the arithmetic of this force pass
     // mixed systems hand over to the refinement at switch_fmax, when FIRE
     // keeps going uphill, or when max|F| stalls near the threshold: first to
@@ -692,18 +696,19 @@ __device__ void e_force_epilogue(EDev *e, ESys &s, const double (&v)[5], bool se
         // check: its noise floor, ~1e-14 of the contact force, is far below any
         // plateau of FIRE near jamming, and uphill runs there are FIRE's own)
         const bool dw_res = p.res && s.prec == 2;
-        const bool stalled = !dw_res && fmax < 100.0 * exit_f && s.iter - s.best_it > kStallIters;
+        const bool stalled = !dw_res && f2 < 1e4 * exit_f * exit_f && s.iter - s.best_it > kStallIters;
         // a PE-change stop (pe_diff_target > 0) is only decided in FP64: once
         // the double-word energy has stopped changing at its own precision
         // (1e-12 relative), hand over so the FP64 test can fire
         const bool pe_flat = s.prec == 2 && p.pe_diff_target > 0 &&
-                             fabs(s.pe / (double)s.n / s.last_avg_pe - 1) < 1e-12;
-        if (fmax <= exit_f || (s.nbad > 5 && !dw_res) || stalled || pe_flat) {
+                             fabs(avg - s.last_avg_pe) < 1e-12 * s.last_avg_pe;
+        const bool at_exit = f2 <= exit_f * exit_f;
+        if (at_exit || (s.nbad > 5 && !dw_res) || stalled || pe_flat) {
             if (s.prec == 0 && p.dw_ok) {
                 s.prec = 2;
                 s.best_f2 = s.fmax2;
                 s.best_it = s.iter;
-            } else if (p.res && s.prec == 2 && fmax <= exit_f && p.fmax_target > 0 && !pe_flat) {
+            } else if (p.res && s.prec == 2 && at_exit && p.fmax_target > 0 && !pe_flat) {
                 s.verify = 1;  // resident form: an FP64 pass checks this state next
             } else {
                 s.prec = 1;
@@ -711,14 +716,15 @@ __device__ void e_force_epilogue(EDev *e, ESys &s, const double (&v)[5], bool se
             }
         }
     }
-    double diff = fabs(avg / s.last_avg_pe - 1);
-    s.last_avg_pe = avg;
-    long long it = s.iter;
+    const long long it = s.iter;
     const bool decompressing = p.jam && s.jam_stage == 0;
     const double pe_t = decompressing ? 1e-16 : p.pe_target;
     const double pe_dt = decompressing ? 0.0 : p.pe_diff_target;
-    if (avg < pe_t || (pass_prec == 1 && diff < pe_dt)) finished = true;
-    else if (p.fmax_target > 0 && fmax <= p.fmax_target && pass_prec == 1) finished = true;
+    // |avg / last - 1| < pe_dt, for last >= 0
+    const bool pe_still = pe_dt > 0 && fabs(avg - s.last_avg_pe) < pe_dt * s.last_avg_pe;
+    s.last_avg_pe = avg;
+    if (avg < pe_t || (pass_prec == 1 && pe_still)) finished = true;
+    else if (p.fmax_target > 0 && f2 <= p.fmax_target * p.fmax_target && pass_prec == 1) finished = true;
     else if (it + 1 >= p.max_steps) finished = true;
     else {
         s.iter = it + 1;

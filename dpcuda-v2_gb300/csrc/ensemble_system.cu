@@ -42,8 +42,8 @@ struct dpg_ensemble_system {
     int form = DPG_FORM_AUTO, pthreads = 0;  // execution form and persistent block size
     int max_n = 0;
     // resident form: one stream per size class, the block -> system lists
-    cudaStream_t rs_stream[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
-    cudaEvent_t rs_fork = nullptr, rs_join[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    cudaStream_t rs_stream[8] = {};
+    cudaEvent_t rs_fork = nullptr, rs_join[8] = {};
     int *d_rs_blocks = nullptr;
 };
 
@@ -65,7 +65,7 @@ static int ealloc(ES *s, void **p, size_t bytes) {
 extern "C" int dpg_ensemble_destroy(dpg_ensemble s) {
     if (!s) return DPG_OK;
     if (s->stream) cudaStreamSynchronize(s->stream);
-    for (int c = 0; c < 5; c++) {
+    for (int c = 0; c < 8; c++) {
         if (s->rs_stream[c]) cudaStreamDestroy(s->rs_stream[c]);
         if (s->rs_join[c]) cudaEventDestroy(s->rs_join[c]);
     }
@@ -117,6 +117,7 @@ extern "C" int dpg_ensemble_create(const dpg_ensemble_params *p, const int64_t *
         ESys &y = s->sys[k];
         y.off = slot;
         y.n = (int)n_particles[k];
+        y.inv_n = 1.0 / (double)y.n;
         y.blk0 = blk;
         y.nblk = (y.n + kEB - 1) / kEB;
         y.L = box[k];
@@ -382,17 +383,38 @@ static int run(ES *s, long long guard_limit) {
 }
 
 // ---- the resident form --------------------------------------------------------
-// Size classes (threads per block x particles per thread x blocks per
-// cluster): a system goes to the first class that holds it.
+typedef void (*res_kernel_fn)(EDev *, const int *, int, long long, unsigned long long);
+// Size classes (threads per block, particles per lane group, blocks per
+// cluster, lanes per particle): a system goes to the first class that holds it.
 struct RClass {
-    int nt, ppt, c;
-    int per_block() const { return nt * ppt; }
-    int capacity() const { return nt * ppt * c; }
+    int nt, ppt, c, g;
+    res_kernel_fn fn;
+    int per_block() const { return nt / g * ppt; }
+    int capacity() const { return nt / g * ppt * c; }
 };
-static const RClass kRClasses[5] = {{64, 4, 1}, {128, 4, 1}, {256, 4, 1}, {256, 4, 2}, {256, 4, 4}};
+constexpr int kNClass = 7;
+#define RC(NT, PPT, C, G) {NT, PPT, C, G, e_res<NT, PPT, C, G>}
+static const RClass kRTables[3][kNClass] = {
+    {RC(64, 4, 1, 1), RC(128, 4, 1, 1), RC(256, 4, 1, 1), RC(256, 4, 2, 1), RC(256, 4, 4, 1),
+     RC(256, 4, 4, 1), RC(256, 4, 4, 1)},
+    {RC(256, 1, 1, 4), RC(256, 1, 1, 2), RC(256, 1, 1, 1), RC(512, 1, 1, 1), RC(512, 1, 2, 1),
+     RC(512, 1, 4, 1), RC(512, 1, 8, 1)},
+    {RC(128, 1, 1, 2), RC(128, 1, 1, 1), RC(128, 2, 1, 1), RC(256, 2, 1, 1), RC(256, 2, 2, 1),
+     RC(256, 2, 4, 1), RC(256, 2, 8, 1)},
+};
+#undef RC
+static const RClass *res_table() {
+    static const RClass *t = nullptr;
+    if (!t) {
+        const char *tb = getenv("DPG_RES_TABLE");
+        t = kRTables[(tb && tb[0] >= '0' && tb[0] <= '2') ? tb[0] - '0' : 0];
+    }
+    return t;
+}
+#define kRClasses res_table()
 
 static int res_class_of(int n) {
-    for (int c = 0; c < 5; c++)
+    for (int c = 0; c < kNClass; c++)
         if (n <= kRClasses[c].capacity()) return c;
     return -1;
 }
@@ -416,37 +438,27 @@ static int res_smem_limit() {
 static bool res_fits(const ES *s) {
     if (s->max_n > kResMaxN) return false;
     const size_t lim = (size_t)res_smem_limit();
-    for (int c = 0; c < 5; c++) {
+    for (int c = 0; c < kNClass; c++) {
         const size_t b = res_smem_bytes(kRClasses[c].per_block(), kRClasses[c].capacity(), res_ncmax(s, c));
         if (b + 4096 > lim) return false;  // room for the kernel's static shared memory
     }
     return true;
 }
 
-typedef void (*res_kernel_t)(EDev *, const int *, int, long long, unsigned long long);
-static res_kernel_t res_kernel(int c) {
-    switch (c) {
-    case 0: return e_res<64, 4, 1>;
-    case 1: return e_res<128, 4, 1>;
-    case 2: return e_res<256, 4, 1>;
-    case 3: return e_res<256, 4, 2>;
-    default: return e_res<256, 4, 4>;
-    }
-}
 
 // Launch every class that has live systems, each on its own stream (forked
 // from and joined back into the ensemble's stream).  slice_ns bounds a launch.
 static int launch_resident(ES *s, long long budget, unsigned long long slice_ns, int *launched) {
     *launched = 0;
-    std::vector<int> order[5];
+    std::vector<int> order[kNClass];
     for (int k = 0; k < s->S; k++) {
         const ESys &y = s->sys[k];
         if (y.phase == kIdle) continue;
         order[res_class_of(y.n)].push_back(k);
     }
     std::vector<int> flat;
-    int first[5];
-    for (int c = 0; c < 5; c++) {
+    int first[kNClass];
+    for (int c = 0; c < kNClass; c++) {
         // largest systems first: they start before the small ones fill the SMs
         std::sort(order[c].begin(), order[c].end(), [&](int a, int b) {
             return s->sys[a].n != s->sys[b].n ? s->sys[a].n > s->sys[b].n : a < b;
@@ -458,7 +470,7 @@ static int launch_resident(ES *s, long long budget, unsigned long long slice_ns,
     CK(cudaMemcpyAsync(s->d_rs_blocks, flat.data(), 4 * flat.size(), cudaMemcpyHostToDevice, s->stream));
     if (!s->rs_fork) CK(cudaEventCreateWithFlags(&s->rs_fork, cudaEventDisableTiming));
     CK(cudaEventRecord(s->rs_fork, s->stream));
-    for (int c = 0; c < 5; c++) {
+    for (int c = 0; c < kNClass; c++) {
         const int nb = (int)order[c].size();
         if (!nb) continue;
         if (!s->rs_stream[c]) {
@@ -468,7 +480,7 @@ static int launch_resident(ES *s, long long budget, unsigned long long slice_ns,
         const RClass &K = kRClasses[c];
         const int ncmax = res_ncmax(s, c);
         const size_t smem = res_smem_bytes(K.per_block(), K.capacity(), ncmax);
-        res_kernel_t kern = res_kernel(c);
+        res_kernel_fn kern = K.fn;
         CK(cudaFuncSetAttribute((const void *)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         CK(cudaStreamWaitEvent(s->rs_stream[c], s->rs_fork, 0));
         // one cluster of K.c blocks per system

@@ -177,7 +177,7 @@ __device__ __forceinline__ void res_dcell(int ca, int cb, int ncd, int &dcx, int
 
 // ---- FP32 pair terms of own particle lo (slot i) from the shared offsets -------
 // (neighbour lists are written by the running launch: plain, coherent loads)
-template <int C, int M>
+template <int C, int M, int G>
 __device__ __forceinline__ void res_forces_f32(const EDev *e, const ESys &s, const RLayout &L, int lo,
                                                int i, float &ax, float &ay, float &en, float &wv,
                                                int &ncount) {
@@ -185,13 +185,14 @@ __device__ __forceinline__ void res_forces_f32(const EDev *e, const ESys &s, con
     const float ecf = (float)e->p.e_c, ncf = (float)e->p.n_c;
     const float4 a = L.pk[lo];
     ax = 0.f; ay = 0.f; en = 0.f; wv = 0.f; ncount = 0;
-    for (int k0 = 0; k0 < cnt; k0 += 8) {
+    const int g = threadIdx.x % G;
+    for (int k0 = g; k0 < cnt; k0 += 8 * G) {
         int jj[8];
 #pragma unroll
-        for (int u = 0; u < 8; u++) jj[u] = k0 + u < cnt ? e->nbr[(size_t)(k0 + u) * T + i] - off : 0;
+        for (int u = 0; u < 8; u++) jj[u] = k0 + u * G < cnt ? e->nbr[(size_t)(k0 + u * G) * T + i] - off : 0;
 #pragma unroll
         for (int u = 0; u < 8; u++) {
-            if (k0 + u >= cnt) break;
+            if (k0 + u * G >= cnt) break;
             float fx, fy, ef, wf;
             int ct;
             pair_f32(a, *res_pk_of<C, M>(L, jj[u]), s.ncd, s.cs_f, ecf, ncf, fx, fy, ef, wf, ct);
@@ -208,7 +209,7 @@ __device__ __forceinline__ void res_forces_f32(const EDev *e, const ESys &s, con
 // Pairs the hi offsets rule out (a 1e-4 relative margin on the contact
 // distance) are skipped; the rest run in double-word arithmetic.  The energy is
 // a double word (the energy-change stop test needs it).
-template <int C, int M>
+template <int C, int M, int G>
 __device__ __forceinline__ void res_forces_dw(const EDev *e, const ESys &s, const RLayout &L, int lo,
                                               int i, dw &sx, dw &sy, dw &se, float &sw, int &ncount) {
     const int T = e->p.T, cnt = min(e->cnt[i], e->p.cap), off = s.off;
@@ -217,13 +218,14 @@ __device__ __forceinline__ void res_forces_dw(const EDev *e, const ESys &s, cons
     const dw csd = {s.cs_f, s.cs_lo}, ec = {e->p.ec_hi, e->p.ec_lo};
     const int ca = __float_as_int(a.w), ncd = s.ncd;
     sx = {0.f, 0.f}; sy = {0.f, 0.f}; se = {0.f, 0.f}; sw = 0.f; ncount = 0;
-    for (int k0 = 0; k0 < cnt; k0 += 4) {
+    const int g = threadIdx.x % G;
+    for (int k0 = g; k0 < cnt; k0 += 4 * G) {
         int jj[4];
 #pragma unroll
-        for (int u = 0; u < 4; u++) jj[u] = k0 + u < cnt ? e->nbr[(size_t)(k0 + u) * T + i] - off : 0;
+        for (int u = 0; u < 4; u++) jj[u] = k0 + u * G < cnt ? e->nbr[(size_t)(k0 + u * G) * T + i] - off : 0;
 #pragma unroll
         for (int u = 0; u < 4; u++) {
-            if (k0 + u >= cnt) break;
+            if (k0 + u * G >= cnt) break;
             const float4 b = *res_pk_of<C, M>(L, jj[u]);
             int dcx, dcy;
             res_dcell(ca, __float_as_int(b.w), ncd, dcx, dcy);
@@ -259,7 +261,7 @@ __device__ __forceinline__ void res_forces_dw(const EDev *e, const ESys &s, cons
 // step).  Forces are accumulated with compensated sums; the energy
 // e_c / 4 ((sigma^2 - d^2) / (sigma (sigma + d)))^2 and the virial in FP32
 // (relative 1e-7; the energy-change stop test uses the full double-word path).
-template <int C, int M>
+template <int C, int M, int G>
 __device__ __forceinline__ void res_forces_dwf(const EDev *e, const ESys &s, const RLayout &L, int lo,
                                                int i, dw &sx, dw &sy, float &se, float &sw,
                                                int &ncount) {
@@ -269,13 +271,14 @@ __device__ __forceinline__ void res_forces_dwf(const EDev *e, const ESys &s, con
     const int ca = __float_as_int(a.w), ncd = s.ncd;
     float fxh = 0.f, fxl = 0.f, fyh = 0.f, fyl = 0.f;
     se = 0.f; sw = 0.f; ncount = 0;
-    for (int k0 = 0; k0 < cnt; k0 += 4) {
+    const int g = threadIdx.x % G;
+    for (int k0 = g; k0 < cnt; k0 += 4 * G) {
         int jj[4];
 #pragma unroll
-        for (int u = 0; u < 4; u++) jj[u] = k0 + u < cnt ? e->nbr[(size_t)(k0 + u) * T + i] - off : 0;
+        for (int u = 0; u < 4; u++) jj[u] = k0 + u * G < cnt ? e->nbr[(size_t)(k0 + u * G) * T + i] - off : 0;
 #pragma unroll
         for (int u = 0; u < 4; u++) {
-            if (k0 + u >= cnt) break;
+            if (k0 + u * G >= cnt) break;
             const float4 b = *res_pk_of<C, M>(L, jj[u]);
             int dcx, dcy;
             res_dcell(ca, __float_as_int(b.w), ncd, dcx, dcy);
@@ -338,7 +341,7 @@ __device__ __forceinline__ void res_forces_dwf(const EDev *e, const ESys &s, con
 // ---- FP64 pair terms of own particle lo (the reference arithmetic on FP64
 // positions; 1/d and 1/rs by Newton steps as in the grid form).  Neighbour
 // positions may have been written by another block of the cluster: L2 loads.
-template <int C, int M>
+template <int C, int M, int G>
 __device__ __forceinline__ void res_forces_f64(const EDev *e, const ESys &s, const RLayout &L, int lo,
                                                int i, double &ax, double &ay, double &en, double &wv,
                                                double &nc) {
@@ -348,7 +351,7 @@ __device__ __forceinline__ void res_forces_f64(const EDev *e, const ESys &s, con
     const double2 xi = e->pos[i];
     const double ri = e->rad[i];
     ax = 0.0; ay = 0.0; en = 0.0; wv = 0.0; nc = 0.0;
-    for (int k = 0; k < cnt; k++) {
+    for (int k = threadIdx.x % G; k < cnt; k += G) {
         const int j = e->nbr[(size_t)k * T + i];
         if (ncd >= 3) {
             const float4 b = *res_pk_of<C, M>(L, j - off);
@@ -472,9 +475,9 @@ __device__ void res_verify_epilogue(EDev *e, ESys &s, const double (&v)[5], int 
     s.verify = 0;
     s.fire_total++;
     s.fp64_total++;
-    const double avg = v[0] / (double)s.n, fmax = sqrt(v[2]);
+    const double avg = v[0] * s.inv_n;
     const double pe_t = (p.jam && s.jam_stage == 0) ? 1e-16 : p.pe_target;
-    if (kind == 2 || avg < pe_t || (p.fmax_target > 0 && fmax <= p.fmax_target)) {
+    if (kind == 2 || avg < pe_t || (p.fmax_target > 0 && v[2] <= p.fmax_target * p.fmax_target)) {
         s.pe = v[0];
         s.power = v[1];
         s.fmax2 = v[2];
@@ -528,11 +531,34 @@ __device__ __forceinline__ void res_bcast(Tv *field, int r, const Tv &x) {
     }
 }
 
+// sum over the G lanes of a particle (xor butterfly; every lane gets the same
+// bits: TwoSum-based double-word addition is commutative)
+template <int G>
+__device__ __forceinline__ dw lanes_dw(dw a) {
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) {
+        const dw b = {__shfl_xor_sync(0xffffffffu, a.hi, o), __shfl_xor_sync(0xffffffffu, a.lo, o)};
+        a = dw_add(a, b);
+    }
+    return a;
+}
+template <int G, typename Tv>
+__device__ __forceinline__ Tv lanes_sum(Tv a) {
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    return a;
+}
+
 // The resident kernel: one system per cluster of C blocks (C = 1: one block).
+// Thread t is lane t % G of particle group t / G; a group owns particles
+// q, q + NT / G, ... (PPT of them) and its G lanes share each particle's
+// neighbour loop (slots g, g + G, ...), the lane sums meeting by shuffles; the
+// group's lane 0 keeps the particle's velocity, force and last-build offset in
+// registers and does the per-particle work of the move and the list build.
 // sys_of_cluster[b]: the system of cluster b (one class); ncmax (cells) sizes
 // the dynamic shared memory; iter_budget: most iterations per system in this
 // launch; slice_ns: the launch's time slice (0 = none).
-template <int NT, int PPT, int C>
+template <int NT, int PPT, int C, int G>
 __global__ void __launch_bounds__(NT) e_res(EDev *e, const int *sys_of_cluster, int ncmax,
                                           long long iter_budget, unsigned long long slice_ns) {
     extern __shared__ float4 res_smem[];
@@ -541,9 +567,11 @@ __global__ void __launch_bounds__(NT) e_res(EDev *e, const int *sys_of_cluster, 
     __shared__ dw smw[NT / 32];
     __shared__ float smv[NT / 32 * 4];
     __shared__ double smd[32 * 5];
-    constexpr int M = NT * PPT;
+    constexpr int NG = NT / G;     // particle groups per block
+    constexpr int M = NG * PPT;    // particles per block
     const RLayout L = res_layout(res_smem, M, ncmax);
-    const int t = threadIdx.x;
+    const int t = threadIdx.x, q = t / G;
+    const bool lead = (t % G) == 0;
     const int r = C == 1 ? 0 : (int)cooperative_groups::this_cluster().block_rank();
     const bool primary = r == 0;
     const int sid = sys_of_cluster[blockIdx.x / C];
@@ -557,15 +585,15 @@ __global__ void __launch_bounds__(NT) e_res(EDev *e, const int *sys_of_cluster, 
     const EParams &p = e->p;
     const int n = s.n, off = s.off, base = r * M;
 
-    // ---- load own particles: offsets (exact double words, or split from the FP64
-    // positions), velocity, force, last-build offsets
+    // ---- load own particles (lead lanes): offsets (exact double words, or split
+    // from the FP64 positions), velocity, force, last-build offsets
     float2 u[PPT], fr[PPT], frl[PPT], orf[PPT];
     float im[PPT];
 #pragma unroll
     for (int k = 0; k < PPT; k++) {
-        const int lo = t + k * NT, l = base + lo;
+        const int lo = q + k * NG, l = base + lo;
         u[k] = make_float2(0.f, 0.f); fr[k] = u[k]; frl[k] = u[k]; orf[k] = u[k]; im[k] = 1.f;
-        if (l >= n) continue;
+        if (!lead || l >= n) continue;
         const int i = off + l;
         if (s.res_valid) {
             L.pk[lo] = e->pk[i];
@@ -614,8 +642,8 @@ __global__ void __launch_bounds__(NT) e_res(EDev *e, const int *sys_of_cluster, 
             const int kind = s.verify;
 #pragma unroll
             for (int k = 0; k < PPT; k++) {
-                const int lo = t + k * NT, l = base + lo;
-                if (!pstale || l >= n) break;
+                const int lo = q + k * NG, l = base + lo;
+                if (!pstale || !lead || l >= n) break;
                 const int i = off + l;
                 e->pos[i] = res_position(L, e->ctr[i], lo);
             }
@@ -625,11 +653,14 @@ __global__ void __launch_bounds__(NT) e_res(EDev *e, const int *sys_of_cluster, 
             double a[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
 #pragma unroll
             for (int k = 0; k < PPT; k++) {
-                const int lo = t + k * NT, l = base + lo;
-                if (l >= n) break;
-                const int i = off + l;
-                double ax, ay, en, wv, nc;
-                res_forces_f64<C, M>(e, s, L, lo, i, ax, ay, en, wv, nc);
+                const int lo = q + k * NG, l = base + lo;
+                const bool live = l < n;
+                const int i = off + (live ? l : 0);
+                double ax = 0, ay = 0, en = 0, wv = 0, nc = 0;
+                if (live) res_forces_f64<C, M, G>(e, s, L, lo, i, ax, ay, en, wv, nc);
+                ax = lanes_sum<G>(ax); ay = lanes_sum<G>(ay); en = lanes_sum<G>(en);
+                wv = lanes_sum<G>(wv); nc = lanes_sum<G>(nc);
+                if (!lead || !live) continue;
                 e->frc[i] = make_double2(ax, ay);
                 fr[k] = make_float2((float)ax, (float)ay);
                 frl[k] = make_float2((float)(ax - (double)fr[k].x), (float)(ay - (double)fr[k].y));
@@ -644,7 +675,7 @@ __global__ void __launch_bounds__(NT) e_res(EDev *e, const int *sys_of_cluster, 
             if (t == 0) {
                 RPartD pd;
 #pragma unroll
-                for (int q = 0; q < 5; q++) pd.v[q] = a[q];
+                for (int b = 0; b < 5; b++) pd.v[b] = a[b];
                 pd.req = req;
                 res_bcast<C>(ctl.partd_in, r, pd);
             }
@@ -652,7 +683,7 @@ __global__ void __launch_bounds__(NT) e_res(EDev *e, const int *sys_of_cluster, 
             if (t == 0) {
                 double tot[5];
 #pragma unroll
-                for (int q = 0; q < 5; q++) tot[q] = ctl.partd_in[0].v[q];
+                for (int b = 0; b < 5; b++) tot[b] = ctl.partd_in[0].v[b];
                 for (int b = 1; b < C; b++) {
                     tot[0] += ctl.partd_in[b].v[0];
                     tot[1] += ctl.partd_in[b].v[1];
@@ -665,7 +696,7 @@ __global__ void __launch_bounds__(NT) e_res(EDev *e, const int *sys_of_cluster, 
             }
             __syncthreads();
         } else {
-            // ---- move (src/integrator/fire.cu:29-40)
+            // ---- move (src/integrator/fire.cu:29-40), lead lanes
             int moved_rb = 0;
             if (!s.resume && s.phase == kMinimize) {
                 int need = 0;
@@ -674,8 +705,8 @@ __global__ void __launch_bounds__(NT) e_res(EDev *e, const int *sys_of_cluster, 
                     const bool uphill = s.uphill;
 #pragma unroll
                     for (int k = 0; k < PPT; k++) {
-                        const int lo = t + k * NT, l = base + lo;
-                        if (l >= n) break;
+                        const int lo = q + k * NG, l = base + lo;
+                        if (!lead || l >= n) break;
                         const float4 a = L.pk[lo], al = L.pkl[lo];
                         dw ox = {a.x, al.x}, oy = {a.y, al.y};
                         float2 v = u[k];
@@ -703,8 +734,8 @@ __global__ void __launch_bounds__(NT) e_res(EDev *e, const int *sys_of_cluster, 
                     const bool from32 = s.vel_f32, stale = pstale;
 #pragma unroll
                     for (int k = 0; k < PPT; k++) {
-                        const int lo = t + k * NT, l = base + lo;
-                        if (l >= n) break;
+                        const int lo = q + k * NG, l = base + lo;
+                        if (!lead || l >= n) break;
                         const int i = off + l;
                         const double2 c = e->ctr[i];
                         double2 x = stale ? res_position(L, c, lo) : e->pos[i];
@@ -754,8 +785,8 @@ __global__ void __launch_bounds__(NT) e_res(EDev *e, const int *sys_of_cluster, 
                 for (int c = t; c < nc; c += NT) L.ccur[c] = 0;
 #pragma unroll
                 for (int k = 0; k < PPT; k++) {
-                    const int lo = t + k * NT, l = base + lo;
-                    if (l >= n) break;
+                    const int lo = q + k * NG, l = base + lo;
+                    if (!lead || l >= n) break;
                     const int i = off + l;
                     const double2 x = stale ? res_position(L, e->ctr[i], lo) : e->pos[i];
                     const double fx = floor(x.x * s.inv_cs), fy = floor(x.y * s.inv_cs);
@@ -804,8 +835,8 @@ __global__ void __launch_bounds__(NT) e_res(EDev *e, const int *sys_of_cluster, 
                 int mx = 0;
 #pragma unroll
                 for (int k = 0; k < PPT; k++) {
-                    const int lo = t + k * NT, l = base + lo;
-                    if (l >= n) break;
+                    const int lo = q + k * NG, l = base + lo;
+                    if (!lead || l >= n) break;
                     mx = max(mx, res_nlist<C, M>(e, s, L, lo, l, off + l));
                 }
 #pragma unroll
@@ -839,33 +870,43 @@ __global__ void __launch_bounds__(NT) e_res(EDev *e, const int *sys_of_cluster, 
                     const bool short_dw = p.pe_diff_target <= 0.0;
 #pragma unroll
                     for (int k = 0; k < PPT; k++) {
-                        const int lo = t + k * NT, l = base + lo;
-                        if (l >= n) break;
-                        const int i = off + l;
-                        float2 f, flo;
-                        float wv;
-                        int ncount;
-                        if (!dwp) {
-                            float en;
-                            res_forces_f32<C, M>(e, s, L, lo, i, f.x, f.y, en, wv, ncount);
-                            flo = make_float2(0.f, 0.f);
-                            pe = dw_add_f(pe, en);
-                        } else if (short_dw) {
-                            dw sx, sy;
-                            float en;
-                            res_forces_dwf<C, M>(e, s, L, lo, i, sx, sy, en, wv, ncount);
-                            f = make_float2(sx.hi, sy.hi);
-                            flo = make_float2(sx.lo, sy.lo);
-                            pe = dw_add_f(pe, en);
-                        } else {
-                            dw sx, sy, se;
-                            res_forces_dw<C, M>(e, s, L, lo, i, sx, sy, se, wv, ncount);
-                            f = make_float2(sx.hi, sy.hi);
-                            flo = make_float2(sx.lo, sy.lo);
-                            pe = dw_add(pe, se);
+                        const int lo = q + k * NG, l = base + lo;
+                        const bool live = l < n;
+                        const int i = off + (live ? l : 0);
+                        dw fx = {0.f, 0.f}, fy = {0.f, 0.f}, en = {0.f, 0.f};
+                        float wv = 0.f;
+                        int ncount = 0;
+                        if (live) {
+                            if (!dwp) {
+                                float ax, ay, ef;
+                                res_forces_f32<C, M, G>(e, s, L, lo, i, ax, ay, ef, wv, ncount);
+                                fx.hi = ax; fy.hi = ay; en.hi = ef;
+                            } else if (short_dw) {
+                                float ef;
+                                res_forces_dwf<C, M, G>(e, s, L, lo, i, fx, fy, ef, wv, ncount);
+                                en.hi = ef;
+                            } else {
+                                res_forces_dw<C, M, G>(e, s, L, lo, i, fx, fy, en, wv, ncount);
+                            }
                         }
+                        if (G > 1) {
+                            if (dwp) {
+                                fx = lanes_dw<G>(fx);
+                                fy = lanes_dw<G>(fy);
+                                en = lanes_dw<G>(en);
+                            } else {
+                                fx.hi = lanes_sum<G>(fx.hi);
+                                fy.hi = lanes_sum<G>(fy.hi);
+                                en.hi = lanes_sum<G>(en.hi);
+                            }
+                            wv = lanes_sum<G>(wv);
+                            ncount = lanes_sum<G>(ncount);
+                        }
+                        if (!lead || !live) continue;
+                        pe = dw_add(pe, en);
+                        const float2 f = make_float2(fx.hi, fy.hi);
                         fr[k] = f;
-                        frl[k] = flo;
+                        frl[k] = make_float2(fx.lo, fy.lo);
                         float2 vv = u[k];
                         if (!setup) {
                             const float hm = h * im[k];
@@ -883,7 +924,7 @@ __global__ void __launch_bounds__(NT) e_res(EDev *e, const int *sys_of_cluster, 
                         RPart pp;
                         pp.pe = pe;
 #pragma unroll
-                        for (int q = 0; q < 4; q++) pp.v[q] = v[q];
+                        for (int b = 0; b < 4; b++) pp.v[b] = v[b];
                         pp.req = req;
                         res_bcast<C>(ctl.part_in, r, pp);
                     }
@@ -892,7 +933,7 @@ __global__ void __launch_bounds__(NT) e_res(EDev *e, const int *sys_of_cluster, 
                         dw tp = ctl.part_in[0].pe;
                         float tv[4];
 #pragma unroll
-                        for (int q = 0; q < 4; q++) tv[q] = ctl.part_in[0].v[q];
+                        for (int b = 0; b < 4; b++) tv[b] = ctl.part_in[0].v[b];
                         for (int b = 1; b < C; b++) {
                             tp = dw_add(tp, ctl.part_in[b].pe);
                             tv[0] += ctl.part_in[b].v[0];
@@ -908,11 +949,14 @@ __global__ void __launch_bounds__(NT) e_res(EDev *e, const int *sys_of_cluster, 
                     double a[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
 #pragma unroll
                     for (int k = 0; k < PPT; k++) {
-                        const int lo = t + k * NT, l = base + lo;
-                        if (l >= n) break;
-                        const int i = off + l;
-                        double ax, ay, en, wv, nc;
-                        res_forces_f64<C, M>(e, s, L, lo, i, ax, ay, en, wv, nc);
+                        const int lo = q + k * NG, l = base + lo;
+                        const bool live = l < n;
+                        const int i = off + (live ? l : 0);
+                        double ax = 0, ay = 0, en = 0, wv = 0, nc = 0;
+                        if (live) res_forces_f64<C, M, G>(e, s, L, lo, i, ax, ay, en, wv, nc);
+                        ax = lanes_sum<G>(ax); ay = lanes_sum<G>(ay); en = lanes_sum<G>(en);
+                        wv = lanes_sum<G>(wv); nc = lanes_sum<G>(nc);
+                        if (!lead || !live) continue;
                         const double2 f = make_double2(ax, ay);
                         e->frc[i] = f;
                         fr[k] = make_float2((float)ax, (float)ay);
@@ -935,7 +979,7 @@ __global__ void __launch_bounds__(NT) e_res(EDev *e, const int *sys_of_cluster, 
                     if (t == 0) {
                         RPartD pd;
 #pragma unroll
-                        for (int q = 0; q < 5; q++) pd.v[q] = a[q];
+                        for (int b = 0; b < 5; b++) pd.v[b] = a[b];
                         pd.req = req;
                         res_bcast<C>(ctl.partd_in, r, pd);
                     }
@@ -943,7 +987,7 @@ __global__ void __launch_bounds__(NT) e_res(EDev *e, const int *sys_of_cluster, 
                     if (t == 0) {
                         double tot[5];
 #pragma unroll
-                        for (int q = 0; q < 5; q++) tot[q] = ctl.partd_in[0].v[q];
+                        for (int b = 0; b < 5; b++) tot[b] = ctl.partd_in[0].v[b];
                         for (int b = 1; b < C; b++) {
                             tot[0] += ctl.partd_in[b].v[0];
                             tot[1] += ctl.partd_in[b].v[1];
@@ -965,8 +1009,8 @@ __global__ void __launch_bounds__(NT) e_res(EDev *e, const int *sys_of_cluster, 
             const bool stale = pstale;
 #pragma unroll
             for (int k = 0; k < PPT; k++) {
-                const int lo = t + k * NT, l = base + lo;
-                if (l >= n) break;
+                const int lo = q + k * NG, l = base + lo;
+                if (!lead || l >= n) break;
                 const int i = off + l;
                 double2 x = stale ? res_position(L, e->ctr[i], lo) : e->pos[i];
                 if (act == kActCompress && s.pressure < p.p_low && s.jam_stage == 1 && s.L_saved == s.L)
@@ -992,8 +1036,8 @@ __global__ void __launch_bounds__(NT) e_res(EDev *e, const int *sys_of_cluster, 
     const bool f64_last = s.prec == 1;
 #pragma unroll
     for (int k = 0; k < PPT; k++) {
-        const int lo = t + k * NT, l = base + lo;
-        if (l >= n) break;
+        const int lo = q + k * NG, l = base + lo;
+        if (!lead || l >= n) break;
         const int i = off + l;
         if (stale) e->pos[i] = res_position(L, e->ctr[i], lo);
         e->pk[i] = L.pk[lo];
