@@ -392,26 +392,18 @@ struct RClass {
     int per_block() const { return nt / g * ppt; }
     int capacity() const { return nt / g * ppt * c; }
 };
+// Measured on one GB300 (double-word FIRE iterations of 4 / 48 systems):
+// lanes per particle and larger blocks for the small systems (N = 128: 5.4 vs
+// 9.4 us per iteration with 4 particles per thread), clusters of 8 blocks for
+// the largest (N = 4096 alone: 18.8 vs 30.0 us on 4 blocks of 4 particles per
+// thread), 2 particles per thread where many large systems share the GPU
+// (N = 2048, 48 systems: 24.9 vs 30.6 us).
 constexpr int kNClass = 7;
 #define RC(NT, PPT, C, G) {NT, PPT, C, G, e_res<NT, PPT, C, G>}
-static const RClass kRTables[3][kNClass] = {
-    {RC(64, 4, 1, 1), RC(128, 4, 1, 1), RC(256, 4, 1, 1), RC(256, 4, 2, 1), RC(256, 4, 4, 1),
-     RC(256, 4, 4, 1), RC(256, 4, 4, 1)},
-    {RC(256, 1, 1, 4), RC(256, 1, 1, 2), RC(256, 1, 1, 1), RC(512, 1, 1, 1), RC(512, 1, 2, 1),
-     RC(512, 1, 4, 1), RC(512, 1, 8, 1)},
-    {RC(128, 1, 1, 2), RC(128, 1, 1, 1), RC(128, 2, 1, 1), RC(256, 2, 1, 1), RC(256, 2, 2, 1),
-     RC(256, 2, 4, 1), RC(256, 2, 8, 1)},
-};
+static const RClass kRClasses[kNClass] = {RC(256, 1, 1, 4), RC(256, 1, 1, 2), RC(256, 1, 1, 1),
+                                          RC(512, 1, 1, 1), RC(512, 1, 2, 1), RC(256, 2, 4, 1),
+                                          RC(256, 2, 8, 1)};
 #undef RC
-static const RClass *res_table() {
-    static const RClass *t = nullptr;
-    if (!t) {
-        const char *tb = getenv("DPG_RES_TABLE");
-        t = kRTables[(tb && tb[0] >= '0' && tb[0] <= '2') ? tb[0] - '0' : 0];
-    }
-    return t;
-}
-#define kRClasses res_table()
 
 static int res_class_of(int n) {
     for (int c = 0; c < kNClass; c++)

@@ -167,6 +167,20 @@ __device__ __forceinline__ void res_reduce(dw &pe, float (&v)[4], dw *smw, float
     }
 }
 
+// FIRE mix with per-particle norms (src/particles/base/kernels.cu:91-112) in
+// FP32 from the hardware reciprocal square root: |v| / |F| = sqrt(v2 / F2)
+// (the mixing weight carries no precision requirement)
+__device__ __forceinline__ float2 res_fire_mix(float2 v, float2 f, float alpha) {
+    const float fn2 = f.x * f.x + f.y * f.y, vn2 = v.x * v.x + v.y * v.y;
+    float mix = 0.f;
+    if (fn2 > 1e-32f) {
+        mix = sqrtf(vn2 * __frcp_rn(fn2)) * alpha;
+    } else {
+        v = make_float2(0.f, 0.f);
+    }
+    return make_float2(v.x * (1.f - alpha) + f.x * mix, v.y * (1.f - alpha) + f.y * mix);
+}
+
 // periodic cell difference of two packed cell codes
 __device__ __forceinline__ void res_dcell(int ca, int cb, int ncd, int &dcx, int &dcy) {
     dcx = code_x(ca) - code_x(cb);
@@ -619,18 +633,22 @@ __global__ void __launch_bounds__(NT) e_res(EDev *e, const int *sys_of_cluster, 
     bool pstale = false;
     long long it = 0;
     const float half_skin2_f = (float)p.half_skin2;
-    for (;;) {
-        // ---- uniform loop exit: every block holds the same copy of s and the
-        // same request of block 0 (exchanged with the last totals)
-        if (t == 0) {
-            int st = (s.phase == kIdle) || (it >= iter_budget) || ctl.req;
-            if (C == 1 && !st && (it & 31) == 0) {
-                if (*(volatile int *)&e->overflow) st = 1;
-                else if (t_end && global_ns() > t_end) st = 1;
-            }
-            ctl.stop = st;
+    // Uniform loop exit, decided by thread 0 after each epilogue (before the
+    // barrier that publishes the epilogue) from the state every block shares:
+    // the system is done, the budget is spent, or block 0 asked to leave (its
+    // request travels with the exchanged totals; one block checks the time
+    // slice and the overflow flag itself, every 32 iterations).
+    auto decide_stop = [&](long long next_it) {
+        int st = (s.phase == kIdle) || (next_it >= iter_budget) || ctl.req;
+        if (C == 1 && !st && (next_it & 31) == 0) {
+            if (*(volatile int *)&e->overflow) st = 1;
+            else if (t_end && global_ns() > t_end) st = 1;
         }
-        __syncthreads();
+        ctl.stop = st;
+    };
+    if (t == 0) decide_stop(0);
+    __syncthreads();
+    for (;;) {
         if (ctl.stop) break;
         // block 0's request to leave after this iteration (multi-block clusters)
         int req = 0;
@@ -693,6 +711,7 @@ __global__ void __launch_bounds__(NT) e_res(EDev *e, const int *sys_of_cluster, 
                 }
                 ctl.req = ctl.partd_in[0].req;
                 res_verify_epilogue(e, s, tot, kind, primary);
+                if (s.pending == kActNone) decide_stop(it + 1);
             }
             __syncthreads();
         } else {
@@ -720,7 +739,7 @@ __global__ void __launch_bounds__(NT) e_res(EDev *e, const int *sys_of_cluster, 
                         const float h = 0.5f * dt * im[k];
                         v.x += f.x * h;
                         v.y += f.y * h;
-                        v = fire_mix_f(v, f, alpha);
+                        v = res_fire_mix(v, f, alpha);
                         u[k] = v;
                         ox = dw_add_f(ox, v.x * dt);
                         oy = dw_add_f(oy, v.y * dt);
@@ -944,6 +963,7 @@ __global__ void __launch_bounds__(NT) e_res(EDev *e, const int *sys_of_cluster, 
                         ctl.req = ctl.part_in[0].req;
                         const double tot[5] = {(double)tp.hi + (double)tp.lo, tv[0], tv[1], tv[2], tv[3]};
                         e_force_epilogue(e, s, tot, setup, primary);
+                        if (s.pending == kActNone) decide_stop(it + 1);
                     }
                 } else {
                     double a[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
@@ -997,6 +1017,7 @@ __global__ void __launch_bounds__(NT) e_res(EDev *e, const int *sys_of_cluster, 
                         }
                         ctl.req = ctl.partd_in[0].req;
                         e_force_epilogue(e, s, tot, setup, primary);
+                        if (s.pending == kActNone) decide_stop(it + 1);
                     }
                 }
                 __syncthreads();
@@ -1023,7 +1044,10 @@ __global__ void __launch_bounds__(NT) e_res(EDev *e, const int *sys_of_cluster, 
                 u[k] = make_float2(0.f, 0.f);
             }
             __syncthreads();
-            if (t == 0) e_transition_sys(p, s, act);
+            if (t == 0) {
+                e_transition_sys(p, s, act);
+                decide_stop(it + 1);
+            }
             pstale = false;
             __syncthreads();
         }
