@@ -55,7 +55,16 @@ CUTOFF, SKIN = 1.7, 0.3     # neighbour cutoff d_max + skin, and the skin
 TUNE_ITERS = 300            # FIRE iterations per autotuner candidate
 FORM_CODES = {"grid": 1, "persist": 2}
 SWITCH_FMAX = 1e-6          # mixed systems switch to FP64 pair forces below this max|F|
-PLAIN_SOLVES = 2            # timed solves of the plain FP64 path (after one untimed)
+PLAIN_SOLVES = 8            # timed solves of the plain FP64 path (after one untimed)
+E2E_BATCHES = 4             # timed batches solved again through host arrays (e2e)
+# jamming leg: the pressure band's centre in the default run (the workload's
+# 1e-7 takes tens of minutes per ensemble: single systems need 1e7-1e8 FIRE
+# iterations there; bench.py --jam-ensemble --jam-pressure 1e-7 runs it)
+JAM_SYSTEMS = 256
+JAM_PRESSURE = 1e-4
+JAM_PLAIN_BUDGET_S = 60.0
+JAM_FIRE = (0.1, 1e-2, 1e-16, 0.0, 100000, 1e-13)  # alpha0, dt0, PE/N target, no PE-change test,
+                                                   # at most 1e5 iterations, max|F| target
 WARMUP_ITERS = 2000         # FIRE iterations of a warm-up solve
 E_FORCE_DRAM_PER_SYSTEM = 10.37e6 / 8  # ncu DRAM bytes per e_force launch per 16384-disk system
 PROFILE_ITERS = 300
@@ -336,79 +345,50 @@ def run_ours(args):
     value = world * args.steps * BATCH / (total_ms / 1e3)
     flat = [r for res in results for r in res]
     ok = all(r["converged"] and r["max_force"] <= FMAX for r in flat)
+    finals = [e.getState() for e, _ in batches]   # after the timed region
 
-    # ---- e2e: host arrays in, host positions/forces out, through the C ABI ---
+    # ---- e2e: host arrays in, host positions/forces out, through the C ABI, on
+    # the first E2E_BATCHES timed batches (the same starts, solved again) --------
     e2e_ms = []
     h2d = BATCH * N_PART * 8 * 4   # x, y, radii, masses
     d2h = BATCH * N_PART * 8 * 4   # x, y, fx, fy
-    n_e2e = len(batches)
-    e2e_results = []
-    for e, sts in batches:
+    e2e_batches = batches[:min(len(batches), E2E_BATCHES)]
+    for e, sts in e2e_batches:
         host = [np.concatenate([st[c] for st in sts]) for c in ("x", "y", "r", "m")]
         l2_flush()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         e.setState(*host)
-        e2e_results.append(solve_batch(e))
+        solve_batch(e)
         out = e.getState()
         _ = float(np.abs(out["fx"]).max())
         e2e_ms.append(1e3 * (time.perf_counter() - t0))
-    e2e_value = world * n_e2e * BATCH / (max_over_ranks(float(np.sum(e2e_ms))) / 1e3)
+    e2e_value = world * len(e2e_batches) * BATCH / (max_over_ranks(float(np.sum(e2e_ms))) / 1e3)
 
-    # ---- the plain FP64 drop-in on the same systems (one per call) -----------
+    # ---- the plain FP64 drop-in on the first PLAIN_SOLVES starts (one per call)
+    # and the batched FP64 form on the same starts -----------------------------
     plain = plain_fp64_leg(dpg, sptr, batches[0][1][:PLAIN_SOLVES + 1], timed)
+    batched64 = batched_fp64_leg(dpg, sptr, batches[0][1][1:PLAIN_SOLVES + 1], timed, form, tune)
 
-    # ---- error of the mixed form: its minima re-evaluated by the FP64 path ----
-    # (the FP64 path is bit-identical to the reference arithmetic; the two forms
-    # reach different minima from the same start, so the check is done at the
-    # mixed form's own final positions)
-    e, sts = batches[0]
-    fin = e.getState()
-    checks, off = [], 0
-    for k, st in enumerate(sts[:4]):
-        xs, ys = fin["x"][off:off + N_PART], fin["y"][off:off + N_PART]
-        off += N_PART
-        d = dpg.Disk(N_PART, st["box"], stream=sptr)
-        d.setState(xs, ys, None, None, st["r"], st["m"])
-        d.setupNeighbors("cell", CUT_MULT, 0.2, 8.0, 0.5)
-        d.zeroForceAndPotentialEnergy()
-        d.calculateForces()
-        g = d.getState()
-        f64 = float(np.sqrt(g["fx"] ** 2 + g["fy"] ** 2).max())
-        pe64 = d.totalPotentialEnergy() / N_PART
-        r = e2e_results[0][k]  # the last solve of this batch
-        checks.append({"max_force_fp64": f64, "max_force_reported": r["max_force"],
-                       "avg_pe_fp64": pe64, "avg_pe_reported": r["avg_pe"],
-                       "avg_pe_rel_diff": abs(r["avg_pe"] - pe64) / pe64})
-        d.close()
-    mixed_check = {"systems": len(checks), "max_force_fp64_max": max(c["max_force_fp64"] for c in checks),
-                   "avg_pe_rel_diff_max": max(c["avg_pe_rel_diff"] for c in checks), "detail": checks}
+    # ---- error of the mixed form: every timed minimum re-evaluated by the FP64
+    # drop-in (bit-identical to the reference arithmetic; the forms reach
+    # different minima from the same start, so the check is at the mixed form's
+    # own final positions) ---------------------------------------------------------
+    mixed_check = fp64_recheck(dpg, sptr, batches, finals, results)
 
-    # ---- roofline of the dominant kernel of the headline form ----------------
+    # ---- roofline of the dominant kernel of the headline form, weighted over the
+    # three arithmetics by the share of force passes each took -------------------
     peak, peak_src = measured_peak_hbm()
-    e, sts = batches[-1]
-    e.setState(*[np.concatenate([st[c] for st in sts]) for c in ("x", "y", "r", "m")])
-    prof = e.profileLoop(PROFILE_ITERS, FIRE_ALPHA0, FIRE_DT0, FMAX)
-    k_mean = plain["mean_neighbors"]
-    # e_force (mixed phase) per particle: read pk[i] 16, count 4, neighbour
-    # indices 4k, vel 16, mass 8; write frc 16, pe 8, vel 16 (neighbours' pk
-    # gathered from cache) -> 84 + 4k
-    bytes_force = BATCH * N_PART * (84 + 4 * k_mean)
-    achieved = bytes_force / (prof["force_us"] * 1e-6) / 1e9
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": E_FORCE_DRAM_PER_SYSTEM * BATCH,
-                "traffic_source": "ncu dram__bytes_read+write of one FP32-phase e_force launch on "
-                                  "8 x 16384 disks (10.37 MB), scaled to the batch by systems",
-                "kernel": "e_force",
-                "peak_source": peak_src, "bytes_per_launch": bytes_force,
-                "launch_us": prof["force_us"], "profile_us_per_iter": prof,
-                "note": f"{BATCH} x 16384 disks, first {PROFILE_ITERS} FIRE iterations (FP32 pair "
-                        f"phase); the working set ({BATCH * 16384 * 200 / 1e6:.0f} MB) is L2-resident, "
-                        "so the kernel is bound by latency and the FP64 pipe, not by HBM"}
+    roofline = headline_roofline(dpg, sptr, batches, finals, flat, plain["mean_neighbors"], peak,
+                                 peak_src, tune)
 
     # ---- large-N force kernel (N = 2^20 NVE, plain FP64) -----------------------
     large = large_n_roofline(dpg, dev, sptr, peak)
     others = other_configs(dpg, sptr)
+
+    # ---- the jamming ensemble (256 uneven systems, pressure band) ---------------
+    jam = None if args.no_jam else jam_leg(dpg, args.jam_systems, args.jam_pressure,
+                                           JAM_PLAIN_BUDGET_S)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -425,7 +405,9 @@ def run_ours(args):
                 "dtype": "f32+f64", "data": "synthetic", "config": workload_config(),
                 "roofline": roofline, "cpu_baseline": cpu,
                 "e2e": {"value": e2e_value, "unit": "FIRE solves/s", "h2d_bytes_per_step": h2d,
-                        "d2h_bytes_per_step": d2h},
+                        "d2h_bytes_per_step": d2h,
+                        "sample": f"the first {len(e2e_batches)} timed batches, solved again "
+                                  "from host arrays"},
                 "gpu_launches": launches, "clocks": clocks,
                 "extra": {"form": "mixed+batched", "systems_per_step": BATCH,
                           "fire_iterations_per_solve": float(np.mean([r["fire_steps"] for r in flat])),
@@ -435,8 +417,11 @@ def run_ours(args):
                           "max_force": float(max(r["max_force"] for r in flat)),
                           "wall_s_timed": t_wall,
                           "plain_fp64": plain,
+                          "batched_fp64": batched64,
                           "mixed_minima_checked_in_fp64": mixed_check,
                           "mixed_batched_over_plain_fp64": value / plain["value"],
+                          "mixed_batched_over_batched_fp64": value / batched64["value"],
+                          "jam_ensemble": jam,
                           "roofline_large": large, "other_workloads": others,
                           "autotune": {"chosen": {"form": tune["form"], "threads": tune["threads"],
                                                   "skin": tune["skin"]},
@@ -450,10 +435,13 @@ def run_ours(args):
 
 def plain_fp64_leg(dpg, sptr, sts, timed):
     """The drop-in FP64 path (bit-identical to the reference arithmetic): one
-    system per call, first start untimed (warm-up), the rest timed."""
+    system per call, first start untimed (warm-up), the rest timed.  Every
+    timed solve must converge to FMAX (the minimizeFire result's converged flag
+    and its FP64 max|F|)."""
     import torch
     dev = torch.device("cuda", torch.cuda.current_device())
-    out = {"solves": 0, "ms": [], "fire_iterations": [], "avg_pe": [], "max_force": []}
+    out = {"solves": 0, "ms": [], "fire_iterations": [], "avg_pe": [], "max_force": [],
+           "converged": []}
     for k, st in enumerate(sts):
         s = dpg.Disk(N_PART, st["box"], stream=sptr)
         arr = {c: torch.from_numpy(st[c]).to(dev) for c in ("x", "y", "r", "m")}
@@ -476,12 +464,114 @@ def plain_fp64_leg(dpg, sptr, sts, timed):
         out["fire_iterations"].append(r["steps"])
         out["avg_pe"].append(s.totalPotentialEnergy() / N_PART)
         out["max_force"].append(r["max_force"])
+        out["converged"].append(bool(r["converged"]) and r["max_force"] <= FMAX)
         s.close()
+    rates = 1e3 / np.array(out["ms"])
     out["value"] = out["solves"] / (float(np.sum(out["ms"])) / 1e3)
+    out["solves_per_s_per_solve"] = {"mean": float(rates.mean()), "min": float(rates.min()),
+                                     "max": float(rates.max())}
+    out["fire_iterations_stats"] = {"mean": float(np.mean(out["fire_iterations"])),
+                                    "min": int(np.min(out["fire_iterations"])),
+                                    "max": int(np.max(out["fire_iterations"]))}
+    out["all_converged"] = all(out["converged"])
     out["unit"] = "FIRE solves/s"
     out["dtype"] = "f64"
     out["force_group"] = "threads per particle chosen by the library (8 at N=16384)"
     return out
+
+
+def batched_fp64_leg(dpg, sptr, sts, timed, form, tune):
+    """The batched form in FP64 pair arithmetic on the starts the plain leg timed
+    (one call for all of them): the batching part of the headline's gain,
+    apart from the precision part."""
+    n = len(sts)
+    e = dpg.Ensemble([N_PART] * n, [st["box"] for st in sts], CUTOFF, SKIN,
+                     precision=dpg.FP64, stream=sptr)
+    e.setForm(form, tune["threads"])
+    host = [np.concatenate([st[c] for st in sts]) for c in ("x", "y", "r", "m")]
+    e.setState(*host)
+    e.minimizeFire(FIRE_ALPHA0, FIRE_DT0, 0.0, 0.0, 200, fmax_target=FMAX)   # graph build
+    e.setState(*host)
+    res, ms = timed(lambda: e.minimizeFire(FIRE_ALPHA0, FIRE_DT0, 0.0, 0.0, MAX_STEPS,
+                                           fmax_target=FMAX))
+    e.close()
+    return {"value": n / (ms / 1e3), "unit": "FIRE solves/s", "systems": n, "dtype": "f64",
+            "all_converged": all(r["converged"] and r["max_force"] <= FMAX for r in res),
+            "fire_iterations_mean": float(np.mean([r["fire_steps"] for r in res])),
+            "sample": "the starts the plain FP64 leg timed, in one batched call"}
+
+
+def fp64_recheck(dpg, sptr, batches, finals, results):
+    """Every timed mixed minimum re-evaluated by the FP64 drop-in at its final
+    positions: max|F| and the relative energy difference to the reported one."""
+    worst_f, worst_pe, n_checked, n_over = 0.0, 0.0, 0, 0
+    for (e, sts), fin, res in zip(batches, finals, results):
+        for k, st in enumerate(sts):
+            sl = slice(k * N_PART, (k + 1) * N_PART)
+            d = dpg.Disk(N_PART, st["box"], stream=sptr)
+            d.setState(fin["x"][sl], fin["y"][sl], None, None, st["r"], st["m"])
+            d.setupNeighbors("cell", CUT_MULT, 0.2, 8.0, 0.5)
+            d.zeroForceAndPotentialEnergy()
+            d.calculateForces()
+            f64 = d.forceStats()[0]
+            pe64 = d.totalPotentialEnergy() / N_PART
+            d.close()
+            worst_f = max(worst_f, f64)
+            worst_pe = max(worst_pe, abs(res[k]["avg_pe"] - pe64) / pe64)
+            n_over += f64 > FMAX
+            n_checked += 1
+    return {"systems": n_checked, "max_force_fp64_max": worst_f, "above_fmax": int(n_over),
+            "avg_pe_rel_diff_max": worst_pe}
+
+
+def headline_roofline(dpg, sptr, batches, finals, flat, k_mean, peak, peak_src, tune):
+    """e_force of the headline form, per arithmetic: the FP32 phase from fresh
+    starts, the double-word phase and the FP64 passes at converged minima
+    (PROFILE_ITERS plain launches each, CUDA events), weighted by the share of
+    force passes each arithmetic took in the timed solves."""
+    e, sts = batches[-1]
+    host = [np.concatenate([st[c] for st in sts]) for c in ("x", "y", "r", "m")]
+    e.setState(*host)
+    p32 = e.profileLoop(PROFILE_ITERS, FIRE_ALPHA0, FIRE_DT0, FMAX)
+    fin = finals[-1]
+    e.setState(fin["x"], fin["y"], host[2], host[3])
+    pdw = e.profileLoop(PROFILE_ITERS, FIRE_ALPHA0, FIRE_DT0, 1e-15)
+    e64 = dpg.Ensemble([N_PART] * BATCH, [st["box"] for st in sts], CUTOFF, SKIN,
+                       precision=dpg.FP64, stream=sptr)
+    e64.setState(fin["x"], fin["y"], host[2], host[3])
+    p64 = e64.profileLoop(PROFILE_ITERS // 3, FIRE_ALPHA0, FIRE_DT0, 1e-15)
+    e64.close()
+    passes = float(sum(r["fire_steps"] for r in flat))
+    n64 = float(sum(r["fp64_steps"] for r in flat))
+    ndw = float(sum(r["dw_steps"] for r in flat))
+    w = {"fp32": (passes - n64 - ndw) / passes, "dword": ndw / passes, "fp64": n64 / passes}
+    # algorithmic bytes per particle and pass: FP32 phase reads the packed
+    # offsets 16, count 4, indices 4k, FP32 velocity 8, 1/m 4 and writes the FP64
+    # force 16, FP32 force 8 and velocity 8 (84 + 4k); the double-word phase also
+    # reads the low words 16 (100 + 4k); FP64 reads position 16, radius 8, packed
+    # offsets 16, count 4, indices 4k, velocity 16, mass 8 and writes force and
+    # velocity 32 (100 + 4k); neighbours' data are gathered from cache
+    per = {"fp32": 84 + 4 * k_mean, "dword": 100 + 4 * k_mean, "fp64": 100 + 4 * k_mean}
+    us = {"fp32": p32["force_us"], "dword": pdw["force_us"], "fp64": p64["force_us"]}
+    phases = {}
+    for ph in ("fp32", "dword", "fp64"):
+        b = BATCH * N_PART * per[ph]
+        ach = b / (us[ph] * 1e-6) / 1e9
+        phases[ph] = {"share_of_passes": w[ph], "launch_us": us[ph], "bytes_per_launch": b,
+                      "achieved": ach, "frac": ach / peak}
+    t_avg = sum(w[ph] * us[ph] for ph in us)
+    b_avg = sum(w[ph] * BATCH * N_PART * per[ph] for ph in per)
+    achieved = b_avg / (t_avg * 1e-6) / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": E_FORCE_DRAM_PER_SYSTEM * BATCH,
+            "traffic_source": "ncu dram__bytes_read+write of one FP32-phase e_force launch on "
+                              "8 x 16384 disks, scaled to the batch by systems",
+            "kernel": "e_force", "peak_source": peak_src, "bytes_per_launch": b_avg,
+            "launch_us": t_avg, "phases": phases,
+            "note": f"{BATCH} x 16384 disks; launch time weighted over the FP32, double-word and "
+                    "FP64 passes by their share of the timed solves' force passes; the working "
+                    "set is L2-resident, so the kernel is bound by latency and the FP64 pipe, "
+                    "not by HBM"}
 
 
 def other_configs(dpg, sptr):
@@ -582,54 +672,135 @@ def large_n_roofline(dpg, dev, sptr, peak):
     return out
 
 
-def jam_ensemble(args):
-    """The batched jamming workload (not the default line): S bidisperse
-    systems with N drawn log-uniformly in [64, 4096] from a seed, each
-    starting at phi = 0.80, compressed by box scaling with a FIRE
-    minimisation (the reference's minimizeFire defaults: PE targets 1e-16,
-    at most 1e5 steps) after each step and bisected on the box length until
-    the pressure is 1e-7 +- 1e-9 (scripts/runArthurJamWithFire.cpp flow).
-    Prints one JSON line: systems jammed per second for the mixed and FP64
-    ensembles and |phi_J(mixed) - phi_J(FP64)| over the systems."""
-    import dpcuda_gb300 as dpg
+def jam_workload(S, seed=2024):
+    """S bidisperse disk systems, N drawn log-uniformly in [64, 4096] from a seed,
+    seeded random starts at phi = 0.80 (the reference's RandomUniform stream)."""
     from dpcuda_gb300.init import disk_packing
-    S = args.jam_systems
-    rng = np.random.default_rng(2024)
+    rng = np.random.default_rng(seed)
     sizes = np.floor(np.exp(rng.uniform(np.log(64), np.log(4096), S))).astype(int)
     sts = [disk_packing(int(n), 0.80, 7000 + k) for k, n in enumerate(sizes)]
+    return sizes, sts
+
+
+def jam_leg(dpg, S, P, plain_budget_s):
+    """Pressure-band jamming of S uneven systems (the scripts/runArthurJamWithFire.cpp
+    protocol: compression by box scaling, a FIRE minimisation after every step,
+    bisection on the box length until the pressure is inside P +- 1% with more
+    than 2 contacts per disk).
+
+    - mixed+batched: every system at once in the resident form (double-word
+      refinement, FP64 passes only certify states);
+    - FP64 check: each jammed state minimised again by the FP64 drop-in at its
+      own box; a state whose FP64 pressure is inside the band with enough
+      contacts has |dphi_J| = 0 (same box, same radii); any other is jammed
+      again by the FP64 drop-in from there with 1e-7 compression steps and
+      |dphi_J| is measured;
+    - plain FP64: the drop-in, one system per call, on a seeded random sample
+      of the systems until plain_budget_s of solving has passed."""
+    import torch
+    from dpcuda_gb300.ensemble import FORM_RESIDENT
+    sizes, sts = jam_workload(S)
+    band = (0.99 * P, 1.01 * P)
+    kw = dict(compression_rate=0.99, length_tolerance=1e-10, decompress_factor=1.01,
+              max_compression_steps=2000)
     cat = [np.concatenate([st[c] for st in sts]) for c in ("x", "y", "r", "m")]
-    band = (args.jam_pressure * 0.99, args.jam_pressure * 1.01)
-    fire = (0.1, 1e-2, 1e-16, 1e-16, 100000, 0.0)
-    print(json.dumps({"jam_sizes": [int(n) for n in sizes]}), file=sys.stderr, flush=True)
-    out = {}
-    for form, prec in (("mixed", dpg.MIXED), ("fp64", dpg.FP64)):
-        e = dpg.Ensemble(sizes, [st["box"] for st in sts], CUTOFF, SKIN, precision=prec,
-                         switch_fmax=SWITCH_FMAX)
-        e.setState(*cat)
-        t0 = time.perf_counter()
-        res = e.jam(*band, compression_rate=0.99, length_tolerance=1e-10, decompress_factor=1.01,
-                    max_compression_steps=args.jam_max_compressions, fire=fire)
-        dt = time.perf_counter() - t0
-        out[form] = {"s": dt, "systems_per_s": S / dt,
-                     "phi": [r["packing_fraction"] for r in res],
-                     "in_band": int(sum(band[0] <= r["pressure"] <= band[1] for r in res)),
-                     "status": [r["status"] for r in res],
-                     "fire_steps_max": int(max(r["fire_steps"] for r in res)),
-                     "minimizations_max": int(max(r["minimizations"] for r in res))}
-        print(json.dumps({"jam_form": form, "s": dt, "systems_per_s": S / dt,
-                          "in_band": out[form]["in_band"]}), file=sys.stderr, flush=True)
-        e.close()
-    d = np.abs(np.array(out["mixed"]["phi"]) - np.array(out["fp64"]["phi"]))
-    line = {"metric": "batched jamming: systems jammed/s, mixed vs FP64", "unit": "systems/s",
-            "value": out["mixed"]["systems_per_s"], "n_gpus": 1, "higher_is_better": True,
-            "config": {"workload": f"{S} systems, N log-uniform [64, 4096], phi0 0.80, "
-                                   f"P = {args.jam_pressure:g} +- 1%, FIRE 1e-16/1e-16/1e5",
-                       "sizes_sum": int(sizes.sum())},
-            "fp64_systems_per_s": out["fp64"]["systems_per_s"],
-            "dphi_J": {"median": float(np.median(d)), "max": float(d.max()),
-                       "frac_below_1e-6": float(np.mean(d <= 1e-6))},
-            "detail": out}
-    print(json.dumps(line), flush=True)
+    e = dpg.Ensemble(sizes, [st["box"] for st in sts], CUTOFF, SKIN, precision=dpg.MIXED,
+                     switch_fmax=SWITCH_FMAX)
+    e.setForm(FORM_RESIDENT)
+    e.setState(*cat)
+    e.minimizeFire(FIRE_ALPHA0, FIRE_DT0, 0.0, 0.0, 20, fmax_target=FMAX)  # module loading
+    e.setState(*cat)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    res = e.jam(*band, fire=JAM_FIRE, **kw)
+    torch.cuda.synchronize()
+    t_mixed = time.perf_counter() - t0
+    fin = e.getState()
+    e.close()
+    offs = np.concatenate([[0], np.cumsum(sizes)])
+    # ---- FP64 check of every jammed state
+    t1 = time.perf_counter()
+    dphi, rejam, n_ok, f64_iters = [], [], 0, []
+    for k in range(S):
+        n = int(sizes[k])
+        sl = slice(offs[k], offs[k + 1])
+        L = res[k]["box_length"]
+        d = dpg.Disk(n, L)
+        d.setState(fin["x"][sl], fin["y"][sl], None, None, sts[k]["r"], sts[k]["m"])
+        d.setupNeighbors("cell", CUT_MULT, 0.2, 8.0, 0.5)
+        r64 = dpg.minimizeFire(d, *JAM_FIRE)
+        f64_iters.append(int(r64["steps"]))
+        P64 = d.getPressure()
+        Z64 = d.getContactCount()
+        if band[0] <= P64 <= band[1] and Z64 > 2 * n:
+            n_ok += 1
+            dphi.append(0.0)
+        else:
+            rj = dpg.jamPressure(d, *band, compression_rate=1 - 1e-7, length_tolerance=1e-12,
+                                 decompress_factor=1 + 1e-7, max_compression_steps=2000,
+                                 fire=JAM_FIRE, neighbors=("cell", CUT_MULT, 0.2, 8.0, 0.5))
+            dphi.append(abs(rj["packing_fraction"] - res[k]["packing_fraction"]))
+            rejam.append({"system": k, "n": n, "pressure_fp64": P64, "contacts_fp64": Z64,
+                          "status": rj["status"], "dphi_J": dphi[-1]})
+        d.close()
+    t_check = time.perf_counter() - t1
+    # ---- plain FP64 drop-in on a seeded random sample, one system per call
+    order = np.random.default_rng(11).permutation(S)
+    plain_t, plain_done, plain_steps = 0.0, [], []
+    for k in order:
+        if plain_t >= plain_budget_s:
+            break
+        n = int(sizes[k])
+        d = dpg.Disk(n, sts[k]["box"])
+        d.setState(sts[k]["x"], sts[k]["y"], None, None, sts[k]["r"], sts[k]["m"])
+        d.setupNeighbors("cell", CUT_MULT, 0.2, 8.0, 0.5)
+        d.synchronize()
+        t2 = time.perf_counter()
+        rp = dpg.jamPressure(d, *band, fire=JAM_FIRE, neighbors=("cell", CUT_MULT, 0.2, 8.0, 0.5), **kw)
+        d.synchronize()
+        plain_t += time.perf_counter() - t2
+        plain_done.append(int(k))
+        plain_steps.append(int(rp["fire_steps_total"]))
+        d.close()
+    mixed_rate = S / t_mixed
+    plain_rate = len(plain_done) / plain_t if plain_t > 0 else None
+    steps = np.array([r["fire_steps"] for r in res])
+    status = [int(r["status"]) for r in res]
+    return {"workload": f"{S} bidisperse systems (radii 0.5/0.7), N log-uniform in [64, 4096] "
+                        f"(seed 2024, {int(sizes.sum())} disks), phi0 0.80, pressure band "
+                        f"{P:g} +- 1%, compression 0.99 / decompression 1.01 in box length, "
+                        "FIRE after every step to PE/N < 1e-16 or max|F| <= 1e-13 "
+                        "(at most 1e5 iterations)",
+            "pressure": P, "band": list(band),
+            "mixed_batched": {"form": "resident", "s": t_mixed, "systems_per_s": mixed_rate,
+                              "in_band": int(sum(band[0] <= r["pressure"] <= band[1] for r in res)),
+                              "status_counts": {str(v): status.count(v) for v in sorted(set(status))},
+                              "fire_iterations": {"mean": float(steps.mean()), "max": int(steps.max()),
+                                                  "sum": int(steps.sum())},
+                              "minimizations_max": int(max(r["minimizations"] for r in res)),
+                              "dw_share": float(sum(r["dw_steps"] for r in res) / steps.sum()),
+                              "fp64_passes": int(sum(r["fp64_steps"] for r in res))},
+            "fp64_check": {"systems": S, "confirmed_in_band": n_ok, "rejammed": rejam,
+                           "dphi_J_max": float(max(dphi)), "s": t_check,
+                           "fp64_fire_iterations_max": int(max(f64_iters))},
+            "plain_fp64": {"systems": len(plain_done), "s": plain_t, "systems_per_s": plain_rate,
+                           "sample": "a seeded random order of the systems, one per call, until "
+                                     f"{plain_budget_s:g} s of solving had passed",
+                           "sizes": [int(sizes[k]) for k in plain_done],
+                           "fire_iterations": plain_steps,
+                           "mixed_fire_iterations_same_systems": [int(steps[k]) for k in plain_done]},
+            "mixed_batched_over_plain_fp64": mixed_rate / plain_rate if plain_rate else None}
+
+
+def jam_ensemble(args):
+    """The jamming leg alone (any pressure, e.g. the 1e-7 of the workload's
+    definition): prints one JSON line."""
+    import dpcuda_gb300 as dpg
+    dpg.load_library()
+    out = jam_leg(dpg, args.jam_systems, args.jam_pressure, JAM_PLAIN_BUDGET_S)
+    print(json.dumps({"metric": "batched jamming: systems jammed/s, mixed+batched vs plain FP64",
+                      "unit": "systems/s", "value": out["mixed_batched"]["systems_per_s"],
+                      "n_gpus": 1, "higher_is_better": True, "detail": out}), flush=True)
 
 
 def fire_ensemble(args):
@@ -762,10 +933,10 @@ def main():
     ap.add_argument("--batch", type=int, default=BATCH, help="systems per step of the batched form")
     ap.add_argument("--jam-ensemble", action="store_true",
                     help="run the batched jamming workload instead of the default line")
-    ap.add_argument("--jam-systems", type=int, default=256)
-    ap.add_argument("--jam-max-compressions", type=int, default=2000)
-    ap.add_argument("--jam-pressure", type=float, default=1e-7,
+    ap.add_argument("--jam-systems", type=int, default=JAM_SYSTEMS)
+    ap.add_argument("--jam-pressure", type=float, default=JAM_PRESSURE,
                     help="target pressure of the batched jamming leg (band +-1%%)")
+    ap.add_argument("--no-jam", action="store_true", help="skip the jamming leg")
     ap.add_argument("--fire-ensemble", action="store_true",
                     help="run batched FIRE on an uneven ensemble instead of the default line")
     ap.add_argument("--fire-systems", type=int, default=256)

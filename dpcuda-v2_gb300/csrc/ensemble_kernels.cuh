@@ -77,6 +77,9 @@ struct ESys {
                              // it fails), 2 = final measurement of a finished minimisation
     double dw_scale;         // resident form: double-word exit at dw_scale * fmax_target
     double inv_n;            // 1 / n (the epilogue multiplies; FP64 division is slow)
+    int fprec;               // grid form: the arithmetic of this iteration's force pass
+                             // (set by the move, so a switch made by one force kernel
+                             // does not give the system a second pass in the other)
 };
 
 struct EParams {
@@ -417,6 +420,7 @@ __global__ void __launch_bounds__(kEB) e_move(EDev *e) {
                           : sys_reduce_t<1, double>(e, s, v, ops, &s.ticket_a, tot);
     if (last) {
         if (live) e_move_sys(e->p, s, tot[0]);
+        s.fprec = s.prec;
         if (s.rebuild && s.phase != kIdle) atomicAdd(&e->n_flagged, 1);
     }
     if (grid_last(e)) {
@@ -804,19 +808,23 @@ __device__ void e_finish(EDev *e, ESys &s, bool primary) {
 
 // Force pass of slot i (+ the kick unless setup): writes the forces and returns
 // its terms: 0 PE, 1 power, 2 |F|^2, 3 virial, 4 contacts, in vf (FP32 phase)
-// or v (refinement and FP64).
-__device__ __forceinline__ void e_force_one(EDev *e, const ESys &s, int i, bool setup,
-                                            double (&v)[5], float (&vf)[5]) {
+// or v (refinement and FP64).  PH: 0 = FP32 pairs only, 1 = double-word or FP64
+// pairs only (the split force kernels, each compiled without the other's
+// paths), -1 = whatever the system's precision says.
+template <int PH>
+__device__ __forceinline__ void e_force_one_t(EDev *e, const ESys &s, int i, bool setup,
+                                              double (&v)[5], float (&vf)[5]) {
     const EParams &p = e->p;
-    const bool f32 = s.prec == 0;
+    const int prec = PH == 0 ? 0 : (PH == 1 ? (s.prec == 2 ? 2 : 1) : s.prec);
+    const bool f32 = prec == 0;
     {
         const int T = p.T;
         int cnt = min(e->cnt[i], p.cap);
         double ax = 0.0, ay = 0.0, en = 0.0, wv = 0.0, nc = 0.0;
         const float4 a = e->pk[i];
-        if (s.prec != 1) {
+        if (prec != 1) {
             int ncount = 0;
-            if (s.prec == 0) {
+            if (prec == 0) {
                 // FP32 pair terms summed in FP32 over runs of 8 neighbours, FP64 across runs;
                 // the 8 indices and offsets of a run are loaded before any is used
                 const float ecf = (float)p.e_c, ncf = (float)p.n_c;
@@ -982,32 +990,44 @@ __device__ __forceinline__ void e_force_one(EDev *e, const ESys &s, int i, bool 
     }
 }
 
-// at most 102 registers, so 5 blocks (20 warps) fit an SM: measured 12 % faster
-// than the unbounded 108-register build on 16 x 16384 disks
-__global__ void __launch_bounds__(kEB, 5) e_force(EDev *e) {
+__device__ __forceinline__ void e_force_one(EDev *e, const ESys &s, int i, bool setup,
+                                            double (&v)[5], float (&vf)[5]) {
+    e_force_one_t<-1>(e, s, i, setup, v, vf);
+}
+
+// The force pass of the grid form, split by arithmetic: e_force_k<0> takes the
+// systems whose pass is FP32 (fprec 0), e_force_k<1> those in the double-word
+// refinement or FP64 (every block of the other systems leaves at once), so the
+// FP32 kernel carries only the FP32 path's registers (the combined kernel held
+// 102-108 registers a thread in every phase).  The second kernel sets the
+// transition node's condition.
+template <int PH>
+__global__ void __launch_bounds__(kEB, PH == 0 ? 6 : 5) e_force_k(EDev *e) {
     if (e->overflow) return;  // lists truncated: the host grows them and reruns this pass
     const int sid = e->blk_sys[blockIdx.x];
     ESys &s = e->sys[sid];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool live = s.phase != kIdle;
-    const bool setup = s.phase == kSetup;
-    // partials: 0 PE, 1 power, 2 max|F|^2, 3 virial, 4 contacts (FP32 block
-    // sums in the FP32 phase; FP64 in the refinement, whose energies are exact
-    // to ~1e-14 and are the ones reported)
-    const bool f32 = s.prec == 0;
-    double v[5] = {0, 0, 0, 0, 0};
-    float vf[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
-    if (live && i < s.off + s.n) e_force_one(e, s, i, setup, v, vf);
-    const int ops[5] = {0, 0, 1, 0, 0};
-    double tot[5];
-    const bool last = f32 ? sys_reduce_t<5, float>(e, s, vf, ops, &s.ticket_a, tot)
-                          : sys_reduce_t<5, double>(e, s, v, ops, &s.ticket_a, tot);
-    if (last && live) {
-        e_force_epilogue(e, s, tot, setup);
-        if (s.pending != kActNone) atomicAdd(&e->n_pending, 1);
+    const bool mine = (PH == 0) == (s.fprec == 0);
+    if (mine) {
+        const int i = blockIdx.x * blockDim.x + threadIdx.x;
+        const bool live = s.phase != kIdle;
+        const bool setup = s.phase == kSetup;
+        // partials: 0 PE, 1 power, 2 max|F|^2, 3 virial, 4 contacts (FP32 block
+        // sums in the FP32 phase; FP64 in the refinement, whose energies are exact
+        // to ~1e-14 and are the ones reported)
+        double v[5] = {0, 0, 0, 0, 0};
+        float vf[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+        if (live && i < s.off + s.n) e_force_one_t<PH>(e, s, i, setup, v, vf);
+        const int ops[5] = {0, 0, 1, 0, 0};
+        double tot[5];
+        const bool last = PH == 0 ? sys_reduce_t<5, float>(e, s, vf, ops, &s.ticket_a, tot)
+                                  : sys_reduce_t<5, double>(e, s, v, ops, &s.ticket_a, tot);
+        if (last && live) {
+            e_force_epilogue(e, s, tot, setup);
+            if (s.pending != kActNone) atomicAdd(&e->n_pending, 1);
+        }
     }
     // the transition pass (graph IF node) runs only when some system asked for one
-    if (grid_last(e) && e->h_tr) cudaGraphSetConditional(e->h_tr, e->n_pending > 0 ? 1u : 0u);
+    if (PH == 1 && grid_last(e) && e->h_tr) cudaGraphSetConditional(e->h_tr, e->n_pending > 0 ? 1u : 0u);
 }
 
 // ---- transitions between minimisations (save / restore / scale, FIRE reset) ----

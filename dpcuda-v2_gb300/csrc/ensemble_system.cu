@@ -231,6 +231,13 @@ static cudaGraphNode_t addk(cudaGraph_t g, cudaGraphNode_t dep, void *fn, int bl
     return node;
 }
 
+// the split force pass: FP32 systems, then refinement / FP64 systems
+static int enqueue_force(ES *s) {
+    LAUNCH(e_force_k<0>, s->nblocks, kEB, s->d);
+    LAUNCH(e_force_k<1>, s->nblocks, kEB, s->d);
+    return DPG_OK;
+}
+
 static int enqueue_rebuild(ES *s) {
     LAUNCH(e_cell_count, s->nblocks, kEB, s->d);
     LAUNCH(e_cell_scan, s->S, kEScanTPB, s->d);
@@ -243,7 +250,7 @@ static int enqueue_rebuild(ES *s) {
 static int enqueue_iteration(ES *s) {
     LAUNCH(e_move, s->nblocks, kEB, s->d);
     TRY(enqueue_rebuild(s));
-    LAUNCH(e_force, s->nblocks, kEB, s->d);
+    TRY(enqueue_force(s));
     LAUNCH(e_transition, s->nblocks, kEB, s->d);
     return DPG_OK;
 }
@@ -282,7 +289,8 @@ static int build_graph(ES *s) {
         prev = addk(ib, prev, (void *)e_cell_fill, s->nblocks, kEB, a, &err);
         prev = addk(ib, prev, (void *)e_cell_sort, (s->total_cells + 255) / 256, 256, a, &err);
         prev = addk(ib, prev, (void *)e_nlist, s->nblocks, kEB, a, &err);
-        last = addk(body, inode, (void *)e_force, s->nblocks, kEB, a, &err);
+        last = addk(body, inode, (void *)e_force_k<0>, s->nblocks, kEB, a, &err);
+        last = addk(body, last, (void *)e_force_k<1>, s->nblocks, kEB, a, &err);
         // IF(any system queued a transition) { e_transition }
         cudaGraphNodeParams tp = {};
         tp.type = cudaGraphNodeTypeConditional;
@@ -370,7 +378,7 @@ static int run(ES *s, long long guard_limit) {
             CK(cudaMemcpyAsync(s->d_sys, s->sys.data(), sizeof(ESys) * s->S, cudaMemcpyHostToDevice, s->stream));
             TRY(put(s, &s->d->n_flagged, 1));
             TRY(enqueue_rebuild(s));
-            LAUNCH(e_force, s->nblocks, kEB, s->d);
+            TRY(enqueue_force(s));
             LAUNCH(e_transition, s->nblocks, kEB, s->d);
             TRY(pull_dev(s, &cur));
             if (cur.overflow) continue;
@@ -654,6 +662,7 @@ static int prepare(ES *s, const dpg_fire_params *fp, int jam, const dpg_jam_para
         y.res_valid = 0;
         y.verify = 0;
         y.dw_scale = 0.9;
+        y.fprec = y.prec;
     }
     CK(cudaMemcpyAsync(s->d_sys, s->sys.data(), sizeof(ESys) * s->S, cudaMemcpyHostToDevice, s->stream));
     CK(cudaMemcpyAsync(&s->d->p, &p, sizeof(EParams), cudaMemcpyHostToDevice, s->stream));
@@ -725,12 +734,14 @@ extern "C" int dpg_ensemble_compute_forces(dpg_ensemble s, int precision, dpg_en
     const dpg_fire_params fp = {0.1, 1e-2, 0.0, 0.0, 1, 0.0};
     for (int attempt = 0; attempt < 8; attempt++) {
         TRY(prepare(s, &fp, 0, nullptr));
-        for (auto &y : s->sys)
+        for (auto &y : s->sys) {
             y.prec = y.ncd < 3 ? 1 : (precision == DPG_MIXED ? 0 : (precision == DPG_DWORD ? 2 : 1));
+            y.fprec = y.prec;
+        }
         CK(cudaMemcpyAsync(s->d_sys, s->sys.data(), sizeof(ESys) * s->S, cudaMemcpyHostToDevice, s->stream));
         TRY(put(s, &s->d->n_flagged, 1));
         TRY(enqueue_rebuild(s));
-        LAUNCH(e_force, s->nblocks, kEB, s->d);
+        TRY(enqueue_force(s));
         EDev cur;
         TRY(pull_dev(s, &cur));
         if (!cur.overflow) {
@@ -762,7 +773,7 @@ extern "C" int dpg_ensemble_profile_loop(dpg_ensemble s, const dpg_fire_params *
         cudaEventRecord(ev[5 * i + 1], s->stream);
         rc = enqueue_rebuild(s);
         cudaEventRecord(ev[5 * i + 2], s->stream);
-        LAUNCH(e_force, s->nblocks, kEB, s->d);
+        TRY(enqueue_force(s));
         cudaEventRecord(ev[5 * i + 3], s->stream);
         LAUNCH(e_transition, s->nblocks, kEB, s->d);
         cudaEventRecord(ev[5 * i + 4], s->stream);
