@@ -176,7 +176,8 @@ def test_autotune_restores_positions_and_picks_a_form(dpg):
     e = make(dpg, sts, dpg.MIXED)
     x0 = e.getState()["x"].copy()
     t = e.autotune(iters=100)
-    assert t["form"] in ("grid", "persist") and len(t["candidates"]) == 12
+    # 3 skins x (grid, persistent 128 / 256 / 512, resident)
+    assert t["form"] in ("grid", "persist", "resident") and len(t["candidates"]) == 15
     assert all(c["rate"] > 0 for c in t["candidates"])
     assert t["skin"] in {c["skin"] for c in t["candidates"]}
     np.testing.assert_array_equal(e.getState()["x"], x0)
