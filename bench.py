@@ -57,17 +57,27 @@ FORM_CODES = {"grid": 1, "persist": 2}
 SWITCH_FMAX = 1e-6          # mixed systems switch to FP64 pair forces below this max|F|
 PLAIN_SOLVES = 8            # timed solves of the plain FP64 path (after one untimed)
 E2E_BATCHES = 4             # timed batches solved again through host arrays (e2e)
-# jamming leg: the pressure band's centre in the default run (the workload's
-# 1e-7 takes tens of minutes per ensemble: single systems need 1e7-1e8 FIRE
-# iterations there; bench.py --jam-ensemble --jam-pressure 1e-7 runs it)
-JAM_SYSTEMS = 256
+# jamming leg of the default run: 64 systems drawn as the 256-system workload
+# draws them, at P = 1e-4 (at 1e-7 single systems need 1e7-1e8 FIRE iterations
+# and the ensemble takes tens of minutes; bench.py --jam-ensemble --jam-systems
+# 256 --jam-pressure 1e-7 runs it)
+JAM_SYSTEMS = 64
 JAM_PRESSURE = 1e-4
 JAM_PLAIN_BUDGET_S = 60.0
 JAM_FIRE = (0.1, 1e-2, 1e-16, 0.0, 100000, 1e-13)  # alpha0, dt0, PE/N target, no PE-change test,
                                                    # at most 1e5 iterations, max|F| target
+JAM_CHECK_STEPS = 20000     # FP64 re-minimisation of a jammed state (already a minimum)
 WARMUP_ITERS = 2000         # FIRE iterations of a warm-up solve
 E_FORCE_DRAM_PER_SYSTEM = 10.37e6 / 8  # ncu DRAM bytes per e_force launch per 16384-disk system
 PROFILE_ITERS = 300
+
+
+_T0 = time.perf_counter()
+
+
+def log(msg):
+    """Progress on stderr (the JSON line is the only stdout output)."""
+    print(f"[bench {time.perf_counter() - _T0:8.1f} s] {msg}", file=sys.stderr, flush=True)
 
 
 def step_seeds(rank, k):
@@ -293,6 +303,7 @@ def run_ours(args):
                       precision=dpg.MIXED, switch_fmax=SWITCH_FMAX, stream=sptr)
     te.setState(*[np.concatenate([st[c] for st in tune_sts]) for c in ("x", "y", "r", "m")])
     tune = te.autotune(TUNE_ITERS)
+    log("autotune done")
     te.close()
     skin = tune["skin"]
     form = FORM_CODES[tune["form"]]
@@ -318,6 +329,7 @@ def run_ours(args):
         e.setState(*[np.concatenate([st[c] for st in sts]) for c in ("x", "y", "r", "m")])
     torch.cuda.synchronize()
 
+    log("warm-up done, headline")
     # ---- headline: mixed precision, BATCH systems per step --------------------
     sampler = ClockSampler(dev.index or 0)
     results, ev_ms, launches = [], [], 0
@@ -347,6 +359,7 @@ def run_ours(args):
     ok = all(r["converged"] and r["max_force"] <= FMAX for r in flat)
     finals = [e.getState() for e, _ in batches]   # after the timed region
 
+    log("headline done, e2e")
     # ---- e2e: host arrays in, host positions/forces out, through the C ABI, on
     # the first E2E_BATCHES timed batches (the same starts, solved again) --------
     e2e_ms = []
@@ -365,27 +378,32 @@ def run_ours(args):
         e2e_ms.append(1e3 * (time.perf_counter() - t0))
     e2e_value = world * len(e2e_batches) * BATCH / (max_over_ranks(float(np.sum(e2e_ms))) / 1e3)
 
+    log("plain FP64 and batched FP64")
     # ---- the plain FP64 drop-in on the first PLAIN_SOLVES starts (one per call)
     # and the batched FP64 form on the same starts -----------------------------
     plain = plain_fp64_leg(dpg, sptr, batches[0][1][:PLAIN_SOLVES + 1], timed)
     batched64 = batched_fp64_leg(dpg, sptr, batches[0][1][1:PLAIN_SOLVES + 1], timed, form, tune)
 
+    log("FP64 re-check of the mixed minima")
     # ---- error of the mixed form: every timed minimum re-evaluated by the FP64
     # drop-in (bit-identical to the reference arithmetic; the forms reach
     # different minima from the same start, so the check is at the mixed form's
     # own final positions) ---------------------------------------------------------
     mixed_check = fp64_recheck(dpg, sptr, batches, finals, results)
 
+    log("roofline")
     # ---- roofline of the dominant kernel of the headline form, weighted over the
     # three arithmetics by the share of force passes each took -------------------
     peak, peak_src = measured_peak_hbm()
     roofline = headline_roofline(dpg, sptr, batches, finals, flat, plain["mean_neighbors"], peak,
                                  peak_src, tune)
 
+    log("large-N and other workloads")
     # ---- large-N force kernel (N = 2^20 NVE, plain FP64) -----------------------
     large = large_n_roofline(dpg, dev, sptr, peak)
     others = other_configs(dpg, sptr)
 
+    log("jamming leg")
     # ---- the jamming ensemble (256 uneven systems, pressure band) ---------------
     jam = None if args.no_jam else jam_leg(dpg, args.jam_systems, args.jam_pressure,
                                            JAM_PLAIN_BUDGET_S)
@@ -700,6 +718,7 @@ def jam_leg(dpg, S, P, plain_budget_s):
     import torch
     from dpcuda_gb300.ensemble import FORM_RESIDENT
     sizes, sts = jam_workload(S)
+    log(f"jamming: {S} systems ({int(sizes.sum())} disks) at P = {P:g}")
     band = (0.99 * P, 1.01 * P)
     kw = dict(compression_rate=0.99, length_tolerance=1e-10, decompress_factor=1.01,
               max_compression_steps=2000)
@@ -715,6 +734,7 @@ def jam_leg(dpg, S, P, plain_budget_s):
     res = e.jam(*band, fire=JAM_FIRE, **kw)
     torch.cuda.synchronize()
     t_mixed = time.perf_counter() - t0
+    log(f"jamming: mixed+batched {S} systems in {t_mixed:.1f} s")
     fin = e.getState()
     e.close()
     offs = np.concatenate([[0], np.cumsum(sizes)])
@@ -728,7 +748,7 @@ def jam_leg(dpg, S, P, plain_budget_s):
         d = dpg.Disk(n, L)
         d.setState(fin["x"][sl], fin["y"][sl], None, None, sts[k]["r"], sts[k]["m"])
         d.setupNeighbors("cell", CUT_MULT, 0.2, 8.0, 0.5)
-        r64 = dpg.minimizeFire(d, *JAM_FIRE)
+        r64 = dpg.minimizeFire(d, *JAM_FIRE[:4], JAM_CHECK_STEPS, JAM_FIRE[5])
         f64_iters.append(int(r64["steps"]))
         P64 = d.getPressure()
         Z64 = d.getContactCount()
@@ -744,6 +764,7 @@ def jam_leg(dpg, S, P, plain_budget_s):
                           "status": rj["status"], "dphi_J": dphi[-1]})
         d.close()
     t_check = time.perf_counter() - t1
+    log(f"jamming: FP64 check in {t_check:.1f} s")
     # ---- plain FP64 drop-in on a seeded random sample, one system per call
     order = np.random.default_rng(11).permutation(S)
     plain_t, plain_done, plain_steps = 0.0, [], []
@@ -762,6 +783,7 @@ def jam_leg(dpg, S, P, plain_budget_s):
         plain_done.append(int(k))
         plain_steps.append(int(rp["fire_steps_total"]))
         d.close()
+        log(f"jamming: plain FP64 system {k} (N={n}) done, {plain_t:.1f} s so far")
     mixed_rate = S / t_mixed
     plain_rate = len(plain_done) / plain_t if plain_t > 0 else None
     steps = np.array([r["fire_steps"] for r in res])
