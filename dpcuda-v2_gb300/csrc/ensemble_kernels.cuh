@@ -97,6 +97,10 @@ struct EParams {
     double p_low, p_high, compression_rate, length_tol, decompress;
     long long max_compressions;
     int res;                 // resident form: FP64 passes only verify double-word states
+    double fmax_cert2;       // (0.99 fmax_target)^2: an FP64 pass certifies max|F| with a 1 %
+                             // margin, so the reference arithmetic (IEEE division and square
+                             // root where these passes use Newton steps; ulp-level force
+                             // differences) also finds max|F| <= fmax_target
 };
 
 struct EDev {
@@ -121,6 +125,8 @@ struct EDev {
     unsigned ticket;
     long long guard, guard_limit;
     unsigned long long h_loop, h_rb, h_tr;
+    unsigned long long h_f32, h_fhi;  // graph IF nodes of the two force kernels
+    int n_f32, n_fhi;                 // live systems whose pass is FP32 / refinement or FP64
 };
 
 __device__ __forceinline__ int code_of(int cx, int cy) { return cx | (cy << 16); }
@@ -422,10 +428,16 @@ __global__ void __launch_bounds__(kEB) e_move(EDev *e) {
         if (live) e_move_sys(e->p, s, tot[0]);
         s.fprec = s.prec;
         if (s.rebuild && s.phase != kIdle) atomicAdd(&e->n_flagged, 1);
+        if (s.phase != kIdle) atomicAdd(s.prec == 0 ? &e->n_f32 : &e->n_fhi, 1);
     }
     if (grid_last(e)) {
         int any = e->n_flagged > 0;
         if (e->h_rb) cudaGraphSetConditional(e->h_rb, any ? 1u : 0u);
+        // launch only the force kernels some system needs this iteration
+        if (e->h_f32) cudaGraphSetConditional(e->h_f32, e->n_f32 > 0 ? 1u : 0u);
+        if (e->h_fhi) cudaGraphSetConditional(e->h_fhi, e->n_fhi > 0 ? 1u : 0u);
+        e->n_f32 = 0;
+        e->n_fhi = 0;
     }
 }
 
@@ -728,7 +740,7 @@ __device__ void e_force_epilogue(EDev *e, ESys &s, const double (&v)[5], bool se
     const bool pe_still = pe_dt > 0 && fabs(avg - s.last_avg_pe) < pe_dt * s.last_avg_pe;
     s.last_avg_pe = avg;
     if (avg < pe_t || (pass_prec == 1 && pe_still)) finished = true;
-    else if (p.fmax_target > 0 && f2 <= p.fmax_target * p.fmax_target && pass_prec == 1) finished = true;
+    else if (p.fmax_target > 0 && f2 <= p.fmax_cert2 && pass_prec == 1) finished = true;
     else if (it + 1 >= p.max_steps) finished = true;
     else {
         s.iter = it + 1;
@@ -1026,8 +1038,11 @@ __global__ void __launch_bounds__(kEB, PH == 0 ? 6 : 5) e_force_k(EDev *e) {
             if (s.pending != kActNone) atomicAdd(&e->n_pending, 1);
         }
     }
-    // the transition pass (graph IF node) runs only when some system asked for one
-    if (PH == 1 && grid_last(e) && e->h_tr) cudaGraphSetConditional(e->h_tr, e->n_pending > 0 ? 1u : 0u);
+}
+
+// sets the transition node's condition after the force kernels (one thread)
+__global__ void e_after_force(EDev *e) {
+    if (e->h_tr) cudaGraphSetConditional(e->h_tr, e->n_pending > 0 ? 1u : 0u);
 }
 
 // ---- transitions between minimisations (save / restore / scale, FIRE reset) ----

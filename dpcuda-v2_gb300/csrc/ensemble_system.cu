@@ -36,7 +36,7 @@ struct dpg_ensemble_system {
     double *xfer = nullptr;
     size_t n_total = 0;
     cudaGraphExec_t exec = nullptr;
-    cudaGraphConditionalHandle h_loop = 0, h_rb = 0, h_tr = 0;
+    cudaGraphConditionalHandle h_loop = 0, h_rb = 0, h_tr = 0, h_f32 = 0, h_fhi = 0;
     bool have_state = false;
     int mode = 2;
     int form = DPG_FORM_AUTO, pthreads = 0;  // execution form and persistent block size
@@ -235,6 +235,7 @@ static cudaGraphNode_t addk(cudaGraph_t g, cudaGraphNode_t dep, void *fn, int bl
 static int enqueue_force(ES *s) {
     LAUNCH(e_force_k<0>, s->nblocks, kEB, s->d);
     LAUNCH(e_force_k<1>, s->nblocks, kEB, s->d);
+    LAUNCH(e_after_force, 1, 1, s->d);
     return DPG_OK;
 }
 
@@ -270,6 +271,8 @@ static int build_graph(ES *s) {
     cudaGraph_t body = err == cudaSuccess ? wp.conditional.phGraph_out[0] : nullptr;
     if (err == cudaSuccess) err = cudaGraphConditionalHandleCreate(&s->h_rb, body, 0, 0);
     if (err == cudaSuccess) err = cudaGraphConditionalHandleCreate(&s->h_tr, body, 0, 0);
+    if (err == cudaSuccess) err = cudaGraphConditionalHandleCreate(&s->h_f32, body, 0, 0);
+    if (err == cudaSuccess) err = cudaGraphConditionalHandleCreate(&s->h_fhi, body, 0, 0);
     EDev *dp = s->d;
     void *a[] = {&dp};
     cudaGraphNode_t last = nullptr;
@@ -289,8 +292,23 @@ static int build_graph(ES *s) {
         prev = addk(ib, prev, (void *)e_cell_fill, s->nblocks, kEB, a, &err);
         prev = addk(ib, prev, (void *)e_cell_sort, (s->total_cells + 255) / 256, 256, a, &err);
         prev = addk(ib, prev, (void *)e_nlist, s->nblocks, kEB, a, &err);
-        last = addk(body, inode, (void *)e_force_k<0>, s->nblocks, kEB, a, &err);
-        last = addk(body, last, (void *)e_force_k<1>, s->nblocks, kEB, a, &err);
+        // IF(some system's pass is FP32) { e_force_k<0> }, IF(some refinement /
+        // FP64 pass) { e_force_k<1> }, then the transition condition
+        cudaGraphNode_t fprev = inode;
+        const cudaGraphConditionalHandle fh[2] = {s->h_f32, s->h_fhi};
+        void *fk[2] = {(void *)e_force_k<0>, (void *)e_force_k<1>};
+        for (int q = 0; q < 2 && err == cudaSuccess; q++) {
+            cudaGraphNodeParams fp = {};
+            fp.type = cudaGraphNodeTypeConditional;
+            fp.conditional.handle = fh[q];
+            fp.conditional.type = cudaGraphCondTypeIf;
+            fp.conditional.size = 1;
+            cudaGraphNode_t fnode = nullptr;
+            err = cudaGraphAddNode(&fnode, body, &fprev, nullptr, 1, &fp);
+            if (err == cudaSuccess) addk(fp.conditional.phGraph_out[0], nullptr, fk[q], s->nblocks, kEB, a, &err);
+            fprev = fnode;
+        }
+        last = addk(body, fprev, (void *)e_after_force, 1, 1, a, &err);
         // IF(any system queued a transition) { e_transition }
         cudaGraphNodeParams tp = {};
         tp.type = cudaGraphNodeTypeConditional;
@@ -348,10 +366,14 @@ static int run(ES *s, long long guard_limit) {
             TRY(put(s, &s->d->h_loop, (unsigned long long)s->h_loop));
             TRY(put(s, &s->d->h_rb, (unsigned long long)s->h_rb));
             TRY(put(s, &s->d->h_tr, (unsigned long long)s->h_tr));
+            TRY(put(s, &s->d->h_f32, (unsigned long long)s->h_f32));
+            TRY(put(s, &s->d->h_fhi, (unsigned long long)s->h_fhi));
             CK(cudaGraphLaunch(s->exec, s->stream));
             TRY(put(s, &s->d->h_loop, 0ULL));
             TRY(put(s, &s->d->h_rb, 0ULL));
             TRY(put(s, &s->d->h_tr, 0ULL));
+            TRY(put(s, &s->d->h_f32, 0ULL));
+            TRY(put(s, &s->d->h_fhi, 0ULL));
             ran = true;
         }
         if (!ran) {
@@ -642,6 +664,7 @@ static int prepare(ES *s, const dpg_fire_params *fp, int jam, const dpg_jam_para
     p.alpha0 = fp->alpha_init; p.dt0 = fp->dt;
     p.pe_target = fp->avg_pe_target; p.pe_diff_target = fp->avg_pe_diff_target;
     p.fmax_target = fp->fmax_target; p.max_steps = fp->max_steps;
+    p.fmax_cert2 = (0.99 * fp->fmax_target) * (0.99 * fp->fmax_target);
     p.jam = jam;
     p.res = res;
     if (jp) {

@@ -491,7 +491,7 @@ __device__ void res_verify_epilogue(EDev *e, ESys &s, const double (&v)[5], int 
     s.fp64_total++;
     const double avg = v[0] * s.inv_n;
     const double pe_t = (p.jam && s.jam_stage == 0) ? 1e-16 : p.pe_target;
-    if (kind == 2 || avg < pe_t || (p.fmax_target > 0 && v[2] <= p.fmax_target * p.fmax_target)) {
+    if (kind == 2 || avg < pe_t || (p.fmax_target > 0 && v[2] <= p.fmax_cert2)) {
         s.pe = v[0];
         s.power = v[1];
         s.fmax2 = v[2];
