@@ -401,6 +401,11 @@ def run_ours(args):
     log("large-N and other workloads")
     # ---- large-N force kernel (N = 2^20 NVE, plain FP64) -----------------------
     large = large_n_roofline(dpg, dev, sptr, peak)
+    fma = fma_peaks(dpg)
+    # the FP64 force + kick kernel is bound by the FP64 pipe (ncu: pipe
+    # utilisation in profiles/); its denominator is the measured DFMA rate
+    large["fp64"]["fp64_pipe"] = {"peak_tflops": fma["fp64"]["tflops"], "peak_source":
+                                  "dpg_measure_fma_peak (measured DFMA rate)"}
     others = other_configs(dpg, sptr)
 
     log("jamming leg")
@@ -441,6 +446,7 @@ def run_ours(args):
                           "mixed_batched_over_batched_fp64": value / batched64["value"],
                           "jam_ensemble": jam,
                           "roofline_large": large, "other_workloads": others,
+                          "fma_peaks_measured": fma,
                           "autotune": {"chosen": {"form": tune["form"], "threads": tune["threads"],
                                                   "skin": tune["skin"]},
                                        "iters_per_candidate": TUNE_ITERS,
@@ -648,6 +654,17 @@ def profile(dpg, s, kind, iters, dt=1e-2):
     dpg.lib.check(s.lib.dpg_profile_loop(s.h, kind, iters, dt, avg, cnt))
     return {"move_us": avg[0], "rebuild_us": avg[1], "force_us": avg[2], "iters": cnt[0],
             "list_builds": cnt[1], "cell_builds": cnt[2]}
+
+
+def fma_peaks(dpg):
+    """Measured FP64 and FP32 FMA throughput (dpg_measure_fma_peak), TFLOP/s."""
+    import ctypes as C
+    out = {}
+    for name, fp64, iters in (("fp64", 1, 1 << 12), ("fp32", 0, 1 << 16)):
+        tf, ms = C.c_double(), C.c_double()
+        dpg.lib.check(dpg.load_library().dpg_measure_fma_peak(fp64, iters, C.byref(tf), C.byref(ms)))
+        out[name] = {"tflops": tf.value, "launch_ms": ms.value}
+    return out
 
 
 def large_n_roofline(dpg, dev, sptr, peak):

@@ -27,6 +27,7 @@ UNITS = [
     ("bumpy_system.cu", ["--fmad=false"]),
     ("ensemble_system.cu", []),
     ("noalloc.cu", ["--fmad=false"]),
+    ("peaks.cu", []),
     ("jam.cpp", []),
     ("state_io.cpp", []),
 ]

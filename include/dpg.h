@@ -614,6 +614,13 @@ int dpg_profile_loop(dpg_handle h, int kind, int iters, double dt, double *avg_u
 int dpg_ensemble_profile_loop(dpg_ensemble e, const dpg_fire_params *p, int iters, double *avg_us,
                               int64_t *counts);
 
+/* Measured multiply-add throughput of the current GPU (no reference
+ * counterpart; the roofline denominator of arithmetic-bound kernels): fp64 = 1
+ * for the FP64 pipe, 0 for FP32; `iters` rounds of 8 independent FMA chains
+ * per thread over 8 blocks of 256 threads per SM, one launch timed with CUDA
+ * events.  *tflops = 2 x FMAs / time; *ms (nullable) = the launch's time. */
+int dpg_measure_fma_peak(int fp64, int iters, double *tflops, double *ms);
+
 /* ---- forces without device allocation --------------------------------- */
 /* No counterpart in the reference.  Harmonic forces fx, fy and per-particle
  * energies pe of n disks (device arrays, any order, square box of side
