@@ -906,8 +906,9 @@ def ncu_case(which):
     """Small fixed workloads for ncu captures (plain stream launches, a few
     hundred kernels): 'fire' = 64 FIRE iterations of the 16384-disk system,
     'nve_large' = 8 NVE steps of the 2^20-disk system, 'ensemble' = 64 FIRE
-    iterations of the batched mixed form on 8 x 16384 disks, 'bumpy_nve' = 192
-    NVE steps of 4096 rigid bumpy bodies."""
+    iterations of the batched mixed form on 16 x 16384 disks, 'bumpy_nve' =
+    192 NVE steps of 4096 rigid bumpy bodies, 'resident' = 3000 FIRE
+    iterations of 16 uneven systems in the resident form."""
     os.environ["DPG_LOOP_MODE"] = "stream"
     import dpcuda_gb300 as dpg
     if which == "bumpy_nve":
@@ -924,6 +925,19 @@ def ncu_case(which):
         r.nveSteps(5e-3, 64)
         r.nveSteps(5e-3, 128)
         print(json.dumps({"ncu_case": which, "n_rebuilds": r.neighborInfo()["n_rebuilds"]}))
+        return
+    if which == "resident":
+        # the jamming leg's first 16 systems (64-4096 disks), FIRE from their starts
+        # for at most 3000 iterations in the resident form (time-sliced launches,
+        # one per size class)
+        from dpcuda_gb300.ensemble import FORM_RESIDENT
+        sizes, sts = jam_workload(16)
+        e = dpg.Ensemble(sizes, [st["box"] for st in sts], CUTOFF, SKIN, precision=dpg.MIXED,
+                         switch_fmax=SWITCH_FMAX)
+        e.setForm(FORM_RESIDENT)
+        e.setState(*[np.concatenate([st[c] for st in sts]) for c in ("x", "y", "r", "m")])
+        r = e.minimizeFire(FIRE_ALPHA0, FIRE_DT0, 0.0, 0.0, 3000, fmax_target=FMAX)
+        print(json.dumps({"ncu_case": which, "steps": max(x["fire_steps"] for x in r)}))
         return
     if which == "ensemble_forces":
         # one force pass per arithmetic (FP32, double-word, FP64) on 8 x 16384 disks
@@ -973,7 +987,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--ncu-case", choices=["fire", "nve_large", "ensemble", "ensemble_forces",
-                                           "bumpy_nve"],
+                                           "bumpy_nve", "resident"],
                     default=None,
                     help="run a small fixed workload for ncu captures and exit")
     ap.add_argument("--batch", type=int, default=BATCH, help="systems per step of the batched form")
