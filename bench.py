@@ -63,7 +63,7 @@ E2E_BATCHES = 4             # timed batches solved again through host arrays (e2
 # 256 --jam-pressure 1e-7 runs it)
 JAM_SYSTEMS = 64
 JAM_PRESSURE = 1e-4
-JAM_PLAIN_BUDGET_S = 60.0
+JAM_PLAIN_BUDGET_S = 120.0
 JAM_FIRE = (0.1, 1e-2, 1e-16, 0.0, 100000, 1e-13)  # alpha0, dt0, PE/N target, no PE-change test,
                                                    # at most 1e5 iterations, max|F| target
 JAM_CHECK_STEPS = 20000     # FP64 re-minimisation of a jammed state (already a minimum)
@@ -782,10 +782,13 @@ def jam_leg(dpg, S, P, plain_budget_s):
             dpg.minimizeFire(d, *JAM_FIRE[:4], JAM_CHECK_STEPS, JAM_FIRE[5])
             P1, phi1 = d.getPressure(), d.getPackingFraction()
             slope = (P1 - P64) / (phi1 - phi0)
-            phi_fp64 = phi0 + (P - P64) / slope if slope > 0 else float("nan")
-            dphi.append(abs(phi_fp64 - res[k]["packing_fraction"]))
+            # a non-positive slope: the FP64 minimisations did not settle within
+            # JAM_CHECK_STEPS (the mixed run's last minimisation stopped at its cap)
+            phi_fp64 = phi0 + (P - P64) / slope if slope > 0 else None
+            dphi.append(abs(phi_fp64 - res[k]["packing_fraction"]) if phi_fp64 is not None else None)
             rejam.append({"system": k, "n": n, "pressure_fp64": P64, "contacts_fp64": Z64,
-                          "phi_J_fp64": phi_fp64, "dphi_J": dphi[-1]})
+                          "phi_J_fp64": phi_fp64, "dphi_J": dphi[-1],
+                          "mixed_fire_iterations": int(res[k]["fire_steps"])})
         d.close()
     t_check = time.perf_counter() - t1
     log(f"jamming: FP64 check in {t_check:.1f} s")
@@ -810,6 +813,13 @@ def jam_leg(dpg, S, P, plain_budget_s):
         log(f"jamming: plain FP64 system {k} (N={n}) done, {plain_t:.1f} s so far")
     mixed_rate = S / t_mixed
     plain_rate = len(plain_done) / plain_t if plain_t > 0 else None
+    # projection over all S systems: the plain path's measured time per FIRE
+    # iteration times the mixed run's iterations, scaled by the plain / mixed
+    # iteration ratio on the sampled systems
+    steps_all = float(sum(r["fire_steps"] for r in res))
+    mixed_same = float(sum(res[k]["fire_steps"] for k in plain_done))
+    t_it = plain_t / max(1, sum(plain_steps))
+    proj_t = t_it * steps_all * (sum(plain_steps) / mixed_same) if mixed_same > 0 else None
     steps = np.array([r["fire_steps"] for r in res])
     status = [int(r["status"]) for r in res]
     return {"workload": f"{S} bidisperse systems (radii 0.5/0.7), N log-uniform in [64, 4096] "
@@ -827,7 +837,8 @@ def jam_leg(dpg, S, P, plain_budget_s):
                               "dw_share": float(sum(r["dw_steps"] for r in res) / steps.sum()),
                               "fp64_passes": int(sum(r["fp64_steps"] for r in res))},
             "fp64_check": {"systems": S, "confirmed_in_band": n_ok, "linearised_rejam": rejam,
-                           "dphi_J_max": float(max(dphi)), "s": t_check,
+                           "dphi_J_max": float(max(v for v in dphi if v is not None)),
+                           "unresolved": int(sum(v is None for v in dphi)), "s": t_check,
                            "fp64_fire_iterations_max": int(max(f64_iters))},
             "plain_fp64": {"systems": len(plain_done), "s": plain_t, "systems_per_s": plain_rate,
                            "sample": "a seeded random order of the systems, one per call, until "
@@ -835,7 +846,13 @@ def jam_leg(dpg, S, P, plain_budget_s):
                            "sizes": [int(sizes[k]) for k in plain_done],
                            "fire_iterations": plain_steps,
                            "mixed_fire_iterations_same_systems": [int(steps[k]) for k in plain_done]},
-            "mixed_batched_over_plain_fp64": mixed_rate / plain_rate if plain_rate else None}
+            "plain_fp64_projected": {"systems_per_s": S / proj_t if proj_t else None,
+                                     "us_per_fire_iteration": 1e6 * t_it,
+                                     "basis": "measured time per FIRE iteration of the sampled "
+                                              "systems x the mixed run's iterations of all systems "
+                                              "x the sampled plain / mixed iteration ratio"},
+            "mixed_batched_over_plain_fp64": mixed_rate / plain_rate if plain_rate else None,
+            "mixed_batched_over_plain_fp64_projected": mixed_rate * proj_t / S if proj_t else None}
 
 
 def jam_ensemble(args):
