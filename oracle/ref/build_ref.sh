@@ -3,15 +3,15 @@
 # (mmccraw98/dpCUDA-v2 src/particles/{base,disk,rigid_bumpy}/kernels.cu, read in
 # place, never copied) compiled as host C++ through shim/, linked with
 # ref_driver.cpp / ref_bumpy_driver.cpp.  TEST INFRASTRUCTURE ONLY: used to pin
-# the oracle and to generate tests/golden fixtures.  Needs the reference tree
-# (default /root/reference, override with DPG_REFERENCE); exits 0 without
-# building when it is absent.
+# the oracle and to generate tests/golden fixtures.  Needs the reference tree,
+# named by DPG_REFERENCE; exits 0 without building when that is unset or the
+# tree is absent.
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
-REF="${DPG_REFERENCE:-/root/reference}"
+REF="${DPG_REFERENCE:-}"
 OUT="$HERE/../_ref"
-if [ ! -d "$REF/src/particles" ]; then
-  echo "reference tree not found at $REF; oracle/_ref not built"
+if [ -z "$REF" ] || [ ! -d "$REF/src/particles" ]; then
+  echo "DPG_REFERENCE does not name the reference tree; oracle/_ref not built"
   exit 0
 fi
 mkdir -p "$OUT"
