@@ -30,6 +30,52 @@ def partition_systems(n_particles, world):
         parts[r].append(k)
         loads[r] += n[k]
     return [sorted(p) for p in parts]
+def solve_partitioned(n_particles, solve, group=None):
+    """Independent systems over the ranks of a torch.distributed group (one
+    GPU per rank; no exchange on the data path): every rank computes the same
+    partition_systems assignment, solves its own share with
+    solve(indices) -> list of per-system results (in the order of indices),
+    and rank 0 gathers the results in input order.  Returns that list on rank
+    0 and None on the others; without an initialised process group the caller
+    is the only rank and solves every system."""
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()):
+        return list(solve(list(range(len(n_particles)))))
+    world, rank = dist.get_world_size(group), dist.get_rank(group)
+    mine = partition_systems(n_particles, world)[rank]
+    res = list(solve(mine)) if mine else []
+    if len(res) != len(mine):
+        raise ValueError("solve() must return one result per system index")
+    gathered = [None] * world if rank == 0 else None
+    dist.gather_object(list(zip(mine, res)), gathered, dst=0, group=group)
+    if rank != 0:
+        return None
+    out = [None] * len(n_particles)
+    for part in gathered:
+        for k, r in part:
+            out[k] = r
+    return out
+
+
+def ensemble_solver(n_particles, boxes, states, mode="fire", precision=MIXED, cutoff=1.7,
+                    skin=0.3, switch_fmax=1e-6, stream=None, **params):
+    """A solve() for solve_partitioned on this rank's GPU: the given systems
+    as one Ensemble (states[k] = dict with x, y, r, m), minimised by FIRE
+    (mode "fire", params as Ensemble.minimizeFire) or jammed (mode "jam",
+    params as Ensemble.jam)."""
+    def solve(indices):
+        if not indices:
+            return []
+        e = Ensemble([n_particles[k] for k in indices], [boxes[k] for k in indices], cutoff, skin,
+                     precision=precision, switch_fmax=switch_fmax, stream=stream)
+        try:
+            e.setState(*[np.concatenate([states[k][c] for k in indices]) for c in ("x", "y", "r", "m")])
+            return e.jam(**params) if mode == "jam" else e.minimizeFire(**params)
+        finally:
+            e.close()
+    return solve
+
+
 FORM_AUTO, FORM_GRID, FORM_PERSIST, FORM_RESIDENT = 0, 1, 2, 3
 _FORM_NAMES = {FORM_GRID: "grid", FORM_PERSIST: "persist", FORM_RESIDENT: "resident"}
 

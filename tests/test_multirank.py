@@ -95,3 +95,62 @@ def test_partition_is_consistent_across_ranks(tmp_path):
         port = sk.getsockname()[1]
     torch.multiprocessing.spawn(_partition_rank, args=(2, port, str(tmp_path)), nprocs=2, join=True)
     assert (tmp_path / "parts.txt").read_text().startswith("True")
+
+
+def _oracle_fire(indices, sts):
+    """CPU stand-in for a rank's GPU: each system minimised by the oracle."""
+    from oracle.oracle import DiskOracle
+    out = []
+    for k in indices:
+        st = sts[k]
+        o = DiskOracle(len(st["r"]), st["box"])
+        o.set_arrays(x=st["x"], y=st["y"], r=st["r"], m=st["m"])
+        o.setup_neighbors(0, 1.7 / 1.4, 0.2, 8.0, 0.5)
+        steps, _ = o.minimize_fire(0.1, 1e-2, 0.0, 0.0, 3000, 1e-10)
+        out.append({"steps": int(steps), "avg_pe": o.total_pe() / len(st["r"]),
+                    "max_force": o.max_force()})
+        o.close()
+    return out
+
+
+SOLVE_SIZES = [64, 300, 150, 90, 200, 120, 64, 250]
+
+
+def _solve_rank(rank, world, port, out_dir):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank),
+                      WORLD_SIZE=str(world), LOCAL_RANK=str(rank))
+    sys.path[:0] = [str(ROOT), str(ROOT / "dpcuda-v2_gb300")]
+    import json
+    import torch.distributed as dist
+    from dpcuda_gb300.ensemble import solve_partitioned
+    from oracle.oracle import disk_packing
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    sts = [disk_packing(n, 0.86, 500 + k) for k, n in enumerate(SOLVE_SIZES)]
+    res = solve_partitioned(SOLVE_SIZES, lambda idx: _oracle_fire(idx, sts))
+    if rank == 0:
+        Path(out_dir, "gathered.json").write_text(json.dumps(res))
+    else:
+        Path(out_dir, f"rank{rank}.json").write_text(json.dumps(res))
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_partitioned_solve_gathers_the_single_rank_results(tmp_path):
+    """Two ranks each solve their share of uneven systems (the oracle standing
+    in for a rank's GPU); rank 0 gathers every system's result in input order,
+    equal to one rank solving them all."""
+    torch = pytest.importorskip("torch")
+    import json
+    import socket
+    sys.path[:0] = [str(ROOT), str(ROOT / "dpcuda-v2_gb300")]
+    from dpcuda_gb300.ensemble import solve_partitioned
+    from oracle.oracle import disk_packing
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    torch.multiprocessing.spawn(_solve_rank, args=(2, port, str(tmp_path)), nprocs=2, join=True)
+    gathered = json.loads((tmp_path / "gathered.json").read_text())
+    assert json.loads((tmp_path / "rank1.json").read_text()) is None
+    sts = [disk_packing(n, 0.86, 500 + k) for k, n in enumerate(SOLVE_SIZES)]
+    single = solve_partitioned(SOLVE_SIZES, lambda idx: _oracle_fire(idx, sts))
+    assert gathered == single
