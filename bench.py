@@ -63,7 +63,7 @@ E2E_BATCHES = 4             # timed batches solved again through host arrays (e2
 # 256 --jam-pressure 1e-7 runs it)
 JAM_SYSTEMS = 64
 JAM_PRESSURE = 1e-4
-JAM_PLAIN_BUDGET_S = 120.0
+JAM_PLAIN_BUDGET_S = 60.0
 JAM_FIRE = (0.1, 1e-2, 1e-16, 0.0, 100000, 1e-13)  # alpha0, dt0, PE/N target, no PE-change test,
                                                    # at most 1e5 iterations, max|F| target
 JAM_CHECK_STEPS = 20000     # FP64 re-minimisation of a jammed state (already a minimum)

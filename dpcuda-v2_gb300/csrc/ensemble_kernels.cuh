@@ -1013,12 +1013,13 @@ __device__ __forceinline__ void e_force_one(EDev *e, const ESys &s, int i, bool 
 // FP32 kernel carries only the FP32 path's registers (the combined kernel held
 // 102-108 registers a thread in every phase).  The second kernel sets the
 // transition node's condition.
+// PH = -1: one kernel for every arithmetic (the systems' own precision).
 template <int PH>
 __global__ void __launch_bounds__(kEB, PH == 0 ? 6 : 5) e_force_k(EDev *e) {
     if (e->overflow) return;  // lists truncated: the host grows them and reruns this pass
     const int sid = e->blk_sys[blockIdx.x];
     ESys &s = e->sys[sid];
-    const bool mine = (PH == 0) == (s.fprec == 0);
+    const bool mine = PH < 0 || ((PH == 0) == (s.fprec == 0));
     if (mine) {
         const int i = blockIdx.x * blockDim.x + threadIdx.x;
         const bool live = s.phase != kIdle;
@@ -1031,8 +1032,9 @@ __global__ void __launch_bounds__(kEB, PH == 0 ? 6 : 5) e_force_k(EDev *e) {
         if (live && i < s.off + s.n) e_force_one_t<PH>(e, s, i, setup, v, vf);
         const int ops[5] = {0, 0, 1, 0, 0};
         double tot[5];
-        const bool last = PH == 0 ? sys_reduce_t<5, float>(e, s, vf, ops, &s.ticket_a, tot)
-                                  : sys_reduce_t<5, double>(e, s, v, ops, &s.ticket_a, tot);
+        const bool f32 = PH == 0 || (PH < 0 && s.fprec == 0);
+        const bool last = f32 ? sys_reduce_t<5, float>(e, s, vf, ops, &s.ticket_a, tot)
+                              : sys_reduce_t<5, double>(e, s, v, ops, &s.ticket_a, tot);
         if (last && live) {
             e_force_epilogue(e, s, tot, setup);
             if (s.pending != kActNone) atomicAdd(&e->n_pending, 1);

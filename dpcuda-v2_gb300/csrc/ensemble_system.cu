@@ -41,6 +41,7 @@ struct dpg_ensemble_system {
     int mode = 2;
     int form = DPG_FORM_AUTO, pthreads = 0;  // execution form and persistent block size
     int max_n = 0;
+    bool split_force = true;     // grid form: FP32 and refinement force kernels apart
     // resident form: one stream per size class, the block -> system lists
     cudaStream_t rs_stream[8] = {};
     cudaEvent_t rs_fork = nullptr, rs_join[8] = {};
@@ -108,6 +109,10 @@ extern "C" int dpg_ensemble_create(const dpg_ensemble_params *p, const int64_t *
     if (f && !strcmp(f, "grid")) s->form = DPG_FORM_GRID;
     if (f && !strcmp(f, "persist")) s->form = DPG_FORM_PERSIST;
     if (f && !strcmp(f, "resident")) s->form = DPG_FORM_RESIDENT;
+    // DPG_FORCE_SPLIT=0: the grid form's force pass as one kernel for every
+    // arithmetic instead of two kernels under IF nodes (a tuning knob)
+    const char *fs = getenv("DPG_FORCE_SPLIT");
+    if (fs && !strcmp(fs, "0")) s->split_force = false;
     // layout: each system padded to whole blocks; its own cell grid
     s->sys.assign(s->S, ESys{});
     int slot = 0, blk = 0, cell = 0, item = 0;
@@ -233,8 +238,12 @@ static cudaGraphNode_t addk(cudaGraph_t g, cudaGraphNode_t dep, void *fn, int bl
 
 // the split force pass: FP32 systems, then refinement / FP64 systems
 static int enqueue_force(ES *s) {
-    LAUNCH(e_force_k<0>, s->nblocks, kEB, s->d);
-    LAUNCH(e_force_k<1>, s->nblocks, kEB, s->d);
+    if (s->split_force) {
+        LAUNCH(e_force_k<0>, s->nblocks, kEB, s->d);
+        LAUNCH(e_force_k<1>, s->nblocks, kEB, s->d);
+    } else {
+        LAUNCH(e_force_k<-1>, s->nblocks, kEB, s->d);
+    }
     LAUNCH(e_after_force, 1, 1, s->d);
     return DPG_OK;
 }
@@ -297,7 +306,8 @@ static int build_graph(ES *s) {
         cudaGraphNode_t fprev = inode;
         const cudaGraphConditionalHandle fh[2] = {s->h_f32, s->h_fhi};
         void *fk[2] = {(void *)e_force_k<0>, (void *)e_force_k<1>};
-        for (int q = 0; q < 2 && err == cudaSuccess; q++) {
+        if (!s->split_force) fprev = addk(body, inode, (void *)e_force_k<-1>, s->nblocks, kEB, a, &err);
+        for (int q = 0; q < 2 && err == cudaSuccess && s->split_force; q++) {
             cudaGraphNodeParams fp = {};
             fp.type = cudaGraphNodeTypeConditional;
             fp.conditional.handle = fh[q];
