@@ -956,6 +956,31 @@ def ncu_case(which):
         r = e.minimizeFire(FIRE_ALPHA0, FIRE_DT0, 0.0, 0.0, 3000, fmax_target=FMAX)
         print(json.dumps({"ncu_case": which, "steps": max(x["fire_steps"] for x in r)}))
         return
+    if which in ("resident_dw_small", "resident_dw_large"):
+        # S systems of N disks relaxed to max|F| <= 1e-9, then 1000 FIRE
+        # iterations in the double-word phase inside an NVTX range "dw" (the
+        # capture filters on it): 48 x 128 disks (lanes per particle) or 8 x
+        # 4096 disks (8-block clusters)
+        import torch
+        from dpcuda_gb300.ensemble import FORM_RESIDENT
+        from dpcuda_gb300.init import disk_packing
+        N, S = (128, 48) if which.endswith("small") else (4096, 8)
+        sts = [disk_packing(N, 0.86, 700 + k) for k in range(S)]
+        cat = [np.concatenate([st[c] for st in sts]) for c in ("x", "y", "r", "m")]
+        e = dpg.Ensemble([N] * S, [st["box"] for st in sts], CUTOFF, SKIN, precision=dpg.MIXED,
+                         switch_fmax=SWITCH_FMAX)
+        e.setForm(FORM_RESIDENT)
+        e.setState(*cat)
+        e.minimizeFire(FIRE_ALPHA0, FIRE_DT0, 0.0, 0.0, 30000, fmax_target=1e-9)
+        fin = e.getState()
+        e.setState(fin["x"], fin["y"], cat[2], cat[3])
+        torch.cuda.nvtx.range_push("dw")
+        r = e.minimizeFire(FIRE_ALPHA0, FIRE_DT0, 0.0, 0.0, 1000, fmax_target=1e-15)
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
+        print(json.dumps({"ncu_case": which, "steps": max(x["fire_steps"] for x in r),
+                          "dw_steps": float(np.mean([x["dw_steps"] for x in r]))}))
+        return
     if which == "ensemble_forces":
         # one force pass per arithmetic (FP32, double-word, FP64) on 8 x 16384 disks
         from dpcuda_gb300.ensemble import DWORD
@@ -1004,7 +1029,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--ncu-case", choices=["fire", "nve_large", "ensemble", "ensemble_forces",
-                                           "bumpy_nve", "resident"],
+                                           "bumpy_nve", "resident", "resident_dw_small",
+                                           "resident_dw_large"],
                     default=None,
                     help="run a small fixed workload for ncu captures and exit")
     ap.add_argument("--batch", type=int, default=BATCH, help="systems per step of the batched form")
