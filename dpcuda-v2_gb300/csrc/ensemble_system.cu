@@ -280,8 +280,9 @@ static int build_graph(ES *s) {
     cudaGraph_t body = err == cudaSuccess ? wp.conditional.phGraph_out[0] : nullptr;
     if (err == cudaSuccess) err = cudaGraphConditionalHandleCreate(&s->h_rb, body, 0, 0);
     if (err == cudaSuccess) err = cudaGraphConditionalHandleCreate(&s->h_tr, body, 0, 0);
-    if (err == cudaSuccess) err = cudaGraphConditionalHandleCreate(&s->h_f32, body, 0, 0);
-    if (err == cudaSuccess) err = cudaGraphConditionalHandleCreate(&s->h_fhi, body, 0, 0);
+    s->h_f32 = s->h_fhi = 0;
+    if (err == cudaSuccess && s->split_force) err = cudaGraphConditionalHandleCreate(&s->h_f32, body, 0, 0);
+    if (err == cudaSuccess && s->split_force) err = cudaGraphConditionalHandleCreate(&s->h_fhi, body, 0, 0);
     EDev *dp = s->d;
     void *a[] = {&dp};
     cudaGraphNode_t last = nullptr;
