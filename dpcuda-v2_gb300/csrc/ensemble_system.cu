@@ -388,6 +388,7 @@ static int run(ES *s, long long guard_limit) {
             ran = true;
         }
         if (!ran) {
+            (void)cudaGetLastError();  // a failed graph build leaves its error behind
             s->mode = 0;
             for (long long it = 0; it < guard_limit; it++) {
                 TRY(enqueue_iteration(s));
