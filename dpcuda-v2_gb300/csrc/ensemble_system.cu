@@ -41,7 +41,7 @@ struct dpg_ensemble_system {
     int mode = 2;
     int form = DPG_FORM_AUTO, pthreads = 0;  // execution form and persistent block size
     int max_n = 0;
-    bool split_force = true;     // grid form: FP32 and refinement force kernels apart
+    bool split_force = false;    // grid form: FP32 and refinement force kernels apart
     // resident form: one stream per size class, the block -> system lists
     cudaStream_t rs_stream[8] = {};
     cudaEvent_t rs_fork = nullptr, rs_join[8] = {};
@@ -109,10 +109,13 @@ extern "C" int dpg_ensemble_create(const dpg_ensemble_params *p, const int64_t *
     if (f && !strcmp(f, "grid")) s->form = DPG_FORM_GRID;
     if (f && !strcmp(f, "persist")) s->form = DPG_FORM_PERSIST;
     if (f && !strcmp(f, "resident")) s->form = DPG_FORM_RESIDENT;
-    // DPG_FORCE_SPLIT=0: the grid form's force pass as one kernel for every
-    // arithmetic instead of two kernels under IF nodes (a tuning knob)
+    // DPG_FORCE_SPLIT=1: the grid form's force pass as two kernels under IF
+    // nodes (FP32 systems; refinement / FP64 systems) instead of one kernel for
+    // every arithmetic.  Measured on 16 x 16384 disks, the split costs 6-8 % per
+    // iteration (FP32 phase 98 vs 92 us, double-word 112 vs 104 us): the FP32
+    // kernel's 80 registers (against 102) do not pay for the extra nodes.
     const char *fs = getenv("DPG_FORCE_SPLIT");
-    if (fs && !strcmp(fs, "0")) s->split_force = false;
+    if (fs && !strcmp(fs, "1")) s->split_force = true;
     // layout: each system padded to whole blocks; its own cell grid
     s->sys.assign(s->S, ESys{});
     int slot = 0, blk = 0, cell = 0, item = 0;
@@ -440,11 +443,13 @@ struct RClass {
 // the largest (N = 4096 alone: 18.8 vs 30.0 us on 4 blocks of 4 particles per
 // thread), 2 particles per thread where many large systems share the GPU
 // (N = 2048, 48 systems: 24.9 vs 30.6 us).
-constexpr int kNClass = 7;
+// The last class holds up to 16384 disks: 8-block clusters of 512 threads x 4
+// particles (2048 disks and ~146 KB of shared memory a block).
+constexpr int kNClass = 8;
 #define RC(NT, PPT, C, G) {NT, PPT, C, G, e_res<NT, PPT, C, G>}
 static const RClass kRClasses[kNClass] = {RC(256, 1, 1, 4), RC(256, 1, 1, 2), RC(256, 1, 1, 1),
                                           RC(512, 1, 1, 1), RC(512, 1, 2, 1), RC(256, 2, 4, 1),
-                                          RC(256, 2, 8, 1)};
+                                          RC(256, 2, 8, 1), RC(512, 4, 8, 1)};
 #undef RC
 
 static int res_class_of(int n) {

@@ -52,7 +52,7 @@
 namespace dpg {
 namespace {
 
-constexpr int kResMaxN = 4096;  // largest system the resident form holds
+constexpr int kResMaxN = 16384;  // largest system the resident form holds
 
 __device__ __forceinline__ unsigned long long global_ns() {
     unsigned long long t;
