@@ -599,7 +599,7 @@ static int run_resident(ES *s, long long guard_limit) {
 }
 
 // ---- the persistent form ----------------------------------------------------
-// AUTO runs the resident form when it holds every system (at most 4096
+// AUTO runs the resident form when it holds every system (at most 16384
 // particles each, shared memory within the device limit), else the grid form:
 // on one GB300 the grid form measured faster than the persistent form both for
 // 16 x 16384 disks (1.62 vs 0.34 FIRE solves/s) and for 32 systems of 64-4096

@@ -174,7 +174,7 @@ class Ensemble:
     def setForm(self, form=FORM_AUTO, threads=0):
         """FORM_GRID (one launch per stage over all systems, a CUDA graph loop),
         FORM_PERSIST (one persistent block per system), FORM_RESIDENT (one
-        block per system holding it on chip, systems of at most 4096
+        block per system holding it on chip, systems of at most 16384
         particles), FORM_AUTO (resident when it holds every system, else grid,
         or the autotuner's choice); threads: the persistent block size (128,
         256, 512; 0 = by system size)."""

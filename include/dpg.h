@@ -554,7 +554,7 @@ int dpg_ensemble_jam(dpg_ensemble e, const dpg_jam_params *p, dpg_ensemble_resul
  *                    offsets and cell lists in shared memory, per-particle
  *                    dynamics in registers) for time-sliced persistent launches;
  *                    FP64 pair arithmetic only verifies double-word states and
- *                    measures finished minimisations; systems of at most 4096
+ *                    measures finished minimisations; systems of at most 16384
  *                    particles, in size classes that run side by side;
  *  DPG_FORM_AUTO     the resident form when it holds every system, else the
  *                    grid form, or the form dpg_ensemble_autotune chose. */
