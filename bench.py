@@ -1,23 +1,24 @@
 """Benchmark: FIRE minimisations of bidisperse disks, N = 16384, phi = 0.86, run
 to max|F_i| <= 1e-13 (the 16384-disk FIRE workload): the mixed-precision
-batched form against the plain FP64 drop-in, plus the per-kernel roofline and
-the CPU baseline.
+batched form against the plain FP64 drop-in and the batched FP64 form, with the
+per-kernel roofline, the CPU baseline and the batched jamming workload.
 
 A solve is one complete FIRE minimisation of one seeded random packing (cell
 list + neighbour list build, initial forces, then FIRE until max|F_i| <= 1e-13).
-A step is one call of the batched form on 8 such systems (8 distinct seeds,
-FP32 pair forces with FP64 accumulation, each system switching to the FP64
-pair arithmetic below max|F| = 1e-7 for the final refinement).
+A step is one call of the batched form on BATCH = 16 such systems (16 distinct
+seeds, FP32 pair forces below which each system refines in double-word FP32
+pairs; FP64 pair arithmetic certifies every reported minimum).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 --impl ours (default): the GB300 library through its C ABI.  `value` = solves/s
 of the batched mixed form with the initial packings resident in HBM; `e2e` =
-the same through host buffers (positions/radii/masses in, positions/forces
-out).  The plain FP64 path (one system per call, bit-identical to the
-reference arithmetic) is timed on the same starts and reported in
-extra.plain_fp64.  L2 (126 MB) is flushed between timed solves (a 512 MiB
-write).
+the first timed batches again through host buffers (positions/radii/masses in,
+positions/forces out).  extra: the plain FP64 path (one system per call,
+bit-identical to the reference arithmetic) and the batched FP64 form on the
+same starts, every mixed minimum re-checked by the FP64 drop-in, the jamming
+ensemble (pressure-band protocol on 64 systems of 64-4096 disks).  L2 (126 MB)
+is flushed between timed solves (a 512 MiB write).  Progress goes to stderr.
 --impl reference: the CPU restatement of the reference algorithm (the oracle,
 oracle/dpg_oracle.c, FP64, OpenMP over all host cores) running full
 minimisations of the same seeds, one per step.  Under torchrun (N > 1) each
