@@ -54,7 +54,7 @@ L2_FLUSH_BYTES = 512 << 20
 BATCH = 16                  # systems per step of the batched form
 CUTOFF, SKIN = 1.7, 0.3     # neighbour cutoff d_max + skin, and the skin
 TUNE_ITERS = 300            # FIRE iterations per autotuner candidate
-FORM_CODES = {"grid": 1, "persist": 2}
+FORM_CODES = {"grid": 1, "persist": 2, "resident": 3}
 SWITCH_FMAX = 1e-6          # mixed systems switch to FP64 pair forces below this max|F|
 PLAIN_SOLVES = 8            # timed solves of the plain FP64 path (after one untimed)
 E2E_BATCHES = 4             # timed batches solved again through host arrays (e2e)
@@ -70,6 +70,11 @@ JAM_FIRE = (0.1, 1e-2, 1e-16, 0.0, 100000, 1e-13)  # alpha0, dt0, PE/N target, n
 JAM_CHECK_STEPS = 20000     # FP64 re-minimisation of a jammed state (already a minimum)
 WARMUP_ITERS = 2000         # FIRE iterations of a warm-up solve
 E_FORCE_DRAM_PER_SYSTEM = 10.37e6 / 8  # ncu DRAM bytes per e_force launch per 16384-disk system
+# ncu DRAM bytes (read + write) per disk of one e_res launch (a time slice of
+# a few thousand iterations): the kernel loads and stores each system's state
+# once per launch, so its traffic grows with the disks, not the iterations
+# (None: not captured)
+E_RES_DRAM_PER_DISK = None
 PROFILE_ITERS = 300
 
 
@@ -333,7 +338,8 @@ def run_ours(args):
     log("warm-up done, headline")
     # ---- headline: mixed precision, BATCH systems per step --------------------
     sampler = ClockSampler(dev.index or 0)
-    results, ev_ms, launches = [], [], 0
+    results, ev_ms = [], []
+    launches0, graph_kernels = sum(e.launchCount() for e, _ in batches), 0
     barrier()
     torch.cuda.synchronize()
     sampler.start()
@@ -342,15 +348,16 @@ def run_ours(args):
         res, ms = timed(lambda: solve_batch(e))
         ev_ms.append(ms)
         results.append(res)
-        iters = max(r["fire_steps"] for r in res)
-        if form == FORM_CODES["persist"]:
-            # one persistent launch per 2^17 iterations
-            launches += 1 + iters // (1 << 17)
-        else:
-            # kernels per iteration of the graph loop: move, force, transition,
-            # guard; 5 rebuild kernels on iterations where any system rebuilt
-            launches += 4 * (iters + 1) + 5 * max(r["rebuilds"] for r in res)
+        if form == FORM_CODES["grid"]:
+            # the graph loop runs its kernels on the device: move, force, its
+            # epilogue, transition (at most) and guard every iteration, 5
+            # rebuild kernels on the iterations where any system rebuilt
+            iters = max(r["fire_steps"] for r in res)
+            graph_kernels += 5 * (iters + 1) + 5 * max(r["rebuilds"] for r in res)
     torch.cuda.synchronize()
+    # the library's own count of the launches it issued (stream and cluster
+    # launches; a graph launch counts once, its kernels are added above)
+    launches = sum(e.launchCount() for e, _ in batches) - launches0 + graph_kernels
     t_wall = time.perf_counter() - t_wall0
     barrier()
     clocks = sampler.stop()
@@ -393,11 +400,19 @@ def run_ours(args):
     mixed_check = fp64_recheck(dpg, sptr, batches, finals, results)
 
     log("roofline")
-    # ---- roofline of the dominant kernel of the headline form, weighted over the
-    # three arithmetics by the share of force passes each took -------------------
+    # ---- roofline of the dominant kernel of the headline form: the resident
+    # kernel over the timed solves, or the grid form's e_force weighted over the
+    # three arithmetics by the share of force passes each took (measured in
+    # either case: the grid form's figure explains the resident form's gain) ---
     peak, peak_src = measured_peak_hbm()
-    roofline = headline_roofline(dpg, sptr, batches, finals, flat, plain["mean_neighbors"], peak,
-                                 peak_src, tune)
+    grid_roofline = headline_roofline(dpg, sptr, batches, finals, flat, plain["mean_neighbors"],
+                                      peak, peak_src, tune)
+    if form == FORM_CODES["resident"]:
+        roofline = resident_roofline(flat, total_ms / world, launches, plain["mean_neighbors"],
+                                     peak, peak_src)
+        roofline["grid_form_e_force"] = grid_roofline
+    else:
+        roofline = grid_roofline
 
     log("large-N and other workloads")
     # ---- large-N force kernel (N = 2^20 NVE, plain FP64) -----------------------
@@ -597,6 +612,35 @@ def headline_roofline(dpg, sptr, batches, finals, flat, k_mean, peak, peak_src, 
                     "FP64 passes by their share of the timed solves' force passes; the working "
                     "set is L2-resident, so the kernel is bound by latency and the FP64 pipe, "
                     "not by HBM"}
+
+
+def resident_roofline(flat, total_ms, launches, k_mean, peak, peak_src):
+    """e_res, the resident form's kernel, over the timed solves.  Its launches
+    (time slices of about 0.2 s, each carrying every system of its size class
+    for as many iterations as fit) fill the timed region, so the launch time is
+    the region's CUDA-event time over the launches (gaps between slices
+    included: the achieved figure is a lower bound).  Algorithmic bytes: a FIRE
+    iteration's compulsory traffic, 144 + 4k per disk (force 48 + 4k; update
+    reads v, F, x, x_ref 64 and writes v, x 32), times the disk-iterations the
+    timed solves ran."""
+    per = 144 + 4 * k_mean
+    disk_iters = float(sum(N_PART * r["fire_steps"] for r in flat))
+    b = disk_iters * per / launches
+    us = total_ms * 1e3 / launches
+    achieved = b / (us * 1e-6) / 1e9
+    traffic = None if E_RES_DRAM_PER_DISK is None else E_RES_DRAM_PER_DISK * BATCH * N_PART
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": traffic,
+            "traffic_source": "ncu dram__bytes_read+write of one e_res launch on 2 x 16384 disks "
+                              "(bench.py --ncu-case resident_headline), scaled by disks",
+            "kernel": "e_res", "peak_source": peak_src, "bytes_per_launch": b,
+            "launch_us": us, "launches": launches, "bytes_per_disk_iteration": per,
+            "us_per_iteration": total_ms * 1e3 / max(r["fire_steps"] for r in flat),
+            "note": f"{BATCH} x 16384 disks, one 8-block cluster per system holding it in shared "
+                    "memory for all its iterations: DRAM carries each system's state once per "
+                    "launch, not once per iteration, so the bound is the iteration's latency "
+                    "(barriers, the double-word dependency chains, remote shared-memory reads), "
+                    "and the fraction is the algorithmic rate of a FIRE iteration against HBM"}
 
 
 def other_configs(dpg, sptr):
@@ -957,6 +1001,19 @@ def ncu_case(which):
         r = e.minimizeFire(FIRE_ALPHA0, FIRE_DT0, 0.0, 0.0, 3000, fmax_target=FMAX)
         print(json.dumps({"ncu_case": which, "steps": max(x["fire_steps"] for x in r)}))
         return
+    if which == "resident_headline":
+        # 2 of the headline's 16384-disk systems, FIRE from their starts for at
+        # most 3000 iterations in the resident form (8-block clusters)
+        from dpcuda_gb300.ensemble import FORM_RESIDENT
+        sts = [packing(sd) for sd in step_seeds(0, 0)[:2]]
+        e = dpg.Ensemble([N_PART] * 2, [st["box"] for st in sts], CUTOFF, SKIN,
+                         precision=dpg.MIXED, switch_fmax=SWITCH_FMAX)
+        e.setForm(FORM_RESIDENT)
+        e.setState(*[np.concatenate([st[c] for st in sts]) for c in ("x", "y", "r", "m")])
+        r = e.minimizeFire(FIRE_ALPHA0, FIRE_DT0, 0.0, 0.0, 3000, fmax_target=FMAX)
+        print(json.dumps({"ncu_case": which, "steps": max(x["fire_steps"] for x in r),
+                          "launches": e.launchCount()}))
+        return
     if which in ("resident_dw_small", "resident_dw_large"):
         # S systems of N disks relaxed to max|F| <= 1e-9, then 1000 FIRE
         # iterations in the double-word phase inside an NVTX range "dw" (the
@@ -1030,8 +1087,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--ncu-case", choices=["fire", "nve_large", "ensemble", "ensemble_forces",
-                                           "bumpy_nve", "resident", "resident_dw_small",
-                                           "resident_dw_large"],
+                                           "bumpy_nve", "resident", "resident_headline",
+                                           "resident_dw_small", "resident_dw_large"],
                     default=None,
                     help="run a small fixed workload for ncu captures and exit")
     ap.add_argument("--batch", type=int, default=BATCH, help="systems per step of the batched form")

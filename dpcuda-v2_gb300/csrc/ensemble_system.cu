@@ -42,6 +42,7 @@ struct dpg_ensemble_system {
     int form = DPG_FORM_AUTO, pthreads = 0;  // execution form and persistent block size
     int max_n = 0;
     bool split_force = false;    // grid form: FP32 and refinement force kernels apart
+    long long launches = 0;      // kernel launches and graph launches issued for this ensemble
     // resident form: one stream per size class, the block -> system lists
     cudaStream_t rs_stream[8] = {};
     cudaEvent_t rs_fork = nullptr, rs_join[8] = {};
@@ -54,6 +55,7 @@ typedef dpg_ensemble_system ES;
     do {                                                          \
         kern<<<(blocks), (threads), 0, s->stream>>>(__VA_ARGS__); \
         CK(cudaGetLastError());                                   \
+        s->launches++;                                            \
     } while (0)
 
 static int ealloc(ES *s, void **p, size_t bytes) {
@@ -383,6 +385,7 @@ static int run(ES *s, long long guard_limit) {
             TRY(put(s, &s->d->h_f32, (unsigned long long)s->h_f32));
             TRY(put(s, &s->d->h_fhi, (unsigned long long)s->h_fhi));
             CK(cudaGraphLaunch(s->exec, s->stream));
+            s->launches++;
             TRY(put(s, &s->d->h_loop, 0ULL));
             TRY(put(s, &s->d->h_rb, 0ULL));
             TRY(put(s, &s->d->h_tr, 0ULL));
@@ -538,6 +541,7 @@ static int launch_resident(ES *s, long long budget, unsigned long long slice_ns,
         const int *blocks = s->d_rs_blocks + first[c];
         EDev *dev = s->d;
         CK(cudaLaunchKernelEx(&cfg, kern, dev, blocks, ncmax, budget, slice_ns));
+        s->launches++;
         CK(cudaEventRecord(s->rs_join[c], s->rs_stream[c]));
         CK(cudaStreamWaitEvent(s->stream, s->rs_join[c], 0));
         (*launched)++;
@@ -656,6 +660,12 @@ static int run_persist(ES *s, long long guard_limit) {
         spent += chunk;
     }
     return set_err(DPG_ERR_STATE, "ensemble loop did not finish");
+}
+
+extern "C" int dpg_ensemble_launch_count(dpg_ensemble s, int64_t *count) {
+    if (!s || !count) return set_err(DPG_ERR_ARG, "null argument");
+    *count = s->launches;
+    return DPG_OK;
 }
 
 extern "C" int dpg_ensemble_set_form(dpg_ensemble s, int form, int threads) {

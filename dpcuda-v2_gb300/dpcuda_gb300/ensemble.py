@@ -171,6 +171,12 @@ class Ensemble:
         return {"move_us": avg[0], "rebuild_us": avg[1], "force_us": avg[2], "transition_us": avg[3],
                 "iters": cnt[0], "rebuilds": cnt[1], "force_passes": cnt[2]}
 
+    def launchCount(self):
+        """Kernel launches (a CUDA-graph launch counting as one) issued so far."""
+        n = C.c_int64()
+        check(self.lib.dpg_ensemble_launch_count(self.h, C.byref(n)))
+        return n.value
+
     def setForm(self, form=FORM_AUTO, threads=0):
         """FORM_GRID (one launch per stage over all systems, a CUDA graph loop),
         FORM_PERSIST (one persistent block per system), FORM_RESIDENT (one

@@ -157,6 +157,7 @@ SIGNATURES = {
     "dpg_autotune_force_group": [VP, I32, C.POINTER(I32), DP],
     "dpg_disk_forces_noalloc": [VP, VP, VP, I64, D, D, D, D, D, VP, VP, VP, VP],
     "dpg_measure_fma_peak": [I32, I32, DP, DP],
+    "dpg_ensemble_launch_count": [VP, I64P],
     "dpg_ensemble_create": [C.POINTER(EnsembleParams), I64P, DP, VP, C.POINTER(VP)],
     "dpg_ensemble_destroy": [VP],
     "dpg_ensemble_set_state": [VP, DP, DP, DP, DP],

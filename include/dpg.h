@@ -564,6 +564,10 @@ int dpg_ensemble_jam(dpg_ensemble e, const dpg_jam_params *p, dpg_ensemble_resul
 #define DPG_FORM_RESIDENT 3
 /* threads: persistent form's threads per system block (128, 256 or 512; 0 = by size) */
 int dpg_ensemble_set_form(dpg_ensemble e, int form, int threads);
+/* Launches the host has issued for this ensemble so far (no reference
+ * counterpart; a measurement hook): every kernel launch, and a CUDA-graph
+ * launch as one (the grid form's loop runs its kernels inside one graph). */
+int dpg_ensemble_launch_count(dpg_ensemble e, int64_t *count);
 
 typedef struct {
     int form;                  /* chosen form (DPG_FORM_GRID / _PERSIST / _RESIDENT) */

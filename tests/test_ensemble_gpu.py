@@ -184,3 +184,23 @@ def test_autotune_restores_positions_and_picks_a_form(dpg):
     res = e.minimizeFire(0.1, 1e-2, 0.0, 0.0, 1_000_000, fmax_target=1e-12)
     assert all(r["converged"] == 1 and r["max_force"] <= 1e-12 for r in res)
     e.close()
+
+
+def test_launch_count_follows_the_forms(dpg):
+    """dpg_ensemble_launch_count: the resident form issues one launch per size
+    class and time slice, the grid form one graph launch per loop segment
+    (2^24 iterations), so a short solve of three size classes costs three
+    resident launches and one graph launch."""
+    from dpcuda_gb300.ensemble import FORM_GRID, FORM_RESIDENT
+    sts = packings([100, 600, 3000], 0.86, 40)
+    for form, expect in ((FORM_RESIDENT, 3), (FORM_GRID, 1)):
+        e = make(dpg, sts, dpg.MIXED, form=form)
+        e.minimizeFire(0.1, 1e-2, 0.0, 0.0, 50, fmax_target=1e-13)
+        n0 = e.launchCount()
+        e.setState(np.concatenate([s["x"] for s in sts]), np.concatenate([s["y"] for s in sts]),
+                   np.concatenate([s["r"] for s in sts]), np.concatenate([s["m"] for s in sts]))
+        e.minimizeFire(0.1, 1e-2, 0.0, 0.0, 200, fmax_target=1e-13)
+        issued = e.launchCount() - n0
+        e.close()
+        assert issued >= expect
+        assert issued < expect + 12   # plus the setup kernels of one solve
