@@ -73,8 +73,7 @@ E_FORCE_DRAM_PER_SYSTEM = 10.37e6 / 8  # ncu DRAM bytes per e_force launch per 1
 # ncu DRAM bytes (read + write) per disk of one e_res launch (a time slice of
 # a few thousand iterations): the kernel loads and stores each system's state
 # once per launch, so its traffic grows with the disks, not the iterations
-# (None: not captured)
-E_RES_DRAM_PER_DISK = None
+E_RES_DRAM_PER_DISK = (4868864 + 40192) / (2 * 16384)
 PROFILE_ITERS = 300
 
 
@@ -390,7 +389,7 @@ def run_ours(args):
     # ---- the plain FP64 drop-in on the first PLAIN_SOLVES starts (one per call)
     # and the batched FP64 form on the same starts -----------------------------
     plain = plain_fp64_leg(dpg, sptr, batches[0][1][:PLAIN_SOLVES + 1], timed)
-    batched64 = batched_fp64_leg(dpg, sptr, batches[0][1][1:PLAIN_SOLVES + 1], timed, form, tune)
+    batched64 = batched_fp64_leg(dpg, sptr, batches[0][1][1:PLAIN_SOLVES + 1], timed)
 
     log("FP64 re-check of the mixed minima")
     # ---- error of the mixed form: every timed minimum re-evaluated by the FP64
@@ -408,8 +407,8 @@ def run_ours(args):
     grid_roofline = headline_roofline(dpg, sptr, batches, finals, flat, plain["mean_neighbors"],
                                       peak, peak_src, tune)
     if form == FORM_CODES["resident"]:
-        roofline = resident_roofline(flat, total_ms / world, launches, plain["mean_neighbors"],
-                                     peak, peak_src)
+        roofline = resident_roofline(results, total_ms / world, launches,
+                                     plain["mean_neighbors"], peak, peak_src)
         roofline["grid_form_e_force"] = grid_roofline
     else:
         roofline = grid_roofline
@@ -520,14 +519,17 @@ def plain_fp64_leg(dpg, sptr, sts, timed):
     return out
 
 
-def batched_fp64_leg(dpg, sptr, sts, timed, form, tune):
+def batched_fp64_leg(dpg, sptr, sts, timed):
     """The batched form in FP64 pair arithmetic on the starts the plain leg timed
     (one call for all of them): the batching part of the headline's gain,
-    apart from the precision part."""
+    apart from the precision part.  The grid form: at 16384 disks its FP64 pass
+    spreads over every SM (measured 0.387 solves/s for 8 systems), while the
+    resident form runs a system's FP64 pairs on its own 8-block cluster (0.219)."""
+    from dpcuda_gb300.ensemble import FORM_GRID
     n = len(sts)
     e = dpg.Ensemble([N_PART] * n, [st["box"] for st in sts], CUTOFF, SKIN,
                      precision=dpg.FP64, stream=sptr)
-    e.setForm(form, tune["threads"])
+    e.setForm(FORM_GRID)
     host = [np.concatenate([st[c] for st in sts]) for c in ("x", "y", "r", "m")]
     e.setState(*host)
     e.minimizeFire(FIRE_ALPHA0, FIRE_DT0, 0.0, 0.0, 200, fmax_target=FMAX)   # graph build
@@ -536,6 +538,7 @@ def batched_fp64_leg(dpg, sptr, sts, timed, form, tune):
                                            fmax_target=FMAX))
     e.close()
     return {"value": n / (ms / 1e3), "unit": "FIRE solves/s", "systems": n, "dtype": "f64",
+            "form": "grid",
             "all_converged": all(r["converged"] and r["max_force"] <= FMAX for r in res),
             "fire_iterations_mean": float(np.mean([r["fire_steps"] for r in res])),
             "sample": "the starts the plain FP64 leg timed, in one batched call"}
@@ -614,7 +617,7 @@ def headline_roofline(dpg, sptr, batches, finals, flat, k_mean, peak, peak_src, 
                     "not by HBM"}
 
 
-def resident_roofline(flat, total_ms, launches, k_mean, peak, peak_src):
+def resident_roofline(results, total_ms, launches, k_mean, peak, peak_src):
     """e_res, the resident form's kernel, over the timed solves.  Its launches
     (time slices of about 0.2 s, each carrying every system of its size class
     for as many iterations as fit) fill the timed region, so the launch time is
@@ -624,7 +627,10 @@ def resident_roofline(flat, total_ms, launches, k_mean, peak, peak_src):
     reads v, F, x, x_ref 64 and writes v, x 32), times the disk-iterations the
     timed solves ran."""
     per = 144 + 4 * k_mean
+    flat = [r for res in results for r in res]
     disk_iters = float(sum(N_PART * r["fire_steps"] for r in flat))
+    # a batch runs as long as its slowest system: iterations of the timed region
+    region_iters = float(sum(max(r["fire_steps"] for r in res) for res in results))
     b = disk_iters * per / launches
     us = total_ms * 1e3 / launches
     achieved = b / (us * 1e-6) / 1e9
@@ -635,7 +641,7 @@ def resident_roofline(flat, total_ms, launches, k_mean, peak, peak_src):
                               "(bench.py --ncu-case resident_headline), scaled by disks",
             "kernel": "e_res", "peak_source": peak_src, "bytes_per_launch": b,
             "launch_us": us, "launches": launches, "bytes_per_disk_iteration": per,
-            "us_per_iteration": total_ms * 1e3 / max(r["fire_steps"] for r in flat),
+            "us_per_iteration": total_ms * 1e3 / region_iters,
             "note": f"{BATCH} x 16384 disks, one 8-block cluster per system holding it in shared "
                     "memory for all its iterations: DRAM carries each system's state once per "
                     "launch, not once per iteration, so the bound is the iteration's latency "
@@ -943,25 +949,42 @@ def fire_ensemble(args):
         e.close()
     # the plain FP64 drop-in, one system per call, on the ensemble's systems in
     # order until 30 s of solving have passed (a sample of the same workload)
-    done, t_tot, n_tot = 0, 0.0, 0
+    done, t_tot, n_tot, conv = 0, 0.0, 0, []
     for k in range(S):
         st = sts[k]
         s = dpg.Disk(int(sizes[k]), st["box"])
         s.setState(st["x"], st["y"], None, None, st["r"], st["m"])
         s.setupNeighbors("cell", CUT_MULT, 0.2, 8.0, 0.5)
         t0 = time.perf_counter()
-        dpg.minimizeFire(s, FIRE_ALPHA0, FIRE_DT0, 0.0, 0.0, 10**6, fmax_target=FMAX)
+        r = dpg.minimizeFire(s, FIRE_ALPHA0, FIRE_DT0, 0.0, 0.0, 10**6, fmax_target=FMAX)
         s.synchronize()
         t_tot += time.perf_counter() - t0
+        conv.append(bool(r["converged"]))
         n_tot += int(sizes[k])
         done += 1
         s.close()
         if t_tot > 30:
             break
+    # the mixed batched form on exactly the systems the plain path solved, so
+    # that the two rates compare the same starts
+    sub = [np.concatenate([st[c] for st in sts[:done]]) for c in ("x", "y", "r", "m")]
+    e = dpg.Ensemble(sizes[:done], [st["box"] for st in sts[:done]], CUTOFF, SKIN,
+                     precision=dpg.MIXED, switch_fmax=SWITCH_FMAX)
+    e.setState(*sub)
+    e.minimizeFire(FIRE_ALPHA0, FIRE_DT0, 0.0, 0.0, 50, fmax_target=FMAX)
+    e.setState(*sub)
+    t0 = time.perf_counter()
+    r = e.minimizeFire(FIRE_ALPHA0, FIRE_DT0, 0.0, 0.0, 10**6, fmax_target=FMAX)
+    t_mixed = time.perf_counter() - t0
+    e.close()
     print(json.dumps({"metric": "batched FIRE solves/s, uneven ensemble", "form": "plain_fp64",
                       "systems": done, "particles": n_tot, "s": t_tot,
-                      "systems_per_s": done / t_tot,
-                      "sample": f"the first {done} of the {S} systems, one per call"}), flush=True)
+                      "systems_per_s": done / t_tot, "converged": int(sum(conv)),
+                      "sample": f"the first {done} of the {S} systems, one per call",
+                      "mixed_batched_same_systems": {
+                          "s": t_mixed, "systems_per_s": done / t_mixed,
+                          "converged": int(sum(x["converged"] for x in r)),
+                          "over_plain_fp64": t_tot / t_mixed}}), flush=True)
 
 
 def ncu_case(which):
@@ -970,7 +993,10 @@ def ncu_case(which):
     'nve_large' = 8 NVE steps of the 2^20-disk system, 'ensemble' = 64 FIRE
     iterations of the batched mixed form on 16 x 16384 disks, 'bumpy_nve' =
     192 NVE steps of 4096 rigid bumpy bodies, 'resident' = 3000 FIRE
-    iterations of 16 uneven systems in the resident form."""
+    iterations of 16 uneven systems in the resident form, 'resident_headline'
+    = 3000 FIRE iterations of 2 of the headline's 16384-disk systems in the
+    resident form, 'resident_dw_small' / 'resident_dw_large' = 1000
+    double-word FIRE iterations of 48 x 128 / 8 x 4096 disks."""
     os.environ["DPG_LOOP_MODE"] = "stream"
     import dpcuda_gb300 as dpg
     if which == "bumpy_nve":
