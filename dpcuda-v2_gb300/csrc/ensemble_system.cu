@@ -202,11 +202,43 @@ extern "C" int dpg_ensemble_create(const dpg_ensemble_params *p, const int64_t *
     return DPG_OK;
 }
 
+// Slot order of each system: its particles sorted by the row-major index of
+// the cell holding their position (a stable counting sort), so that
+// consecutive slots -- each block of the grid form, each block of a resident
+// cluster -- cover a compact stripe of the box and most of a particle's
+// neighbours sit in its own block.  Input order is restored on the way out
+// (e_get reads the same map).
+static void order_slots(ES *s, const double *x, const double *y) {
+    std::vector<int> key, start;
+    size_t in = 0;
+    for (int k = 0; k < s->S; k++) {
+        const ESys &Y = s->sys[k];
+        const int n = Y.n, nc = Y.ncd;
+        const double L = Y.L, inv = nc / L;
+        auto cell = [&](double v) {
+            double w = v - L * std::floor(v / L);  // wrapped into [0, L)
+            if (!(w >= 0.0 && w < L)) w = 0.0;      // non-finite input: any cell
+            return std::min((int)(w * inv), nc - 1);
+        };
+        key.resize(n);
+        start.assign((size_t)nc * nc + 1, 0);
+        for (int i = 0; i < n; i++) {
+            key[i] = cell(y[in + i]) * nc + cell(x[in + i]);
+            start[key[i] + 1]++;
+        }
+        for (int c = 0; c < nc * nc; c++) start[c + 1] += start[c];
+        for (int i = 0; i < n; i++) s->src_index[Y.off + start[key[i]]++] = (int)(in + i);
+        in += n;
+    }
+}
+
 extern "C" int dpg_ensemble_set_state(dpg_ensemble s, const double *x, const double *y,
                                       const double *radii, const double *masses) {
     if (!s || !x || !y || !radii || !masses) return set_err(DPG_ERR_ARG, "null argument");
     const size_t n = s->n_total;
     const double *src[4] = {x, y, radii, masses};
+    order_slots(s, x, y);
+    CK(cudaMemcpyAsync(s->d_src, s->src_index.data(), 4 * (size_t)s->T, cudaMemcpyHostToDevice, s->stream));
     for (int k = 0; k < 4; k++)
         CK(cudaMemcpyAsync(s->xfer + k * n, src[k], 8 * n, cudaMemcpyHostToDevice, s->stream));
     LAUNCH(e_put, (s->T + 255) / 256, 256, s->d, s->xfer, s->xfer + n, s->xfer + 2 * n, s->xfer + 3 * n, s->d_src);

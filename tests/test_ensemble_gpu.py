@@ -204,3 +204,31 @@ def test_launch_count_follows_the_forms(dpg):
         e.close()
         assert issued >= expect
         assert issued < expect + 12   # plus the setup kernels of one solve
+
+
+def test_state_round_trips_in_input_order(dpg):
+    """setState orders each system's slots by cell (a spatial sort); getState
+    returns positions in the caller's order, bit for bit (unwrapped
+    coordinates included), and a force pass's forces follow the same order."""
+    sts = packings([70, 1000, 4000], 0.86, 60)
+    rng = np.random.default_rng(5)
+    shifted = [dict(st, x=st["x"] + st["box"] * rng.integers(-2, 3, len(st["x"])))
+               for st in sts]
+    e = make(dpg, shifted, dpg.FP64)
+    out = e.getState()
+    e.close()
+    assert np.array_equal(out["x"], np.concatenate([s["x"] for s in shifted]))
+    assert np.array_equal(out["y"], np.concatenate([s["y"] for s in shifted]))
+    e = make(dpg, sts, dpg.FP64)
+    e.calculateForces(dpg.FP64)
+    got = e.getState()
+    for k, st in enumerate(sts):
+        s = single(dpg, st)
+        s.zeroForceAndPotentialEnergy()
+        s.calculateForces()
+        want = s.getState()
+        s.close()
+        scale = np.abs(want["fx"]).max()
+        for c in ("fx", "fy"):
+            np.testing.assert_allclose(split(e, got[c])[k], want[c], rtol=0, atol=1e-12 * scale)
+    e.close()
