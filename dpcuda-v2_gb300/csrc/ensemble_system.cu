@@ -46,6 +46,8 @@ struct dpg_ensemble_system {
     // resident form: one stream per size class, the block -> system lists
     cudaStream_t rs_stream[8] = {};
     cudaEvent_t rs_fork = nullptr, rs_join[8] = {};
+    int rs_fit[8] = {};          // clusters of each class the GPU holds at once (0: not yet asked)
+    int rs_rot[8] = {};          // rotation of each class's systems between launches
     int *d_rs_blocks = nullptr;
 };
 
@@ -520,8 +522,29 @@ static bool res_fits(const ES *s) {
 }
 
 
+// one cluster of K.c blocks per system, nb systems
+static cudaLaunchConfig_t res_config(const RClass &K, int nb, size_t smem, cudaStream_t st,
+                                     cudaLaunchAttribute *attr) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(nb * K.c);
+    cfg.blockDim = dim3(K.nt);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = K.c;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cfg;
+}
+
 // Launch every class that has live systems, each on its own stream (forked
 // from and joined back into the ensemble's stream).  slice_ns bounds a launch.
+// A launch carries at most as many systems of a class as the GPU holds
+// clusters of it at once (cudaOccupancyMaxActiveClusters): more would run as a
+// second wave after the first wave's time slice, on a mostly idle GPU.  The
+// class's systems take turns, rotating between launches.
 static int launch_resident(ES *s, long long budget, unsigned long long slice_ns, int *launched) {
     *launched = 0;
     std::vector<int> order[kNClass];
@@ -532,12 +555,36 @@ static int launch_resident(ES *s, long long budget, unsigned long long slice_ns,
     }
     std::vector<int> flat;
     int first[kNClass];
+    size_t smem[kNClass];
+    int ncmax[kNClass];
     for (int c = 0; c < kNClass; c++) {
+        first[c] = (int)flat.size();
+        if (order[c].empty()) continue;
+        const RClass &K = kRClasses[c];
+        ncmax[c] = res_ncmax(s, c);
+        smem[c] = res_smem_bytes(K.per_block(), K.capacity(), ncmax[c]);
+        CK(cudaFuncSetAttribute((const void *)K.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem[c]));
+        if (!s->rs_fit[c]) {
+            cudaLaunchAttribute attr[1];
+            const cudaLaunchConfig_t cfg = res_config(K, (int)order[c].size(), smem[c], s->stream, attr);
+            int fit = 0;
+            if (cudaOccupancyMaxActiveClusters(&fit, (const void *)K.fn, &cfg) != cudaSuccess || fit <= 0) {
+                (void)cudaGetLastError();
+                fit = 1 << 30;  // unknown: no cap
+            }
+            s->rs_fit[c] = fit;
+        }
         // largest systems first: they start before the small ones fill the SMs
         std::sort(order[c].begin(), order[c].end(), [&](int a, int b) {
             return s->sys[a].n != s->sys[b].n ? s->sys[a].n > s->sys[b].n : a < b;
         });
-        first[c] = (int)flat.size();
+        const int nb = (int)order[c].size();
+        if (nb > s->rs_fit[c]) {
+            const int rot = s->rs_rot[c] % nb;
+            std::rotate(order[c].begin(), order[c].begin() + rot, order[c].end());
+            order[c].resize(s->rs_fit[c]);
+            s->rs_rot[c] = (int)(((long long)rot + s->rs_fit[c]) % nb);
+        }
         flat.insert(flat.end(), order[c].begin(), order[c].end());
     }
     if (flat.empty()) return DPG_OK;
@@ -552,27 +599,13 @@ static int launch_resident(ES *s, long long budget, unsigned long long slice_ns,
             CK(cudaEventCreateWithFlags(&s->rs_join[c], cudaEventDisableTiming));
         }
         const RClass &K = kRClasses[c];
-        const int ncmax = res_ncmax(s, c);
-        const size_t smem = res_smem_bytes(K.per_block(), K.capacity(), ncmax);
         res_kernel_fn kern = K.fn;
-        CK(cudaFuncSetAttribute((const void *)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         CK(cudaStreamWaitEvent(s->rs_stream[c], s->rs_fork, 0));
-        // one cluster of K.c blocks per system
-        cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3(nb * K.c);
-        cfg.blockDim = dim3(K.nt);
-        cfg.dynamicSmemBytes = smem;
-        cfg.stream = s->rs_stream[c];
         cudaLaunchAttribute attr[1];
-        attr[0].id = cudaLaunchAttributeClusterDimension;
-        attr[0].val.clusterDim.x = K.c;
-        attr[0].val.clusterDim.y = 1;
-        attr[0].val.clusterDim.z = 1;
-        cfg.attrs = attr;
-        cfg.numAttrs = 1;
+        const cudaLaunchConfig_t cfg = res_config(K, nb, smem[c], s->rs_stream[c], attr);
         const int *blocks = s->d_rs_blocks + first[c];
         EDev *dev = s->d;
-        CK(cudaLaunchKernelEx(&cfg, kern, dev, blocks, ncmax, budget, slice_ns));
+        CK(cudaLaunchKernelEx(&cfg, kern, dev, blocks, ncmax[c], budget, slice_ns));
         s->launches++;
         CK(cudaEventRecord(s->rs_join[c], s->rs_stream[c]));
         CK(cudaStreamWaitEvent(s->stream, s->rs_join[c], 0));
