@@ -73,7 +73,7 @@ E_FORCE_DRAM_PER_SYSTEM = 10.37e6 / 8  # ncu DRAM bytes per e_force launch per 1
 # ncu DRAM bytes (read + write) per disk of one e_res launch (a time slice of
 # a few thousand iterations): the kernel loads and stores each system's state
 # once per launch, so its traffic grows with the disks, not the iterations
-E_RES_DRAM_PER_DISK = (4868864 + 40192) / (2 * 16384)
+E_RES_DRAM_PER_DISK = (4019456 + 39680) / (2 * 16384)
 PROFILE_ITERS = 300
 
 
