@@ -669,11 +669,12 @@ static int run_resident(ES *s, long long guard_limit) {
 
 // ---- the persistent form ----------------------------------------------------
 // AUTO runs the resident form when it holds every system (at most 16384
-// particles each, shared memory within the device limit), else the grid form:
-// on one GB300 the grid form measured faster than the persistent form both for
-// 16 x 16384 disks (1.62 vs 0.34 FIRE solves/s) and for 32 systems of 64-4096
-// disks (3.5e8 vs 3.0e8 particle-iterations/s, 512-thread blocks).
-// dpg_ensemble_autotune measures and may choose any of them.
+// particles each, shared memory within the device limit), else the grid form.
+// Measured on one GB300, FIRE of 16 x 16384 disks to max|F| <= 1e-13: resident
+// 4.86 solves/s, grid 1.50, persistent below 0.4; for 32 systems of 64-4096
+// disks the grid form ran 3.5e8 particle-iterations/s against the persistent
+// form's 3.0e8 (512-thread blocks).  dpg_ensemble_autotune measures and may
+// choose any of them.
 static int form_of(const ES *s) {
     if (s->form != DPG_FORM_AUTO) return s->form;
     return res_fits(s) ? DPG_FORM_RESIDENT : DPG_FORM_GRID;

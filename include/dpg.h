@@ -550,12 +550,14 @@ int dpg_ensemble_jam(dpg_ensemble e, const dpg_jam_params *p, dpg_ensemble_resul
  *  DPG_FORM_PERSIST  one persistent block per system runs its whole
  *                    minimisation / jamming protocol with no further launches
  *                    (no grid-wide synchronisation; each system at its own pace);
- *  DPG_FORM_RESIDENT one block per system holds the system on chip (packed
+ *  DPG_FORM_RESIDENT one block or cluster per system holds the system on chip (packed
  *                    offsets and cell lists in shared memory, per-particle
  *                    dynamics in registers) for time-sliced persistent launches;
  *                    FP64 pair arithmetic only verifies double-word states and
  *                    measures finished minimisations; systems of at most 16384
- *                    particles, in size classes that run side by side;
+ *                    particles, in size classes that run side by side, each
+ *                    launch carrying as many clusters of a class as the GPU
+ *                    holds at once (the class's systems take turns);
  *  DPG_FORM_AUTO     the resident form when it holds every system, else the
  *                    grid form, or the form dpg_ensemble_autotune chose. */
 #define DPG_FORM_AUTO 0
