@@ -110,8 +110,11 @@ def workload_config():
                      "f_inc": 1.1, "f_dec": 0.5, "f_alpha": 0.99, "n_min": 5},
             "neighbors": {"method": "cell", "cutoff": "d_max + skin", "skin": "0.3, or the "
                           "autotuner's 0.225 / 0.15 (extra.autotune)", "particles_per_cell": 8},
-            "form": f"mixed precision (FP32 pairs, FP64 accumulation, FP64 pair refinement "
-                    f"below max|F| = {SWITCH_FMAX:g}), {BATCH} systems per step",
+            "form": f"mixed precision, {BATCH} systems per step, the execution form the "
+                    f"autotuner picks (extra.autotune): resident form = FP32 pairs, then "
+                    f"double-word FP32 pairs below max|F| = {SWITCH_FMAX:g}, FP64 passes only "
+                    f"to certify a minimum and to measure it; grid form = FP32 pairs, then "
+                    f"double-word / FP64 pairs below the same max|F|",
             "l2": "flushed between steps (512 MiB write)",
             "warmup_kind": f"bounded solves of {WARMUP_ITERS} FIRE iterations over the timed batches",
             "e2e_steps": "the same batches as the timed steps, solved again from host arrays",
